@@ -1,0 +1,196 @@
+"""Generate the golden fixtures in this folder by running PARLA 0.1.4 itself.
+
+Run in a container that holds the reference source tree::
+
+    python tests/golden/make_golden.py /root/reference
+
+The reference targets NumPy 1.x; two names it uses were removed in NumPy 2
+(``np.NaN`` and ``np.row_stack``), so they are restored as aliases before the
+import.  Nothing is written into the reference tree (bytecode is disabled).
+
+Each fixture stores the seeded inputs together with the reference outputs, so
+the tests that read them never need the reference itself.  Library versions
+are recorded because NumPy Generator streams and LAPACK results can change
+between releases.
+"""
+import os
+import sys
+import warnings
+
+import numpy as np
+import scipy
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def _import_reference(path):
+    sys.dont_write_bytecode = True
+    np.NaN = np.nan
+    np.row_stack = np.vstack
+    sys.path.insert(0, path)
+    import parla  # noqa: F401
+    return parla
+
+
+def _ls_problem(m, n, log_cond, noise, seed):
+    """A = U diag(s) V' with logspaced s, b = A x* + noise * unit r_perp."""
+    rng = np.random.default_rng(seed)
+    g = rng.standard_normal((m, n))
+    U, _ = np.linalg.qr(g)
+    V, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    s = np.logspace(0, -log_cond, n)
+    A = (U * s) @ V.T
+    x = rng.standard_normal(n)
+    r = rng.standard_normal(m)
+    r -= U @ (U.T @ r)
+    r /= np.linalg.norm(r)
+    b = A @ x + noise * r
+    return A, b
+
+
+def sketches(parla):
+    import parla.utils.sketching as usk
+    out = {}
+    out['ga_wide'] = usk.gaussian_operator(12, 50, np.random.default_rng(11))
+    out['ga_tall'] = usk.gaussian_operator(50, 7, np.random.default_rng(12))
+    out['ga_raw'] = usk.gaussian_operator(6, 9, np.random.default_rng(10),
+                                          normalize=False)
+    out['sj_wide'] = usk.sjlt_operator(16, 64, np.random.default_rng(13), 8).toarray()
+    out['sj_tall'] = usk.sjlt_operator(64, 16, np.random.default_rng(14), 8).toarray()
+    out['sj_nnz3'] = usk.sjlt_operator(20, 300, np.random.default_rng(21), 3).toarray()
+    with warnings.catch_warnings():
+        warnings.simplefilter('ignore')
+        out['sj_repl'] = usk.sjlt_operator(5, 30, np.random.default_rng(15), 8).toarray()
+    rng = np.random.default_rng(16)
+    r, e, perm = usk.generate_srct(16, 100, rng)
+    out['srct_r'], out['srct_e'], out['srct_perm'] = r, e, perm
+    mat = np.random.default_rng(17).standard_normal((100, 5))
+    out['srct_in'] = mat
+    out['srct_fwd'] = usk.apply_srct(r, e, mat, perm)
+    small = np.random.default_rng(18).standard_normal((16, 5))
+    out['srct_adj_in'] = small
+    out['srct_adj'] = usk.apply_srct(r, e, small, perm, forward=False)
+    out['srct_vec'] = usk.apply_srct(r, e, mat[:, 0], perm)
+    op = usk.srct_operator(24, 120, np.random.default_rng(22))
+    m2 = np.random.default_rng(23).standard_normal((120, 3))
+    out['srct_op_in'] = m2
+    out['srct_op_out'] = op @ m2
+    out['on_tall'] = usk.orthonormal_operator(40, 10, np.random.default_rng(19))
+    out['on_wide'] = usk.orthonormal_operator(10, 40, np.random.default_rng(20))
+    return out
+
+
+def lsqr_case(parla):
+    from parla.comps.determiter.lsqr import lsqr
+    from scipy.sparse.linalg import aslinearoperator
+    A, b = _ls_problem(60, 8, 3, 1e-2, 31)
+    out = {'A': A, 'b': b}
+    for tag, kw in (('plain', dict(atol=1e-12, btol=1e-12, iter_lim=50)),
+                    ('lim3', dict(atol=1e-12, btol=1e-12, iter_lim=3)),
+                    ('damp', dict(damp=0.3, atol=1e-10, btol=1e-10, iter_lim=50)),
+                    ('x0', dict(atol=1e-12, btol=1e-12, iter_lim=50,
+                                x0=np.ones(8)))):
+        res = lsqr(aslinearoperator(A), b, **kw)
+        out[f'{tag}_x'] = res[0]
+        out[f'{tag}_istop'] = np.array(res[1])
+        out[f'{tag}_itn'] = np.array(res[2])
+        out[f'{tag}_arnorms'] = np.asarray(res[7])
+    return out
+
+
+def spo_cases(parla):
+    import parla.comps.sketchers.oblivious as sko
+    from parla.drivers.least_squares import SPO, SSO1
+    A, b = _ls_problem(400, 20, 6, 1e-6, 41)
+    out = {'A': A, 'b': b}
+    gens = {'ga': sko.SkOpGA(), 'sj': sko.SkOpSJ(8), 'tc': sko.SkOpTC()}
+    seed = 100
+    for gname, gen in gens.items():
+        for mode in ('qr', 'chol', 'svd'):
+            seed += 1
+            alg = SPO(gen, 4, mode)
+            x, log = alg(A, b, 0.0, 1e-12, 100, np.random.default_rng(seed))
+            out[f'{gname}_{mode}_seed'] = np.array(seed)
+            out[f'{gname}_{mode}_x'] = x
+            out[f'{gname}_{mode}_errors'] = log.errors
+    x, log = SPO(sko.SkOpGA(), 3, 'qr')(A, b, 0.25, 1e-12, 100,
+                                         np.random.default_rng(7))
+    out['ridge_x'], out['ridge_errors'] = x, log.errors
+    with warnings.catch_warnings():
+        warnings.simplefilter('ignore')
+        x, _ = SSO1(sko.SkOpSJ(8), 3, 'gelsd')(A, b, 0.0, np.nan, 1,
+                                               np.random.default_rng(9))
+    out['sso_x'] = x
+    return out
+
+
+def lowrank_cases(parla):
+    import parla.comps.sketchers.oblivious as sko
+    from parla.comps.sketchers.aware import RS1
+    from parla.comps.rangefinders import RF1
+    from parla.comps.qb import QB1
+    from parla.drivers.svd import SVD1
+    from parla.drivers.evd import EVD1, EVD2
+    import parla.utils.linalg_wrappers as law
+    rng = np.random.default_rng(51)
+    m, n = 120, 60
+    U, _ = np.linalg.qr(rng.standard_normal((m, n)))
+    V, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    s = np.arange(1, n + 1, dtype=float) ** -1.5 + 1e-3
+    A = (U * s) @ V.T
+    out = {'A': A}
+    for p in range(4):
+        rs = RS1(sko.SkOpGA(), p, law.orth, 1)
+        out[f'rs1_p{p}'] = rs(A, 10, np.random.default_rng(60 + p))
+    rs = RS1(sko.SkOpGA(), 4, law.orth, 2)
+    out['rs1_p4_s2'] = rs(A, 10, np.random.default_rng(65))
+    rf = RF1(RS1(sko.SkOpGA(), 2, law.orth, 1))
+    with warnings.catch_warnings():
+        warnings.simplefilter('ignore')
+        out['rf1_Q'] = rf(A, 12, np.nan, np.random.default_rng(70))
+    qb = QB1(rf)
+    out['qb1_Q'], out['qb1_B'] = qb(A, 12, np.nan, np.random.default_rng(71))
+    with warnings.catch_warnings():
+        warnings.simplefilter('ignore')
+        U1, s1, Vh1 = SVD1(qb)(A, 10, np.nan, 5, np.random.default_rng(72))
+    out['svd1_U'], out['svd1_s'], out['svd1_Vh'] = U1, s1, Vh1
+    # symmetric and PSD inputs for the eigensolvers
+    W, _ = np.linalg.qr(rng.standard_normal((80, 80)))
+    lam = np.linspace(1, 80, 80) ** -1.0 * np.where(np.arange(80) % 3 == 0, -1, 1)
+    Asym = (W * lam) @ W.T
+    Asym = 0.5 * (Asym + Asym.T)
+    out['Asym'] = Asym
+    with warnings.catch_warnings():
+        warnings.simplefilter('ignore')
+        V1, l1 = EVD1(qb)(Asym, 10, np.nan, 4, np.random.default_rng(73))
+    out['evd1_V'], out['evd1_lamb'] = V1, l1
+    lam_psd = np.exp(-np.arange(80) / 6.0)
+    Apsd = (W * lam_psd) @ W.T
+    Apsd = 0.5 * (Apsd + Apsd.T)
+    out['Apsd'] = Apsd
+    with warnings.catch_warnings():
+        warnings.simplefilter('ignore')
+        V2, l2 = EVD2(RS1(sko.SkOpGA(), 0, law.orth, 1))(Apsd, 12, np.nan, 4,
+                                                         np.random.default_rng(74))
+        V3, l3 = EVD2(RS1(sko.SkOpGA(), 2, law.orth, 1))(Apsd, 12, np.nan, 4,
+                                                         np.random.default_rng(75))
+    out['evd2_V'], out['evd2_lamb'] = V2, l2
+    out['evd2p2_V'], out['evd2p2_lamb'] = V3, l3
+    return out
+
+
+def main(ref_path):
+    parla = _import_reference(ref_path)
+    meta = dict(numpy=np.__version__, scipy=scipy.__version__,
+                parla=parla.__version__)
+    for name, fn in (('sketch', sketches), ('lsqr', lsqr_case),
+                     ('spo', spo_cases), ('lowrank', lowrank_cases)):
+        data = fn(parla)
+        data['_versions'] = np.array(repr(meta))
+        path = os.path.join(HERE, f'{name}.npz')
+        np.savez_compressed(path, **data)
+        print('wrote', path, sum(v.nbytes for v in data.values()), 'bytes')
+
+
+if __name__ == '__main__':
+    main(sys.argv[1] if len(sys.argv) > 1 else '/root/reference')
