@@ -1,0 +1,194 @@
+/*
+ * rla_gb300.h -- C ABI of librla_gb300.so, the GB300 (sm_103a) kernels behind
+ * the randomized-linear-algebra hot path of PARLA 0.1.4 (sketching operators,
+ * sketch-and-precondition least squares, RS1/RF1/QB1/SVD1, EVD1/EVD2).
+ *
+ * Conventions
+ *   - Every entry point returns an rla_status (0 = RLA_OK) and never throws.
+ *   - Matrices are row-major (NumPy C order) with an explicit leading
+ *     dimension (row stride, in elements).  Pointers are caller-owned device
+ *     pointers unless stated otherwise.
+ *   - `stream` is a cudaStream_t (NULL = legacy default stream); work is
+ *     enqueued asynchronously unless a function says it synchronises.
+ *   - Functions that need scratch memory take (void* ws, size_t* ws_bytes):
+ *     call once with ws == NULL to receive the size in *ws_bytes, then again
+ *     with a buffer of at least that size (LAPACK-style two-call query).
+ *   - No global mutable state except the per-device tcgen05 function
+ *     attributes, set once under a mutex.
+ *
+ * Each declaration names the reference interface (file:line inside the
+ * PARLA source tree) that the entry point replaces.
+ */
+#ifndef RLA_GB300_H
+#define RLA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* rla_stream_t;
+
+enum rla_status {
+  RLA_OK = 0,
+  RLA_ERR_ARG = 1,         /* bad size, pointer or enum                     */
+  RLA_ERR_CUDA = 2,        /* CUDA runtime error; see rla_last_cuda_error() */
+  RLA_ERR_NOT_SPD = 3,     /* Cholesky met a non-positive pivot             */
+  RLA_ERR_MAXITER = 4,     /* iteration limit reached (informational)       */
+  RLA_ERR_NONFINITE = 5,   /* NaN/Inf met in input or iterate               */
+  RLA_ERR_UNSUPPORTED = 6, /* shape or mode not implemented                 */
+  RLA_ERR_TIMEOUT = 7,     /* a bounded device wait gave up                 */
+  RLA_ERR_WORKSPACE = 8    /* workspace missing or too small                */
+};
+
+enum rla_dtype {
+  RLA_F64 = 0,  /* IEEE binary64 storage and arithmetic ("plain FP64")      */
+  RLA_F32 = 1,  /* IEEE binary32                                            */
+  RLA_BF16 = 2, /* bfloat16 storage (tensor-core operands)                  */
+  RLA_DF = 3    /* binary64 storage, double-float (FP32 pair) arithmetic    */
+};
+
+/* ------------------------------------------------------------ library */
+const char* rla_status_string(int status);
+const char* rla_last_cuda_error(void);
+int rla_abi_version(void);
+
+/* ------------------------------------------------------- sketch operators */
+
+/* Dense Gaussian operator: S[i*lds+j] = scale * N(0,1) from a counter-based
+ * Philox4x32-10 stream keyed by `seed` (element index i*cols+j).  dtype
+ * RLA_F64, RLA_F32 or RLA_BF16.  Device-side replacement of
+ * gaussian_operator, parla/utils/sketching.py:20-31 (SkOpGA,
+ * parla/comps/sketchers/oblivious.py:38-45). */
+int rla_gaussian_fill(int dtype, int64_t rows, int64_t cols, uint64_t seed,
+                      double scale, void* S, int64_t lds, rla_stream_t stream);
+
+/* SJLT pattern for a wide d x m operator: for every column j, `nnz` distinct
+ * rows rows[j*nnz + t] in [0, d) and signs[j*nnz + t] in {-1, +1}; the value
+ * of each nonzero is sign / sqrt(nnz).  Device-side replacement of the
+ * per-column sampling loop of sjlt_operator, parla/utils/sketching.py:55-71.
+ * Requires nnz <= d. */
+int rla_sjlt_pattern(int64_t d, int64_t m, int nnz, uint64_t seed,
+                     int32_t* rows, int8_t* signs, rla_stream_t stream);
+
+/* Y (d x n) = S A for a wide SJLT S (d x m) given as (rows, signs) with
+ * `nnz` entries per column, each of value sign*scale.  Accumulation is exact
+ * 64-bit fixed point per column tile, so results do not depend on the order
+ * of the scatter.  dtype RLA_F64 or RLA_F32 (same type for A and Y).
+ * Replaces the CSC product `S @ A` (parla/utils/sketching.py:73-74 and
+ * parla/drivers/least_squares.py:303) for S from SkOpSJ. */
+int rla_sjlt_apply(int dtype, int64_t d, int64_t m, int64_t n, int nnz,
+                   const int32_t* rows, const int8_t* signs, double scale,
+                   const void* A, int64_t lda, void* Y, int64_t ldy, void* ws,
+                   size_t* ws_bytes, rla_stream_t stream);
+
+/* Y (m x k) = A S for a tall SJLT S (n x k) stored as the transpose of a wide
+ * k x n pattern (rows index the k columns of S).  dtype RLA_F64 or RLA_F32.
+ * Replaces `A @ S` for a CSR S from sjlt_operator's tall branch,
+ * parla/utils/sketching.py:75-79 (used by RS1, parla/comps/sketchers/aware.py:164). */
+int rla_sjlt_apply_right(int dtype, int64_t m, int64_t n, int64_t k, int nnz,
+                         const int32_t* rows, const int8_t* signs, double scale,
+                         const void* A, int64_t lda, void* Y, int64_t ldy,
+                         rla_stream_t stream);
+
+/* SRCT: Y (d x n) = (DCT-II_ortho(diag(e) A[perm, :]))[r, :], m = rows of A.
+ * r: d distinct row indices, e: m signed scales, perm: permutation of [0,m)
+ * (NULL for identity).  FP64 storage; dtype RLA_F64.  Replaces apply_srct's
+ * forward branch, parla/utils/sketching.py:148-161 (SkOpTC). */
+int rla_srct_apply(int dtype, int64_t d, int64_t m, int64_t n, const int64_t* r,
+                   const double* e, const int64_t* perm, const double* A,
+                   int64_t lda, double* Y, int64_t ldy, void* ws,
+                   size_t* ws_bytes, rla_stream_t stream);
+
+/* --------------------------------------------------------------- GEMM */
+
+/* C = alpha op(A) op(B) + beta C on CUDA cores (SIMT), row-major.
+ * op(A) is M x K (A is K x M when transa), op(B) is K x N (B is N x K when
+ * transb).  dtype RLA_F64, RLA_F32 or RLA_DF (FP64 storage, double-float
+ * arithmetic).  Uses split-K through `ws` when the output is small.
+ * Replaces the dense products of the reference path: `A @ S` / `A.T @ S`
+ * (parla/comps/sketchers/aware.py:175,179), `Q.T @ A` (parla/comps/qb.py:351),
+ * `Q @ U` (parla/drivers/svd.py:175), `S @ A` (parla/drivers/least_squares.py:303). */
+int rla_gemm(int dtype, int transa, int transb, int64_t M, int64_t N, int64_t K,
+             double alpha, const void* A, int64_t lda, const void* B,
+             int64_t ldb, double beta, void* C, int64_t ldc, void* ws,
+             size_t* ws_bytes, rla_stream_t stream);
+
+/* ------------------------------------------------- small dense factorizations */
+
+/* Householder QR of the first n columns of A (m x (n + nrhs), m >= n),
+ * COLUMN-major (LAPACK layout, column stride lda), in place: R in the upper
+ * triangle, reflector vectors (unit leading entry implied) below it, scalars
+ * in tau[n] (device).  The nrhs trailing columns are overwritten by Q^T times
+ * themselves, which yields Q^T b for the sketch-and-solve presolve.  dtype
+ * RLA_F64 or RLA_DF.  Cooperative launch over all SMs with a bounded grid
+ * barrier between columns.  Replaces la.qr(A_ske) and Q[:d].T @ b_ske at
+ * parla/drivers/least_squares.py:311,315. */
+int rla_geqrf(int dtype, int64_t m, int64_t n, int64_t nrhs, double* A,
+              int64_t lda, double* tau, void* ws, size_t* ws_bytes,
+              rla_stream_t stream);
+
+/* Q (m x n, column-major) = thin orthonormal factor of rla_geqrf's result.
+ * Replaces la.qr(Y)[0] at parla/comps/rangefinders.py:187 and orth,
+ * parla/utils/linalg_wrappers.py:6-7. */
+int rla_orgqr(int dtype, int64_t m, int64_t n, const double* QR, int64_t ldqr,
+              const double* tau, double* Q, int64_t ldq, void* ws,
+              size_t* ws_bytes, rla_stream_t stream);
+
+/* Upper Cholesky factor in place (row-major): G = R^T R, R in the upper
+ * triangle, strict lower triangle zeroed.  dtype RLA_F64, RLA_F32 (float
+ * storage) or RLA_DF.  *info (device int) = 0 on success, j+1 if pivot j was
+ * not positive.  Replaces la.cholesky at parla/drivers/least_squares.py:324
+ * and parla/drivers/evd.py:370. */
+int rla_potrf_upper(int dtype, int64_t n, void* G, int64_t ldg, int* info,
+                    void* ws, size_t* ws_bytes, rla_stream_t stream);
+
+/* X = R^-1 for an upper-triangular R (n x n, row-major), out of place
+ * (X must not alias R).  dtype RLA_F64, RLA_F32 or RLA_DF.  Lets LSQR apply
+ * R^-1 as a product, replacing solve_triangular at
+ * parla/comps/preconditioning.py:28,37,40-41. */
+int rla_trtri_upper(int dtype, int64_t n, const void* R, int64_t ldr, void* X,
+                    int64_t ldx, rla_stream_t stream);
+
+/* ------------------------------------------------------------- LSQR */
+
+/* Preconditioned LSQR on Abar = [A; sqrt_delta I] M, run as one cooperative
+ * kernel.  A (m x n) row-major; M (n x p) dense row-major (R^-1 for the
+ * 'qr'/'chol' preconditioners, V/sigma for 'svd').  dtype RLA_F64 reads A;
+ * dtype RLA_DF reads A_hi/A_lo (rla_split_f64 planes, row stride lda) and
+ * computes in double-float.  z (p, device): start point on entry when
+ * has_x0, LSQR iterate on exit; the caller forms x = M z.  arnorms (HOST
+ * array of iter_lim doubles) receives the per-iteration ||Abar' r||
+ * estimates, itn/istop (host) the iteration count and Paige-Saunders stop
+ * code.  Synchronises `stream`.  Replaces lsqr,
+ * parla/comps/determiter/lsqr.py:98-574, with the operator of
+ * a_lift_precond, parla/comps/preconditioning.py:16-67, as called by PcSS2,
+ * parla/comps/determiter/saddle.py:266-280. */
+int rla_lsqr_run(int dtype, int64_t m, int64_t n, int64_t p, const double* A,
+                 const float* A_hi, const float* A_lo, int64_t lda,
+                 const double* M, int64_t ldm, double sqrt_delta,
+                 const double* b, double* z, int has_x0, double atol,
+                 double btol, double conlim, int iter_lim, double* arnorms,
+                 int* itn, int* istop, void* ws, size_t* ws_bytes,
+                 rla_stream_t stream);
+
+/* ------------------------------------------------- elementwise helpers */
+
+/* y (rows x cols, dst dtype) = convert(x (rows x cols, src dtype)), optional
+ * transpose (y is cols x rows).  Types RLA_F64, RLA_F32, RLA_BF16. */
+int rla_convert(int src_dtype, int dst_dtype, int transpose, int64_t rows,
+                int64_t cols, const void* x, int64_t ldx, void* y, int64_t ldy,
+                rla_stream_t stream);
+
+/* hi (float) + lo (float) = x (double) to about 2^-48 relative; the planes
+ * share the row stride ldh.  Prepares A for the double-float LSQR and GEMM
+ * paths (no reference counterpart: GB300-specific data layout). */
+int rla_split_f64(int64_t rows, int64_t cols, const double* x, int64_t ldx,
+                  float* hi, float* lo, int64_t ldh, rla_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RLA_GB300_H */

@@ -1,0 +1,270 @@
+"""Thin typed wrappers over the C ABI, operating on torch CUDA tensors.
+
+PyTorch supplies device memory and the current stream; every numerical
+operation below is one of the library's own kernels.
+"""
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import RLA_BF16, RLA_DF, RLA_F32, RLA_F64, call, size_query
+
+_TORCH_CODE = {torch.float64: RLA_F64, torch.float32: RLA_F32, torch.bfloat16: RLA_BF16}
+
+
+class _Stats:
+    """Launch accounting and optional per-entry-point CUDA-event timing.
+
+    ``launches`` counts the library's kernel launches (a claim used by the
+    benchmark); when ``timing`` is on, each wrapped call is bracketed by CUDA
+    events on the current stream and the pairs are kept in ``events``.
+    """
+
+    def __init__(self):
+        self.launches = 0
+        self.timing = False
+        self.events = []
+
+    def reset(self):
+        self.launches = 0
+        self.events = []
+
+
+STATS = _Stats()
+
+
+def _timed(name, n_launch, fn, *args):
+    STATS.launches += n_launch
+    if not STATS.timing:
+        return fn(*args)
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    out = fn(*args)
+    e.record()
+    STATS.events.append((name, s, e))
+    return out
+
+
+MODES = {"f64": RLA_F64, "f32": RLA_F32, "df": RLA_DF}
+
+
+def device():
+    if not torch.cuda.is_available():
+        raise RuntimeError("parla_gb300 needs a CUDA device (GB300 / sm_103a); none is visible")
+    return torch.device("cuda", torch.cuda.current_device())
+
+
+def stream():
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def ptr(t):
+    return C.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def to_dev(x, dtype=torch.float64):
+    """numpy or torch -> contiguous CUDA tensor of `dtype` (no copy if already so)."""
+    dev = device()
+    if isinstance(x, torch.Tensor):
+        return x.to(device=dev, dtype=dtype).contiguous()
+    arr = np.ascontiguousarray(np.asarray(x))
+    return torch.from_numpy(arr).to(device=dev, dtype=dtype, non_blocking=False).contiguous()
+
+
+def like_input(t, ref):
+    """Return a numpy array when the user passed numpy, else the tensor."""
+    if isinstance(ref, torch.Tensor):
+        return t
+    return t.detach().cpu().numpy()
+
+
+def workspace(nbytes):
+    return torch.empty(max(int(nbytes), 1), dtype=torch.uint8, device=device())
+
+
+def _ld(t):
+    return t.stride(0) if t.dim() == 2 else 1
+
+
+# ------------------------------------------------------------------ GEMM
+def gemm(A, B, transa=False, transb=False, alpha=1.0, beta=0.0, out=None, mode=None):
+    """out = alpha op(A) op(B) + beta out with the library's SIMT GEMM.
+
+    mode: 'f64' | 'f32' | 'df' (double-float arithmetic on FP64 storage);
+    default from A's dtype.
+    """
+    if mode is None:
+        mode = "f32" if A.dtype == torch.float32 else "f64"
+    code = MODES[mode]
+    tdt = torch.float32 if code == RLA_F32 else torch.float64
+    A2 = A if A.dim() == 2 else A.reshape(-1, 1)
+    B2 = B if B.dim() == 2 else B.reshape(-1, 1)
+    assert A2.dtype == tdt and B2.dtype == tdt and A2.is_contiguous() and B2.is_contiguous()
+    M = A2.shape[1] if transa else A2.shape[0]
+    K = A2.shape[0] if transa else A2.shape[1]
+    N = B2.shape[0] if transb else B2.shape[1]
+    Kb = B2.shape[1] if transb else B2.shape[0]
+    if K != Kb:
+        raise ValueError(f"gemm: inner dimensions differ ({K} vs {Kb})")
+    if out is None:
+        out = torch.empty((M, N), dtype=tdt, device=A.device)
+        beta = 0.0
+    args = (code, int(transa), int(transb), M, N, K, float(alpha), ptr(A2), _ld(A2), ptr(B2), _ld(B2),
+            float(beta), ptr(out), _ld(out))
+    need = size_query("rla_gemm", *args)
+    ws = workspace(need) if need else None
+    nb = C.c_size_t(need)
+    tag = f"gemm_{mode}"
+    _timed(tag, 2 if need else 1, call, "rla_gemm", *args, ptr(ws) if ws is not None else None,
+           C.byref(nb) if ws is not None else None, stream())
+    if B.dim() == 1 and not transb:
+        return out.reshape(-1)
+    return out
+
+
+# ------------------------------------------------------------- sketches
+def gaussian_fill(rows, cols, seed, scale, dtype=torch.float64):
+    S = torch.empty((rows, cols), dtype=dtype, device=device())
+    _timed("gaussian_fill", 1, call, "rla_gaussian_fill", _TORCH_CODE[dtype], rows, cols, C.c_uint64(seed), float(scale), ptr(S), cols, stream())
+    return S
+
+
+def sjlt_pattern(d, m, nnz, seed):
+    rows = torch.empty(m * nnz, dtype=torch.int32, device=device())
+    signs = torch.empty(m * nnz, dtype=torch.int8, device=device())
+    _timed("sjlt_pattern", 1, call, "rla_sjlt_pattern", d, m, nnz, C.c_uint64(seed), ptr(rows), ptr(signs), stream())
+    return rows, signs
+
+
+def sjlt_apply(rows, signs, nnz, d, A, scale):
+    """Y (d x n) = S A for a wide SJLT pattern; A is (m x n) or (m,)."""
+    vec = A.dim() == 1
+    A2 = A.reshape(-1, 1) if vec else A
+    m, n = A2.shape
+    code = _TORCH_CODE[A2.dtype]
+    Y = torch.empty((d, n), dtype=A2.dtype, device=A2.device)
+    head = (code, d, m, n, nnz, ptr(rows), ptr(signs), float(scale), ptr(A2), _ld(A2), ptr(Y), n)
+    need = size_query("rla_sjlt_apply", *head)
+    ws = workspace(need)
+    nb = C.c_size_t(need)
+    _timed("sjlt_apply", 2, call, "rla_sjlt_apply", *head, ptr(ws), C.byref(nb), stream())
+    return Y.reshape(-1) if vec else Y
+
+
+def sjlt_apply_right(rows, signs, nnz, k, A, scale):
+    """Y (m x k) = A S for a tall SJLT (n x k) given by a wide k x n pattern."""
+    m, n = A.shape
+    Y = torch.empty((m, k), dtype=A.dtype, device=A.device)
+    _timed("sjlt_apply_right", 1, call, "rla_sjlt_apply_right", _TORCH_CODE[A.dtype], m, n, k, nnz, ptr(rows), ptr(signs), float(scale),
+         ptr(A), _ld(A), ptr(Y), k, stream())
+    return Y
+
+
+def srct_apply(r, e, perm, A, mode="f64"):
+    vec = A.dim() == 1
+    A2 = A.reshape(-1, 1) if vec else A
+    m, n = A2.shape
+    d = r.numel()
+    Y = torch.empty((d, n), dtype=torch.float64, device=A2.device)
+    head = (MODES[mode], d, m, n, ptr(r), ptr(e), ptr(perm), ptr(A2), _ld(A2), ptr(Y), n)
+    need = size_query("rla_srct_apply", *head)
+    ws = workspace(need)
+    nb = C.c_size_t(need)
+    _timed("srct_apply", 4, call, "rla_srct_apply", *head, ptr(ws), C.byref(nb), stream())
+    return Y.reshape(-1) if vec else Y
+
+
+# ---------------------------------------------------------- factorizations
+def geqrf_colmajor(T, n, mode="f64"):
+    """Householder QR of the column-major matrix stored as T ((n+nrhs) x m).
+
+    On return T[:n, :n].T's upper triangle is R and T[n:, :n] holds Q^T of the
+    extra columns.  Returns tau.
+    """
+    ncols, m = T.shape
+    nrhs = ncols - n
+    tau = torch.empty(max(n, 1), dtype=torch.float64, device=T.device)
+    head = (MODES[mode], m, n, nrhs, ptr(T), T.stride(0))
+    need = size_query("rla_geqrf", *head, ptr(tau))
+    ws = workspace(need)
+    nb = C.c_size_t(need)
+    _timed("geqrf", 1, call, "rla_geqrf", *head, ptr(tau), ptr(ws), C.byref(nb), stream())
+    return tau
+
+
+def orgqr_colmajor(T, n, tau, mode="f64"):
+    """Thin Q (column-major, returned as n x m row-major = Q^T) from geqrf output."""
+    m = T.shape[1]
+    Qt = torch.empty((n, m), dtype=torch.float64, device=T.device)
+    head = (MODES[mode], m, n, ptr(T), T.stride(0), ptr(tau), ptr(Qt), m)
+    need = size_query("rla_orgqr", *head)
+    ws = workspace(need)
+    nb = C.c_size_t(need)
+    _timed("orgqr", 1, call, "rla_orgqr", *head, ptr(ws), C.byref(nb), stream())
+    return Qt
+
+
+def potrf_upper(G, mode=None):
+    """In-place upper Cholesky of G (row-major).  Raises RlaError(NOT_SPD)."""
+    if mode is None:
+        mode = "f32" if G.dtype == torch.float32 else "f64"
+    n = G.shape[0]
+    info = torch.zeros(1, dtype=torch.int32, device=G.device)
+    head = (MODES[mode], n, ptr(G), G.stride(0), ptr(info))
+    need = size_query("rla_potrf_upper", *head)
+    ws = workspace(need)
+    nb = C.c_size_t(need)
+    _timed("potrf", 1, call, "rla_potrf_upper", *head, ptr(ws), C.byref(nb), stream())
+    bad = int(info.item())
+    if bad:
+        raise _lib.RlaError("rla_potrf_upper", 3, f"pivot {bad - 1} not positive")
+    return G
+
+
+def trtri_upper(R, mode=None):
+    if mode is None:
+        mode = "f32" if R.dtype == torch.float32 else "f64"
+    n = R.shape[0]
+    X = torch.empty_like(R)
+    _timed("trtri", 1, call, "rla_trtri_upper", MODES[mode], n, ptr(R), R.stride(0), ptr(X), X.stride(0), stream())
+    return X
+
+
+def split_f64(A):
+    m, n = A.shape
+    hi = torch.empty((m, n), dtype=torch.float32, device=A.device)
+    lo = torch.empty((m, n), dtype=torch.float32, device=A.device)
+    _timed("split_f64", 1, call, "rla_split_f64", m, n, ptr(A), A.stride(0), ptr(hi), ptr(lo), n, stream())
+    return hi, lo
+
+
+def convert(x, dtype, transpose=False):
+    rows, cols = x.shape
+    y = torch.empty((cols, rows) if transpose else (rows, cols), dtype=dtype, device=x.device)
+    _timed("convert", 1, call, "rla_convert", _TORCH_CODE[x.dtype], _TORCH_CODE[dtype], int(transpose), rows, cols, ptr(x),
+         x.stride(0), ptr(y), y.stride(0), stream())
+    return y
+
+
+def lsqr_run(A, M, b, z0, sqrt_delta, atol, btol, conlim, iter_lim, mode="f64", split=None):
+    """Device LSQR on [A; sd I] M.  Returns (z, istop, itn, arnorms)."""
+    m, n = A.shape
+    p = M.shape[1]
+    z = torch.zeros(p, dtype=torch.float64, device=A.device) if z0 is None else z0.clone().contiguous()
+    arn = np.zeros(max(iter_lim, 1), dtype=np.float64)
+    itn = C.c_int(0)
+    istop = C.c_int(0)
+    code = MODES[mode]
+    hi, lo = split if split is not None else (None, None)
+    if code == RLA_DF and split is None:
+        hi, lo = split_f64(A)
+    head = (code, m, n, p, ptr(A), ptr(hi), ptr(lo), A.stride(0), ptr(M), M.stride(0), float(sqrt_delta),
+            ptr(b), ptr(z), int(z0 is not None), float(atol), float(btol), float(conlim), int(iter_lim),
+            arn.ctypes.data_as(C.c_void_p), C.byref(itn), C.byref(istop))
+    need = size_query("rla_lsqr_run", *head)
+    ws = workspace(need)
+    nb = C.c_size_t(need)
+    _timed("lsqr", 1, call, "rla_lsqr_run", *head, ptr(ws), C.byref(nb), stream())
+    return z, istop.value, itn.value, arn[:itn.value].copy()

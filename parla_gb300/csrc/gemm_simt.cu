@@ -1,0 +1,270 @@
+// SIMT GEMM on the CUDA cores: C = alpha op(A) op(B) + beta C, row-major.
+//
+// Three arithmetic policies share one tiled kernel:
+//   F32  - binary32 in/out/accumulate (the plain FP32 path of RSVD),
+//   F64  - binary64 (the plain FP64 path; GB300 runs FP64 at ~1.2 TFLOP/s),
+//   DF   - binary64 storage, double-float accumulation on the FP32 pipes
+//          (~48-bit accurate; the FP64-class path used where a sketch or a
+//          Gram matrix must resolve directions far below FP32 precision).
+// Small outputs use split-K: each z-slice writes a partial tile into the
+// workspace and a second kernel sums the slices in a fixed order, so results
+// are deterministic.
+#include "common.cuh"
+
+namespace rla {
+namespace {
+
+struct PolF32 {
+  using In = float; using Sm = float; using Acc = float; using Part = float; using Out = float;
+  static constexpr int BM = 128, BN = 128, BK = 8, TM = 8, TN = 8;
+  __device__ static Sm cvt(In v) { return v; }
+  __device__ static Sm zero() { return 0.f; }
+  __device__ static Acc acc0() { return 0.f; }
+  __device__ static void madd(Acc& c, Sm a, Sm b) { c = fmaf(a, b, c); }
+  __device__ static void renorm(Acc&) {}
+  __device__ static Part part(Acc c) { return c; }
+  __device__ static Out out(Acc c, double alpha, double beta, const Out* cold) {
+    float r = static_cast<float>(alpha) * c;
+    if (beta != 0.0) r = fmaf(static_cast<float>(beta), *cold, r);
+    return r;
+  }
+};
+
+struct PolF64 {
+  using In = double; using Sm = double; using Acc = double; using Part = double; using Out = double;
+  static constexpr int BM = 64, BN = 64, BK = 8, TM = 4, TN = 4;
+  __device__ static Sm cvt(In v) { return v; }
+  __device__ static Sm zero() { return 0.0; }
+  __device__ static Acc acc0() { return 0.0; }
+  __device__ static void madd(Acc& c, Sm a, Sm b) { c = fma(a, b, c); }
+  __device__ static void renorm(Acc&) {}
+  __device__ static Part part(Acc c) { return c; }
+  __device__ static Out out(Acc c, double alpha, double beta, const Out* cold) {
+    double r = alpha * c;
+    if (beta != 0.0) r = fma(beta, *cold, r);
+    return r;
+  }
+};
+
+struct PolDF {
+  using In = double; using Sm = df; using Acc = df; using Part = double; using Out = double;
+  static constexpr int BM = 64, BN = 64, BK = 8, TM = 4, TN = 4;
+  __device__ static Sm cvt(In v) { return df_from_double(v); }
+  __device__ static Sm zero() { return df{0.f, 0.f}; }
+  __device__ static Acc acc0() { return df{0.f, 0.f}; }
+  // acc += a*b: exact product (two_prod + cross terms), two_sum into hi, lazy lo.
+  __device__ static void madd(Acc& c, Sm a, Sm b) {
+    float p = a.hi * b.hi;
+    float pe = fmaf(a.hi, b.hi, -p);
+    pe = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, pe));
+    float s = c.hi + p;
+    float bb = s - c.hi;
+    float e = (c.hi - (s - bb)) + (p - bb);
+    c.hi = s;
+    c.lo += e + pe;
+  }
+  __device__ static void renorm(Acc& c) { c = quick_two_sum(c.hi, c.lo); }
+  __device__ static Part part(Acc c) { return df_to_double(c); }
+  __device__ static Out out(Acc c, double alpha, double beta, const Out* cold) {
+    double r = alpha * df_to_double(c);
+    if (beta != 0.0) r = fma(beta, *cold, r);
+    return r;
+  }
+};
+
+template <class P, bool TA, bool TB>
+__global__ void __launch_bounds__((P::BM / P::TM) * (P::BN / P::TN))
+gemm_tile_kernel(int64_t M, int64_t N, int64_t K, int64_t kchunk, double alpha,
+                 const typename P::In* __restrict__ A, int64_t lda,
+                 const typename P::In* __restrict__ B, int64_t ldb, double beta,
+                 typename P::Out* __restrict__ C, int64_t ldc,
+                 typename P::Part* __restrict__ part) {
+  constexpr int BM = P::BM, BN = P::BN, BK = P::BK, TM = P::TM, TN = P::TN;
+  constexpr int TX = BN / TN, TY = BM / TM, NT = TX * TY;
+  constexpr int LA = BM * BK / NT, LB = BN * BK / NT;
+  using Sm = typename P::Sm;
+  __shared__ Sm As[BK][BM];
+  __shared__ Sm Bs[BK][BN];
+
+  const int tid = threadIdx.x, tx = tid % TX, ty = tid / TX;
+  const int64_t m0 = static_cast<int64_t>(blockIdx.y) * BM;
+  const int64_t n0 = static_cast<int64_t>(blockIdx.x) * BN;
+  const int64_t kb = static_cast<int64_t>(blockIdx.z) * kchunk;
+  const int64_t ke = min(K, kb + kchunk);
+
+  typename P::Acc acc[TM][TN];
+#pragma unroll
+  for (int i = 0; i < TM; ++i)
+#pragma unroll
+    for (int j = 0; j < TN; ++j) acc[i][j] = P::acc0();
+
+  Sm ra[LA], rb[LB];
+  auto load = [&](int64_t k0) {
+#pragma unroll
+    for (int r = 0; r < LA; ++r) {
+      int e = tid + r * NT;
+      int i, k;
+      if (TA) { k = e / BM; i = e % BM; } else { i = e / BK; k = e % BK; }
+      int64_t gi = m0 + i, gk = k0 + k;
+      bool ok = gi < M && gk < ke;
+      ra[r] = ok ? P::cvt(TA ? A[gk * lda + gi] : A[gi * lda + gk]) : P::zero();
+    }
+#pragma unroll
+    for (int r = 0; r < LB; ++r) {
+      int e = tid + r * NT;
+      int j, k;
+      if (TB) { j = e / BK; k = e % BK; } else { k = e / BN; j = e % BN; }
+      int64_t gj = n0 + j, gk = k0 + k;
+      bool ok = gj < N && gk < ke;
+      rb[r] = ok ? P::cvt(TB ? B[gj * ldb + gk] : B[gk * ldb + gj]) : P::zero();
+    }
+  };
+  auto stash = [&]() {
+#pragma unroll
+    for (int r = 0; r < LA; ++r) {
+      int e = tid + r * NT;
+      int i, k;
+      if (TA) { k = e / BM; i = e % BM; } else { i = e / BK; k = e % BK; }
+      As[k][i] = ra[r];
+    }
+#pragma unroll
+    for (int r = 0; r < LB; ++r) {
+      int e = tid + r * NT;
+      int j, k;
+      if (TB) { j = e / BK; k = e % BK; } else { k = e / BN; j = e % BN; }
+      Bs[k][j] = rb[r];
+    }
+  };
+
+  if (kb < ke) load(kb);
+  for (int64_t k0 = kb; k0 < ke; k0 += BK) {
+    __syncthreads();
+    stash();
+    __syncthreads();
+    if (k0 + BK < ke) load(k0 + BK);
+#pragma unroll
+    for (int k = 0; k < BK; ++k) {
+      Sm a[TM], b[TN];
+#pragma unroll
+      for (int i = 0; i < TM; ++i) a[i] = As[k][ty + i * TY];
+#pragma unroll
+      for (int j = 0; j < TN; ++j) b[j] = Bs[k][tx + j * TX];
+#pragma unroll
+      for (int i = 0; i < TM; ++i)
+#pragma unroll
+        for (int j = 0; j < TN; ++j) P::madd(acc[i][j], a[i], b[j]);
+    }
+#pragma unroll
+    for (int i = 0; i < TM; ++i)
+#pragma unroll
+      for (int j = 0; j < TN; ++j) P::renorm(acc[i][j]);
+  }
+
+#pragma unroll
+  for (int i = 0; i < TM; ++i) {
+    int64_t gi = m0 + ty + i * TY;
+    if (gi >= M) continue;
+#pragma unroll
+    for (int j = 0; j < TN; ++j) {
+      int64_t gj = n0 + tx + j * TX;
+      if (gj >= N) continue;
+      if (part) {
+        part[(static_cast<int64_t>(blockIdx.z) * M + gi) * N + gj] = P::part(acc[i][j]);
+      } else {
+        typename P::Out* c = C + gi * ldc + gj;
+        *c = P::out(acc[i][j], alpha, beta, c);
+      }
+    }
+  }
+}
+
+template <typename Part, typename Out>
+__global__ void splitk_reduce_kernel(int64_t M, int64_t N, int splits, double alpha,
+                                     const Part* __restrict__ part, double beta,
+                                     Out* __restrict__ C, int64_t ldc) {
+  int64_t idx = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= M * N) return;
+  int64_t i = idx / N, j = idx % N;
+  double s = 0.0;
+  for (int z = 0; z < splits; ++z) s += static_cast<double>(part[(static_cast<int64_t>(z) * M + i) * N + j]);
+  double r = alpha * s;
+  if (beta != 0.0) r += beta * static_cast<double>(C[i * ldc + j]);
+  C[i * ldc + j] = static_cast<Out>(r);
+}
+
+template <class P>
+int gemm_launch(int ta, int tb, int64_t M, int64_t N, int64_t K, double alpha,
+                const void* A, int64_t lda, const void* B, int64_t ldb, double beta,
+                void* C, int64_t ldc, void* ws, size_t* ws_bytes, cudaStream_t st) {
+  using In = typename P::In;
+  using Out = typename P::Out;
+  using Part = typename P::Part;
+  const int64_t tiles_m = ceil_div(M, P::BM), tiles_n = ceil_div(N, P::BN);
+  const int64_t tiles = tiles_m * tiles_n;
+  int splits = 1;
+  const int sms = sm_count();
+  if (tiles < 2 * sms && K >= 512) {
+    int64_t want = ceil_div(2 * sms, tiles);
+    int64_t cap = K / 256;
+    splits = static_cast<int>(imax(1, imin(want, imin(cap, 64))));
+  }
+  size_t need = splits > 1 ? static_cast<size_t>(splits) * M * N * sizeof(Part) : 0;
+  if (ws == nullptr && ws_bytes != nullptr) {  // size query
+    *ws_bytes = need;
+    return RLA_OK;
+  }
+  if (splits > 1) {
+    size_t have = ws_bytes ? *ws_bytes : 0;
+    if (ws == nullptr || have < need) {
+      // fit as many slices as the caller's buffer holds
+      int64_t fit = ws ? static_cast<int64_t>(have / (static_cast<size_t>(M) * N * sizeof(Part))) : 0;
+      splits = static_cast<int>(imax(1, imin(fit, splits)));
+    }
+  }
+  if (M == 0 || N == 0) return RLA_OK;
+  const int64_t kchunk = ceil_div(ceil_div(imax(K, 1), splits), P::BK) * P::BK;
+  splits = static_cast<int>(imax(1, ceil_div(imax(K, 1), kchunk)));
+  dim3 grid(static_cast<unsigned>(tiles_n), static_cast<unsigned>(tiles_m), static_cast<unsigned>(splits));
+  dim3 block((P::BM / P::TM) * (P::BN / P::TN));
+  Part* part = splits > 1 ? static_cast<Part*>(ws) : nullptr;
+  auto* a = static_cast<const In*>(A);
+  auto* b = static_cast<const In*>(B);
+  auto* c = static_cast<Out*>(C);
+#define RLA_GEMM_CASE(TA_, TB_) \
+  gemm_tile_kernel<P, TA_, TB_><<<grid, block, 0, st>>>(M, N, K, kchunk, alpha, a, lda, b, ldb, beta, c, ldc, part)
+  if (ta && tb) RLA_GEMM_CASE(true, true);
+  else if (ta) RLA_GEMM_CASE(true, false);
+  else if (tb) RLA_GEMM_CASE(false, true);
+  else RLA_GEMM_CASE(false, false);
+#undef RLA_GEMM_CASE
+  RLA_LAUNCH_CHECK();
+  if (splits > 1) {
+    int64_t total = M * N;
+    splitk_reduce_kernel<Part, Out><<<static_cast<unsigned>(ceil_div(total, 256)), 256, 0, st>>>(
+        M, N, splits, alpha, part, beta, c, ldc);
+    RLA_LAUNCH_CHECK();
+  }
+  return RLA_OK;
+}
+
+}  // namespace
+}  // namespace rla
+
+extern "C" int rla_gemm(int dtype, int transa, int transb, int64_t M, int64_t N, int64_t K,
+                        double alpha, const void* A, int64_t lda, const void* B, int64_t ldb,
+                        double beta, void* C, int64_t ldc, void* ws, size_t* ws_bytes,
+                        rla_stream_t stream) {
+  if (M < 0 || N < 0 || K < 0) return RLA_ERR_ARG;
+  const bool query = (ws == nullptr && ws_bytes != nullptr);
+  if (!query) {
+    if ((M > 0 && N > 0) && (C == nullptr)) return RLA_ERR_ARG;
+    if (K > 0 && M > 0 && N > 0 && (A == nullptr || B == nullptr)) return RLA_ERR_ARG;
+  }
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  switch (dtype) {
+    case RLA_F32: return rla::gemm_launch<rla::PolF32>(transa, transb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, ws, ws_bytes, st);
+    case RLA_F64: return rla::gemm_launch<rla::PolF64>(transa, transb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, ws, ws_bytes, st);
+    case RLA_DF: return rla::gemm_launch<rla::PolDF>(transa, transb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, ws, ws_bytes, st);
+    default: return RLA_ERR_ARG;
+  }
+}

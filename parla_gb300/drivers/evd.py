@@ -1,0 +1,96 @@
+"""Randomized symmetric eigensolvers EVD1 and EVD2 (Nystrom) on the device.
+
+Counterpart of ``parla/drivers/evd.py:171-384``.
+"""
+import warnings
+
+import numpy as np
+import torch
+
+from .. import _kernels as K
+from ..comps.sketchers.aware import _times
+from ..utils import linalg_wrappers as law
+
+EPS = np.finfo(float).eps
+
+
+class EVDecomposer:
+    """(A, k, tol, over, rng) -> (V, lamb)."""
+
+    def __call__(self, A, k, tol, over, rng):
+        raise NotImplementedError()
+
+
+class EVD1(EVDecomposer):
+    """QB(k+over, tol/2), eigh(B Q), keep the r largest |lambda| (``evd.py:218-289``)."""
+
+    TOL_CONTROL = "unknown"
+
+    def __init__(self, qb):
+        self.qb = qb
+
+    def __call__(self, A, k, tol, over, rng):
+        assert k > 0
+        assert k <= min(A.shape)
+        if not np.isnan(tol):
+            assert tol >= 0
+            assert tol < np.inf
+        rng = np.random.default_rng(rng)
+        Ad = A if isinstance(A, torch.Tensor) and A.is_cuda else K.to_dev(A, torch.float64)
+        Q, B = self.qb(Ad, k + over, tol / 2, rng)
+        Q64 = Q.to(torch.float64) if Q.dtype != torch.float64 else Q
+        B64 = B.to(torch.float64) if B.dtype != torch.float64 else B
+        C = K.gemm(B64, Q64, mode="df")
+        lam, U = law.sym_eig(C)
+        alam = torch.abs(lam)
+        d = Q.shape[1]
+        r = min(k, d, int(torch.count_nonzero(alam > 10 * EPS)))
+        idx = torch.argsort(-alam)[:r]
+        V = K.gemm(Q64, U[:, idx].contiguous())
+        return K.like_input(V.to(Q.dtype), A), K.like_input(lam[idx].to(Q.dtype), A)
+
+
+class EVD2(EVDecomposer):
+    """Shifted Nystrom approximation (``evd.py:299-384``; Tropp et al. 2017 Alg. 3).
+
+    Y = A S, nu = sqrt(n) eps ||Y||_F, R = chol(S^T (Y + nu S)), B = Y R^-1,
+    SVD of B through its l x l Gram, truncation rule and lambda = sigma^2 - nu
+    exactly as the reference (only the leading r columns of the reference's
+    full-matrices SVD are used, so the thin factorisation is equivalent).
+    """
+
+    TOL_CONTROL = "none"
+
+    def __init__(self, sk_op):
+        self.sk_op = sk_op
+
+    def __call__(self, A, k, tol, over, rng):
+        assert k > 0
+        n = A.shape[0]
+        assert k < n
+        if not np.isnan(tol):
+            warnings.warn("""
+            This EVDecomposer implementation cannot directly control
+            approximation error. Parameter "tol" is being ignored.
+            """)
+        rng = np.random.default_rng(rng)
+        Ad = A if isinstance(A, torch.Tensor) and A.is_cuda else K.to_dev(A, torch.float64)
+        S = self.sk_op(Ad, k + over, rng)
+        S = S.to(Ad.dtype) if S.dtype != Ad.dtype else S
+        Y = _times(Ad, S)
+        Y64 = Y.to(torch.float64) if Y.dtype != torch.float64 else Y
+        S64 = S.to(torch.float64) if S.dtype != torch.float64 else S
+        nu = float(np.sqrt(n) * EPS * float(torch.linalg.vector_norm(Y64)))
+        Y64 = Y64 + nu * S64
+        G = K.gemm(S64, Y64, transa=True, mode="df")
+        G = 0.5 * (G + G.t())
+        R = K.potrf_upper(G.contiguous(), mode="df")
+        Rinv = K.trtri_upper(R, mode="df")
+        B = K.gemm(Y64, Rinv, mode="df")
+        V, sigma, _ = law.small_svd_tall(B)
+        sig = sigma.cpu().numpy()
+        cuts = [k] + [i for i in range(k - 1) if sig[i + 1] ** 2 <= nu]
+        r = min(cuts)
+        lamb = (sigma ** 2)[:r] - nu
+        V = V[:, :r].contiguous()
+        return K.like_input(V.to(Ad.dtype), A), K.like_input(lamb.to(Ad.dtype), A)

@@ -1,0 +1,85 @@
+"""Orthonormalisation on the device: the RS1 stabilizer and RF1's final QR.
+
+``orth`` mirrors ``parla/utils/linalg_wrappers.py:6-7`` (Q of a thin QR).
+For binary64 input it is Householder QR (``rla_geqrf`` + ``rla_orgqr``); for
+binary32 input it is CholeskyQR2 with the Gram matrix accumulated in
+double-float and a double-float Cholesky, which keeps the first pass
+positive definite for condition numbers up to ~1e7 (a shift is added if it
+is not) while all the O(m k^2) work stays on the FP32 pipes.
+"""
+import torch
+
+from .. import _kernels as K
+from .._lib import RlaError
+
+
+def householder_orth(S):
+    """Thin Q of a binary64 m x k matrix by device Householder QR."""
+    Sd = K.to_dev(S, torch.float64)
+    m, k = Sd.shape
+    T = Sd.t().contiguous()
+    tau = K.geqrf_colmajor(T, k, "f64")
+    Qt = K.orgqr_colmajor(T, k, tau, "f64")
+    return Qt.t().contiguous()
+
+
+def cholqr(Y, passes=2):
+    """CholeskyQR repeated `passes` times; shifted first pass if needed."""
+    Q = Y
+    for p in range(passes):
+        Q64 = Q if Q.dtype == torch.float64 else Q.to(torch.float64)
+        G = K.gemm(Q64, Q64, transa=True, mode="df")
+        try:
+            R = K.potrf_upper(G.clone(), mode="df")
+        except RlaError:
+            k = G.shape[0]
+            shift = 1e-7 * float(torch.trace(G)) / k + 1e-30
+            R = K.potrf_upper(G + shift * torch.eye(k, dtype=G.dtype, device=G.device), mode="df")
+        Rinv = K.trtri_upper(R, mode="df")
+        Q = K.gemm(Q, Rinv if Q.dtype == torch.float64 else Rinv.to(Q.dtype))
+    return Q
+
+
+def orth(S):
+    """Q factor of a thin QR of S (device)."""
+    if isinstance(S, torch.Tensor) and S.dtype == torch.float32:
+        return cholqr(S, passes=2)
+    return householder_orth(S)
+
+
+def sym_eig(G):
+    """Eigenpairs of a small symmetric k x k device matrix, ascending order.
+
+    Uses the vendor dense eigensolver (cuSOLVER ``syevd`` through
+    ``torch.linalg.eigh``) on the device; k is the sketch size (<= ~600).
+    """
+    Gs = 0.5 * (G + G.t())
+    return torch.linalg.eigh(Gs)
+
+
+def small_svd_wide(B):
+    """Thin SVD of a wide k x n device matrix B (k << n) through its Gram.
+
+    G = B B^T is accumulated in double-float, G = U diag(lam) U^T, then
+    s = sqrt(lam) and Vh = diag(1/s) U^T B.  Returned in descending order.
+    """
+    B64 = B if B.dtype == torch.float64 else B.to(torch.float64)
+    G = K.gemm(B64, B64, transb=True, mode="df")
+    lam, U = sym_eig(G)
+    lam, U = lam.flip(0), U.flip(1).contiguous()
+    s = torch.sqrt(torch.clamp(lam, min=0.0))
+    inv = torch.where(s > 0, 1.0 / s, torch.zeros_like(s))
+    Vh = K.gemm(U, B64, transa=True) * inv[:, None]
+    return U, s, Vh.to(B.dtype) if B.dtype != torch.float64 else Vh
+
+
+def small_svd_tall(B):
+    """Thin SVD of a tall n x k device matrix B (k << n) through B^T B."""
+    B64 = B if B.dtype == torch.float64 else B.to(torch.float64)
+    G = K.gemm(B64, B64, transa=True, mode="df")
+    lam, V = sym_eig(G)
+    lam, V = lam.flip(0), V.flip(1).contiguous()
+    s = torch.sqrt(torch.clamp(lam, min=0.0))
+    inv = torch.where(s > 0, 1.0 / s, torch.zeros_like(s))
+    U = K.gemm(B64, V) * inv[None, :]
+    return U.to(B.dtype) if B.dtype != torch.float64 else U, s, V.t().contiguous()

@@ -1,0 +1,204 @@
+"""Device sketching operators: Gaussian, SJLT and SRCT.
+
+Counterpart of ``parla/utils/sketching.py``.  Each constructor returns an
+operator object that applies itself with the library's kernels:
+
+    S @ X   (X on the right: the least-squares sketch S A)
+    X @ S   (X on the left:  the range-finder sketch A S)
+
+Two ways to draw the randomness:
+
+* ``seed_compat=True`` issues exactly the NumPy Generator calls of the
+  reference (``rng.normal``, the per-column ``rng.choice`` loop,
+  ``generate_srct``), so a seed gives the reference's operator bit for bit;
+  only the draws happen on the host, every product runs on the GPU.
+* ``seed_compat=False`` (default) takes one 64-bit seed from ``rng`` and
+  draws on the device (Philox4x32-10): no host work and no PCIe traffic.
+"""
+import warnings
+
+import numpy as np
+import torch
+
+from .. import _kernels as K
+
+
+def _seed_from(rng):
+    return int(np.random.default_rng(rng).integers(0, 2 ** 63 - 1))
+
+
+class DeviceOperator:
+    """Base class: a linear operator whose products run on the GPU."""
+
+    shape = (0, 0)
+
+    def _left(self, X):
+        raise NotImplementedError
+
+    def _right(self, X):
+        raise NotImplementedError
+
+    def __matmul__(self, X):
+        Xd = _as_operand(X)
+        return K.like_input(self._left(Xd), X)
+
+    def __rmatmul__(self, X):
+        Xd = _as_operand(X)
+        return K.like_input(self._right(Xd), X)
+
+    def dense(self):
+        """Materialise the operator on the device (for tests and small cases)."""
+        eye = torch.eye(self.shape[1], dtype=torch.float64, device=K.device())
+        return self._left(eye)
+
+
+def _as_operand(X):
+    if isinstance(X, torch.Tensor) and X.is_cuda and X.dtype in (torch.float32, torch.float64):
+        return X.contiguous()
+    return K.to_dev(X, torch.float64)
+
+
+class DenseOperator(DeviceOperator):
+    """An explicit matrix resident in HBM."""
+
+    def __init__(self, S):
+        self.S = S
+        self.shape = tuple(S.shape)
+
+    def _left(self, X):
+        S = self.S if self.S.dtype == X.dtype else self.S.to(X.dtype)
+        return K.gemm(S, X)
+
+    def _right(self, X):
+        S = self.S if self.S.dtype == X.dtype else self.S.to(X.dtype)
+        return K.gemm(X, S)
+
+
+class GaussianOperator(DenseOperator):
+    """N(0, scale^2) entries from the device Philox stream keyed by `seed`."""
+
+    def __init__(self, n_rows, n_cols, seed, scale, dtype=torch.float64):
+        self.seed, self.scale = seed, scale
+        super().__init__(K.gaussian_fill(n_rows, n_cols, seed, scale, dtype))
+
+
+class SJLTOperator(DeviceOperator):
+    """Sparse sign embedding given by a wide pattern (k x n, nnz per column).
+
+    ``tall=False``: the operator is the wide k x n matrix (applied as S @ X).
+    ``tall=True``: the operator is its transpose n x k (applied as X @ S).
+    """
+
+    def __init__(self, rows, signs, nnz, k, n, tall=False):
+        self.rows, self.signs, self.nnz = rows, signs, nnz
+        self.k, self.n, self.tall = k, n, tall
+        self.scale = 1.0 / np.sqrt(nnz)
+        self.shape = (n, k) if tall else (k, n)
+
+    def _left(self, X):
+        if self.tall:  # (n x k) @ X is off the hot path: explicit operator
+            return self._dense_left(X)
+        return K.sjlt_apply(self.rows, self.signs, self.nnz, self.k, X, self.scale)
+
+    def _dense_left(self, X):
+        D = self.dense_matrix(X.dtype)
+        return K.gemm(D, X)
+
+    def dense_matrix(self, dtype=torch.float64):
+        """Explicit matrix of the operator (device), built with the SJLT kernel."""
+        eye = torch.eye(self.n, dtype=dtype, device=K.device())
+        W = K.sjlt_apply(self.rows, self.signs, self.nnz, self.k, eye, self.scale)  # k x n
+        return W.t().contiguous() if self.tall else W
+
+    def _right(self, X):
+        if self.tall:
+            return K.sjlt_apply_right(self.rows, self.signs, self.nnz, self.k, X, self.scale)
+        # X @ (k x n): via the explicit operator
+        return K.gemm(X, self.dense_matrix(X.dtype))
+
+    def dense(self):
+        return self.dense_matrix()
+
+
+class SRCTOperator(DeviceOperator):
+    """Subsampled randomized DCT-II: S X = (DCT_ortho(diag(e) X[perm]))[r]."""
+
+    def __init__(self, r, e, perm, n_rows, n_cols, mode="f64"):
+        self.r = K.to_dev(r, torch.int64)
+        self.e = K.to_dev(e, torch.float64)
+        self.perm = K.to_dev(perm, torch.int64) if perm is not None else None
+        self.shape = (n_rows, n_cols)
+        self.mode = mode
+        self.sketch_data = (r, e, perm)
+
+    def _left(self, X):
+        Xd = X if X.dtype == torch.float64 else X.to(torch.float64)
+        return K.srct_apply(self.r, self.e, self.perm, Xd, self.mode)
+
+    def _right(self, X):
+        raise NotImplementedError("SRCT is applied from the left (S @ A)")
+
+
+# ----------------------------------------------------------- constructors
+def gaussian_operator(n_rows, n_cols, rng, normalize=True, seed_compat=False, dtype=torch.float64):
+    """Gaussian sketch, entries N(0, 1/min(n_rows, n_cols)) when normalize.
+
+    Mirrors ``parla/utils/sketching.py:20-31``.
+    """
+    scale = float(np.sqrt(1.0 / min(n_rows, n_cols))) if normalize else 1.0
+    if seed_compat:
+        gen = np.random.default_rng(rng)
+        S = gen.normal(0.0, scale, (n_rows, n_cols)) if normalize else gen.standard_normal((n_rows, n_cols))
+        return DenseOperator(K.to_dev(S, dtype))
+    return GaussianOperator(n_rows, n_cols, _seed_from(rng), scale, dtype)
+
+
+def _host_sjlt_pattern(n_rows, n_cols, gen, vec_nnz):
+    """The reference's per-column draws (``parla/utils/sketching.py:55-71``)."""
+    vec_nnz = min(n_cols, vec_nnz)
+    repl = n_rows < vec_nnz
+    if repl:
+        warnings.warn(f"SJLT: {vec_nnz} nonzeros per column of length {n_rows}; "
+                      "sampling rows with replacement")
+    rows = np.empty(n_cols * vec_nnz, dtype=np.int32)
+    for j in range(n_cols):
+        rows[j * vec_nnz:(j + 1) * vec_nnz] = gen.choice(n_rows, vec_nnz, replace=repl)
+    signs = np.where(gen.random(n_cols * vec_nnz) <= 0.5, -1, 1).astype(np.int8)
+    return rows, signs, vec_nnz
+
+
+def sjlt_operator(n_rows, n_cols, rng, vec_nnz=8, seed_compat=False):
+    """SJLT with `vec_nnz` nonzeros +-1/sqrt(nnz) per column (wide) or row (tall).
+
+    Mirrors ``parla/utils/sketching.py:34-80``.
+    """
+    tall = n_cols < n_rows
+    k, n = (n_cols, n_rows) if tall else (n_rows, n_cols)
+    gen = np.random.default_rng(rng)
+    if seed_compat or k < min(n, vec_nnz):
+        rows, signs, nnz = _host_sjlt_pattern(k, n, gen, vec_nnz)
+        rows_d = K.to_dev(rows, torch.int32)
+        signs_d = K.to_dev(signs, torch.int8)
+    else:
+        nnz = min(n, vec_nnz)
+        rows_d, signs_d = K.sjlt_pattern(k, n, nnz, _seed_from(gen))
+    return SJLTOperator(rows_d, signs_d, nnz, k, n, tall=tall)
+
+
+def generate_srct(n_rows, n_cols, rng):
+    """(r, e, perm) exactly as ``parla/utils/sketching.py:106-115`` draws them."""
+    big, small = max(n_rows, n_cols), min(n_rows, n_cols)
+    r = rng.choice(big, size=small, replace=False)
+    draws = rng.random(big)
+    e = np.where(draws > 0.5, 1.0, -1.0) * np.sqrt(big / small)
+    perm = rng.permutation(big)
+    return r, e, perm
+
+
+def srct_operator(n_rows, n_cols, rng, mode="f64"):
+    """SRCT sketch (``parla/utils/sketching.py:179-201``), wide orientation."""
+    if n_cols < n_rows:
+        raise NotImplementedError("SRCT is provided for the wide (sketch-from-the-left) case")
+    gen = rng if isinstance(rng, np.random.Generator) else np.random.default_rng(rng)
+    r, e, perm = generate_srct(n_rows, n_cols, gen)
+    return SRCTOperator(r, e, perm, n_rows, n_cols, mode)

@@ -1,0 +1,52 @@
+"""CPU checks of the C ABI: the library loads and exports every declared symbol."""
+import os
+import re
+
+import pytest
+
+from parla_gb300 import _lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    text = open(os.path.join(ROOT, "include", "rla_gb300.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(rla_[a-z0-9_]+)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not os.path.exists(_lib.LIB_PATH):
+        from parla_gb300 import _build
+        _build.build()
+    return _lib.load()
+
+
+def test_header_declares_entry_points():
+    syms = declared_symbols()
+    assert "rla_gemm" in syms and "rla_lsqr_run" in syms and "rla_sjlt_apply" in syms
+    assert len(syms) >= 15
+
+
+def test_library_exports_every_declared_symbol(lib):
+    missing = [s for s in declared_symbols() if not hasattr(lib, s)]
+    assert not missing, f"declared but not exported: {missing}"
+
+
+def test_python_binding_covers_header():
+    assert set(declared_symbols()) <= set(_lib.SIGNATURES)
+
+
+def test_status_strings(lib):
+    assert lib.rla_status_string(0) == b"RLA_OK"
+    assert b"WORKSPACE" in lib.rla_status_string(8)
+    assert lib.rla_abi_version() == 1
+
+
+def test_argument_errors_need_no_gpu(lib):
+    # invalid sizes are rejected before any CUDA call
+    assert _lib.call_status("rla_gemm", 0, 0, 0, -1, 1, 1, 1.0, None, 1, None, 1, 0.0, None, 1,
+                            None, None, None) == 1
+    assert _lib.call_status("rla_sjlt_pattern", 4, 10, 8, 1, None, None, None) == 1  # nnz > d
+    assert _lib.call_status("rla_trtri_upper", 0, 3, None, 3, None, 3, None) == 1

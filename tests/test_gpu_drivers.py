@@ -1,0 +1,164 @@
+"""Driver-level parity on the GPU: parla_gb300's SPO / SSO1 / RS1 / RF1 / QB1 /
+SVD1 / EVD1 / EVD2 against the CPU oracle (pinned to the reference) on the
+golden inputs, with operators drawn exactly as the reference draws them
+(``seed_compat=True``).
+
+Gated metrics and tolerances:
+  least squares  ||A (x - x_oracle)|| / ||A x_oracle|| <= 1e-10
+  low rank       subspace / singular values within 1e-8 (FP64 inputs)
+"""
+import warnings
+
+import numpy as np
+import pytest
+import scipy.linalg as la
+
+import oracle
+from oracle import sketching as osk
+from oracle import lowrank as olr
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module")
+def pg():
+    import __graft_entry__
+    __graft_entry__.build()
+    import parla_gb300
+    return parla_gb300
+
+
+def pred_err(A, x, xr):
+    return la.norm(A @ (x - xr)) / la.norm(A @ xr)
+
+
+def oracle_op(gname, d, m, rng):
+    if gname == "ga":
+        return osk.gaussian_operator(d, m, rng)
+    if gname == "sj":
+        return osk.sjlt_operator(d, m, rng, 8)
+    return osk.srct_apply_dense(d, m, rng)[3]
+
+
+def gpu_gen(pg, gname):
+    if gname == "ga":
+        return pg.SkOpGA(seed_compat=True)
+    if gname == "sj":
+        return pg.SkOpSJ(8, seed_compat=True)
+    return pg.SkOpTC()
+
+
+@pytest.mark.parametrize("precision", ["f64", "df"])
+@pytest.mark.parametrize("gname", ["ga", "sj", "tc"])
+@pytest.mark.parametrize("mode", ["qr", "chol", "svd"])
+def test_spo_matches_oracle(pg, golden, precision, gname, mode):
+    g = golden("spo")
+    A, b = g["A"], g["b"]
+    seed = int(g[f"{gname}_{mode}_seed"])
+    d = oracle.dim_checks(4, *A.shape)
+    S = oracle_op(gname, d, A.shape[0], np.random.default_rng(seed))
+    xr, logr, _ = oracle.spo(A, b, 0.0, 1e-12, 100, S, mode)
+    x, log = pg.SPO(gpu_gen(pg, gname), 4, mode, precision)(A, b, 0.0, 1e-12, 100, seed)
+    assert isinstance(x, np.ndarray)
+    assert pred_err(A, x, xr) <= 1e-10
+    # against the reference's own output too
+    assert pred_err(A, x, g[f"{gname}_{mode}_x"]) <= 1e-10
+    assert log.errors.size >= 2 and log.times.size == log.errors.size
+    assert abs(log.errors.size - logr.errors.size) <= 2
+
+
+def test_spo_ridge(pg, golden):
+    g = golden("spo")
+    A, b = g["A"], g["b"]
+    x, log = pg.SPO(pg.SkOpGA(seed_compat=True), 3, "qr")(A, b, 0.25, 1e-12, 100, 7)
+    n = A.shape[1]
+    Aa = np.vstack([A, 0.5 * np.eye(n)])
+    xo = la.lstsq(Aa, np.concatenate([b, np.zeros(n)]))[0]
+    assert pred_err(Aa, x, xo) <= 1e-10
+    assert pred_err(Aa, x, g["ridge_x"]) <= 1e-10
+
+
+def test_spo_device_rng_properties(pg, golden):
+    """Device-drawn sketches: the reference's own convergence properties."""
+    g = golden("spo")
+    A, b = g["A"], g["b"]
+    xo = la.lstsq(A, b)[0]
+    for gen in (pg.SkOpGA(), pg.SkOpSJ(8)):
+        for prec in ("f64", "df"):
+            x, log = pg.SPO(gen, 4, "qr", prec)(A, b, 0.0, 1e-12, 100, 5)
+            assert pred_err(A, x, xo) <= 1e-10
+            errs = log.errors[1:]
+            assert errs[-1] <= 1e-6 * max(errs[0], 1e-300) or errs[-1] <= 1e-12
+
+
+def test_sso1(pg, golden):
+    g = golden("spo")
+    A, b = g["A"], g["b"]
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        x, log = pg.SSO1(pg.SkOpSJ(8, seed_compat=True), 3, "gelsd")(A, b, 0.0, np.nan, 1, 9)
+    assert pred_err(A, x, g["sso_x"]) <= 1e-9
+
+
+def _gauss(n_rows, n_cols, rng):
+    return osk.gaussian_operator(n_rows, n_cols, rng)
+
+
+def test_rs1_matches_oracle(pg, golden):
+    g = golden("lowrank")
+    A = g["A"]
+    for p in range(4):
+        S = pg.RS1(pg.SkOpGA(seed_compat=True), p)(A, 10, 60 + p).cpu().numpy()
+        Sr = olr.rs1(A, 10, np.random.default_rng(60 + p), _gauss, p)
+        # same span; orthonormal bases agree up to column signs
+        if p == 0:
+            assert np.allclose(S, Sr, rtol=0, atol=1e-12)
+        else:
+            assert np.allclose(np.abs(S.T @ Sr), np.eye(10), atol=1e-8)
+
+
+@pytest.mark.filterwarnings("ignore::UserWarning")
+def test_qb1_svd1_match_oracle(pg, golden):
+    g = golden("lowrank")
+    A = g["A"]
+    gen = pg.SkOpGA(seed_compat=True)
+    qb = pg.QB1(pg.RF1(pg.RS1(gen, 2)))
+    Q, B = qb(A, 12, np.nan, 71)
+    assert np.allclose(np.abs(Q.T @ g["qb1_Q"]), np.eye(12), atol=1e-8)
+    assert np.linalg.norm(Q @ B - g["qb1_Q"] @ g["qb1_B"]) <= 1e-9 * np.linalg.norm(A)
+    U, s, Vh = pg.SVD1(qb)(A, 10, np.nan, 5, 72)
+    assert np.allclose(s, g["svd1_s"], rtol=1e-8)
+    assert np.allclose(np.abs(U.T @ g["svd1_U"]), np.eye(10), atol=1e-6)
+    assert np.allclose(np.abs(Vh @ g["svd1_Vh"].T), np.eye(10), atol=1e-6)
+
+
+@pytest.mark.filterwarnings("ignore::UserWarning")
+def test_evd1_evd2_match_oracle(pg, golden):
+    g = golden("lowrank")
+    gen = pg.SkOpGA(seed_compat=True)
+    qb = pg.QB1(pg.RF1(pg.RS1(gen, 2)))
+    V, lam = pg.EVD1(qb)(g["Asym"], 10, np.nan, 4, 73)
+    assert np.allclose(lam, g["evd1_lamb"], rtol=1e-8, atol=1e-12)
+    assert np.allclose(np.abs(V.T @ g["evd1_V"]), np.eye(lam.size), atol=1e-6)
+    V, lam = pg.EVD2(pg.RS1(gen, 0))(g["Apsd"], 12, np.nan, 4, 74)
+    assert lam.size == g["evd2_lamb"].size
+    assert np.allclose(lam, g["evd2_lamb"], rtol=1e-7, atol=1e-12)
+    assert np.allclose(np.abs(V.T @ g["evd2_V"]), np.eye(lam.size), atol=1e-5)
+    V, lam = pg.EVD2(pg.RS1(gen, 2))(g["Apsd"], 12, np.nan, 4, 75)
+    assert np.allclose(lam, g["evd2p2_lamb"], rtol=1e-7, atol=1e-12)
+
+
+def test_svd1_float32_accuracy(pg):
+    """Binary32 input through the CholeskyQR2 stabilizer: near-optimal error."""
+    rng = np.random.default_rng(0)
+    m, n, k = 1500, 700, 40
+    U, _ = np.linalg.qr(rng.standard_normal((m, n)))
+    V, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    s = np.arange(1, n + 1, dtype=float) ** -1.5 + 1e-4
+    A = ((U * s) @ V.T).astype(np.float32)
+    Ad = torch.from_numpy(A).cuda()
+    Ug, sg, Vhg = pg.SVD1(pg.QB1(pg.RF1(pg.RS1(pg.SkOpGA(), 4))))(Ad, k, np.nan, 10, 1)
+    err = float(torch.linalg.matrix_norm(Ad.double() - (Ug.double() * sg.double()) @ Vhg.double()))
+    tail = np.sqrt(np.sum(s[k:] ** 2))
+    assert err <= 1.01 * tail

@@ -1,0 +1,233 @@
+"""Kernel-level parity on the GPU: each C-ABI kernel against the CPU oracle /
+an FP64 NumPy reference of the same operation, on seeded inputs.
+
+Tolerances: binary64 and double-float paths 1e-12 relative (df keeps ~48
+bits), binary32 1e-5, exact fixed-point SJLT 1e-14.
+"""
+import numpy as np
+import pytest
+import scipy.linalg as la
+
+import oracle
+from oracle import sketching as osk
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module")
+def K():
+    import __graft_entry__
+    __graft_entry__.build()
+    from parla_gb300 import _kernels
+    return _kernels
+
+
+def rel(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)
+
+
+def dev(x, dt=None):
+    t = torch.from_numpy(np.ascontiguousarray(x)).cuda()
+    return t if dt is None else t.to(dt)
+
+
+@pytest.mark.parametrize("mode,tol", [("f64", 1e-13), ("df", 1e-12), ("f32", 2e-5)])
+@pytest.mark.parametrize("ta,tb", [(False, False), (True, False), (False, True), (True, True)])
+@pytest.mark.parametrize("shape", [(37, 29, 53), (130, 70, 2000), (5, 3, 1)])
+def test_gemm(K, mode, tol, ta, tb, shape):
+    M, N, Kd = shape
+    rng = np.random.default_rng(M * 7 + N)
+    A = rng.standard_normal((Kd, M) if ta else (M, Kd))
+    B = rng.standard_normal((N, Kd) if tb else (Kd, N))
+    ref = (A.T if ta else A) @ (B.T if tb else B)
+    dt = torch.float32 if mode == "f32" else torch.float64
+    out = K.gemm(dev(A, dt), dev(B, dt), transa=ta, transb=tb, mode=mode)
+    assert rel(out.cpu().numpy(), ref) <= tol * (1 + np.sqrt(Kd) * (mode == "f32"))
+
+
+def test_gemm_alpha_beta(K):
+    rng = np.random.default_rng(3)
+    A, B, Cm = rng.standard_normal((50, 40)), rng.standard_normal((40, 30)), rng.standard_normal((50, 30))
+    Cd = dev(Cm.copy())
+    K.gemm(dev(A), dev(B), alpha=2.0, beta=-0.5, out=Cd)
+    assert rel(Cd.cpu().numpy(), 2.0 * A @ B - 0.5 * Cm) <= 1e-13
+
+
+def test_gaussian_fill_statistics(K):
+    S = K.gaussian_fill(1000, 1000, 1234, 0.5).cpu().numpy()
+    assert abs(S.mean()) < 3e-3
+    assert abs(S.std() - 0.5) < 3e-3
+    S2 = K.gaussian_fill(1000, 1000, 1234, 0.5).cpu().numpy()
+    assert np.array_equal(S, S2)  # counter-based: same seed, same operator
+
+
+@pytest.mark.parametrize("d,m,nnz", [(64, 5000, 8), (9, 100, 8), (200, 20000, 3)])
+def test_sjlt_pattern_distinct_rows(K, d, m, nnz):
+    rows, signs = K.sjlt_pattern(d, m, nnz, 99)
+    r = rows.cpu().numpy().reshape(m, nnz)
+    s = signs.cpu().numpy()
+    assert r.min() >= 0 and r.max() < d
+    assert all(len(set(row)) == nnz for row in r[:2000])
+    assert set(np.unique(s)) <= {-1, 1}
+    # rows are roughly uniform
+    counts = np.bincount(r.ravel(), minlength=d)
+    assert counts.std() / counts.mean() < 0.5
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize("d,m,n", [(80, 3000, 20), (800, 20000, 200), (16, 64, 5), (300, 5000, 1)])
+def test_sjlt_apply_matches_reference_operator(K, dtype, d, m, n):
+    rng = np.random.default_rng(d + n)
+    S = osk.sjlt_operator(d, m, np.random.default_rng(5), 8)  # reference draws (CSC)
+    A = rng.standard_normal((m, n)).astype(dtype)
+    A[::7] *= 1e-9  # wide dynamic range
+    ref = S @ A.astype(np.float64)
+    Sc = S.tocsc()
+    rows = Sc.indices.astype(np.int32)
+    signs = np.sign(Sc.data).astype(np.int8)
+    tdt = torch.float64 if dtype == np.float64 else torch.float32
+    Y = K.sjlt_apply(dev(rows), dev(signs), 8, d, dev(A, tdt), 1 / np.sqrt(8)).cpu().numpy()
+    tol = 1e-14 if dtype == np.float64 else 1e-6
+    assert rel(Y, ref) <= tol
+
+
+def test_sjlt_apply_with_replacement_duplicates(K):
+    with pytest.warns(UserWarning):
+        S = osk.sjlt_operator(5, 300, np.random.default_rng(15), 8)
+    A = np.random.default_rng(1).standard_normal((300, 7))
+    Sc = S.tocsc()
+    # duplicates were summed by SciPy: rebuild the raw pattern from the same draws
+    gen = np.random.default_rng(15)
+    rows = np.concatenate([gen.choice(5, 8, replace=True) for _ in range(300)]).astype(np.int32)
+    signs = np.where(gen.random(300 * 8) <= 0.5, -1, 1).astype(np.int8)
+    Y = K.sjlt_apply(dev(rows), dev(signs), 8, 5, dev(A), 1 / np.sqrt(8)).cpu().numpy()
+    assert rel(Y, S @ A) <= 1e-13
+
+
+def test_sjlt_apply_nonfinite_column_propagates(K):
+    rows, signs = K.sjlt_pattern(16, 100, 4, 3)
+    A = np.random.default_rng(2).standard_normal((100, 3))
+    A[10, 1] = np.nan
+    Y = K.sjlt_apply(rows, signs, 4, 16, dev(A), 0.5).cpu().numpy()
+    assert np.all(np.isnan(Y[:, 1])) and np.all(np.isfinite(Y[:, [0, 2]]))
+
+
+def test_sjlt_apply_right(K):
+    S = osk.sjlt_operator(500, 12, np.random.default_rng(8), 4)  # tall (CSR)
+    wide = osk.sjlt_operator(12, 500, np.random.default_rng(8), 4).tocsc()
+    A = np.random.default_rng(4).standard_normal((70, 500))
+    Y = K.sjlt_apply_right(dev(wide.indices.astype(np.int32)), dev(np.sign(wide.data).astype(np.int8)), 4, 12,
+                           dev(A), 0.5).cpu().numpy()
+    assert rel(Y, A @ S) <= 1e-12
+
+
+@pytest.mark.parametrize("mode", ["f64", "df"])
+@pytest.mark.parametrize("d,m,n", [(16, 100, 5), (80, 2000, 20)])
+def test_srct_apply(K, mode, d, m, n):
+    gen = np.random.default_rng(16)
+    r, e, perm = osk.generate_srct(d, m, gen)
+    A = np.random.default_rng(1).standard_normal((m, n))
+    ref = osk.apply_srct(r, e, A, perm)
+    Y = K.srct_apply(dev(r), dev(e), dev(perm), dev(A), mode).cpu().numpy()
+    assert rel(Y, ref) <= 1e-12
+
+
+@pytest.mark.parametrize("mode", ["f64", "df"])
+@pytest.mark.parametrize("m,n", [(800, 200), (50, 50), (300, 7)])
+def test_geqrf_orgqr(K, mode, m, n):
+    rng = np.random.default_rng(m)
+    A = rng.standard_normal((m, n)) @ np.diag(np.logspace(0, -8, n))
+    b = rng.standard_normal(m)
+    T = dev(np.vstack([A.T, b[None, :]]))  # column-major (m x (n+1))
+    tau = K.geqrf_colmajor(T, n, mode)
+    R = np.triu(T[:n, :n].cpu().numpy().T)
+    Qref, Rref = la.qr(A, mode="economic")
+    assert rel(np.abs(R), np.abs(Rref)) <= 1e-10
+    z = T[n, :n].cpu().numpy()
+    assert rel(np.abs(z), np.abs(Qref.T @ b)) <= 1e-10
+    Qt = K.orgqr_colmajor(T, n, tau, mode).cpu().numpy()
+    Q = Qt.T
+    assert np.max(np.abs(Q.T @ Q - np.eye(n))) <= 1e-12
+    assert rel(Q @ R, A) <= 1e-12
+
+
+@pytest.mark.parametrize("mode,tol", [("f64", 1e-12), ("df", 1e-11), ("f32", 1e-4)])
+@pytest.mark.parametrize("n", [1, 17, 210])
+def test_potrf_trtri(K, mode, tol, n):
+    rng = np.random.default_rng(n)
+    X = rng.standard_normal((3 * n, n))
+    G = X.T @ X + n * np.eye(n)
+    dt = torch.float32 if mode == "f32" else torch.float64
+    Gd = dev(G, dt)
+    R = K.potrf_upper(Gd, mode).cpu().numpy().astype(np.float64)
+    Rref = la.cholesky(G, lower=False)
+    assert rel(R, Rref) <= tol
+    Rinv = K.trtri_upper(dev(Rref, dt), mode).cpu().numpy().astype(np.float64)
+    assert rel(Rinv, la.inv(Rref)) <= tol * 10
+
+
+def test_potrf_reports_not_spd(K):
+    from parla_gb300._lib import RlaError
+    G = np.diag([1.0, -1.0, 2.0])
+    with pytest.raises(RlaError) as ei:
+        K.potrf_upper(dev(G), "f64")
+    assert ei.value.status == 3
+
+
+@pytest.mark.parametrize("mode", ["f64", "df"])
+@pytest.mark.parametrize("case", ["plain", "x0", "ridge"])
+def test_lsqr_run_matches_oracle(K, mode, case):
+    rng = np.random.default_rng(31)
+    m, n = 600, 30
+    A = rng.standard_normal((m, n)) @ np.diag(np.logspace(0, -3, n))
+    b = rng.standard_normal(m)
+    M = la.inv(la.qr(A, mode="economic")[1])  # ideal preconditioner -> few iterations
+    M = M + 1e-3 * rng.standard_normal(M.shape) * np.abs(M).max()
+    sd = 0.3 if case == "ridge" else 0.0
+    z0 = rng.standard_normal(n) if case == "x0" else None
+
+    def mv(z):
+        y = M @ z
+        return np.concatenate([A @ y, sd * y]) if sd > 0 else A @ y
+
+    def rmv(u):
+        w = A.T @ u[:m]
+        if sd > 0:
+            w = w + sd * u[m:]
+        return M.T @ w
+
+    rhs = np.concatenate([b, np.zeros(n)]) if sd > 0 else b
+    ref = oracle.lsqr(mv, rmv, n, rhs, atol=1e-12, btol=1e-12, iter_lim=100, x0=z0)
+    z, istop, itn, arn = K.lsqr_run(dev(A), dev(M), dev(b), None if z0 is None else dev(z0), sd,
+                                    1e-12, 1e-12, 1e8, 100, mode)
+    x = M @ z.cpu().numpy()
+    xr = M @ ref[0]
+    Aa = np.vstack([A, sd * np.eye(n)]) if sd > 0 else A
+    assert la.norm(Aa @ (x - xr)) / la.norm(Aa @ xr) <= 1e-11
+    assert istop == ref[1]
+    assert abs(itn - ref[2]) <= 1
+    k = min(itn, ref[2])
+    assert rel(arn[:k], ref[7][:k]) <= 1e-6
+
+
+def test_lsqr_iter_limit_one(K):
+    rng = np.random.default_rng(2)
+    A = rng.standard_normal((200, 10))
+    b = rng.standard_normal(200)
+    z, istop, itn, arn = K.lsqr_run(dev(A), dev(np.eye(10)), dev(b), None, 0.0, 1e-12, 1e-12, 1e8, 1, "f64")
+    ref = oracle.lsqr(lambda v: A @ v, lambda u: A.T @ u, 10, b, atol=1e-12, btol=1e-12, iter_lim=1)
+    assert itn == 1 and istop == ref[1] == 7
+    assert rel(z.cpu().numpy(), ref[0]) <= 1e-12
+
+
+def test_split_and_convert(K):
+    rng = np.random.default_rng(0)
+    A = rng.standard_normal((33, 17)) * 1e3
+    hi, lo = K.split_f64(dev(A))
+    assert rel(hi.double().cpu().numpy() + lo.double().cpu().numpy(), A) <= 2 ** -46
+    At = K.convert(dev(A), torch.float32, transpose=True).cpu().numpy()
+    assert rel(At, A.T.astype(np.float32)) <= 1e-7
