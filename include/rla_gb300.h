@@ -93,6 +93,21 @@ int rla_sjlt_apply_right(int dtype, int64_t m, int64_t n, int64_t k, int nnz,
                          const void* A, int64_t lda, void* Y, int64_t ldy,
                          rla_stream_t stream);
 
+/* Same product as rla_sjlt_apply, for callers that cannot allocate device
+ * memory (allocator-free embeddings, real-time loops where cudaMalloc is not
+ * allowed).  No counterpart in the reference: it adds no new mathematics,
+ * only a different home for the scratch.  The partial sums use a 16 MiB
+ * array compiled into the library, held by every GPU context that loads the
+ * library until exit; problems that need more return RLA_ERR_WORKSPACE.  The
+ * first call on a device resolves the array's address (call it before any
+ * stream capture on that device).  All calls share the array: calls that
+ * overlap on the GPU race and must be serialised by the caller.  Allocates
+ * nothing. */
+int rla_sjlt_apply_noalloc(int dtype, int64_t d, int64_t m, int64_t n, int nnz,
+                           const int32_t* rows, const int8_t* signs,
+                           double scale, const void* A, int64_t lda, void* Y,
+                           int64_t ldy, rla_stream_t stream);
+
 /* SRCT: Y (d x n) = (DCT-II_ortho(diag(e) A[perm, :]))[r, :], m = rows of A.
  * r: d distinct row indices, e: m signed scales, perm: permutation of [0,m)
  * (NULL for identity).  FP64 storage; dtype RLA_F64.  Replaces apply_srct's

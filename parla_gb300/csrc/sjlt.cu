@@ -331,3 +331,82 @@ int rla_sjlt_apply_right(int dtype, int64_t m, int64_t n, int64_t k, int nnz, co
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------------
+// rla_sjlt_apply_noalloc: the same sketch product for callers that cannot
+// allocate device memory (for example code running inside a real-time loop
+// or an allocator-free embedding where cudaMalloc is unavailable or
+// forbidden).  Its per-cluster partial sums live in a fixed array compiled
+// into the library instead of a caller-provided workspace.
+//
+// - The array is kNoAllocScratchBytes (16 MiB); every GPU context that loads
+//   the library holds it until the process exits.
+// - Problems whose partials exceed it are rejected with RLA_ERR_WORKSPACE.
+// - The first call on a device looks up the array's device address with
+//   cudaGetSymbolAddress (with that device current) and caches it; make that
+//   first call before any stream capture on the device.
+// - All calls share the array.  Every partial is written before it is read,
+//   so nothing has to be cleared between calls, but calls that overlap on the
+//   GPU (different streams, or different host threads) race on it and must
+//   be serialised by the caller.
+// - No cudaMalloc, cudaFree or allocating library routine is called.
+#include <mutex>
+
+static constexpr size_t kNoAllocScratchBytes = size_t(16) << 20;
+static __device__ __align__(256) double rla_noalloc_scratch[kNoAllocScratchBytes / sizeof(double)];
+
+namespace rla {
+namespace {
+std::mutex g_noalloc_mu;
+double* g_noalloc_ptr[64] = {};
+
+int noalloc_scratch_ptr(double** out) {
+  int dev = 0;
+  RLA_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return RLA_ERR_UNSUPPORTED;
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (g_noalloc_ptr[dev] == nullptr) {
+    void* p = nullptr;
+    RLA_CUDA_TRY(cudaGetSymbolAddress(&p, rla_noalloc_scratch));
+    g_noalloc_ptr[dev] = static_cast<double*>(p);
+  }
+  *out = g_noalloc_ptr[dev];
+  return RLA_OK;
+}
+
+template <typename T>
+int sjlt_apply_noalloc_impl(int64_t d, int64_t m, int64_t n, int nnz, const int32_t* rows, const int8_t* signs,
+                            double scale, const void* A, int64_t lda, void* Y, int64_t ldy, cudaStream_t st) {
+  SjltPlan p = sjlt_plan(d, m, n, nnz);
+  if (static_cast<size_t>(d) * 8 > kSjltSmemCap) return RLA_ERR_UNSUPPORTED;
+  if (p.ws > kNoAllocScratchBytes) return RLA_ERR_WORKSPACE;
+  if (d == 0 || n == 0) return RLA_OK;
+  double* scratch = nullptr;
+  int rc = noalloc_scratch_ptr(&scratch);
+  if (rc != RLA_OK) return rc;
+  auto kern = sjlt_apply_kernel<T>;
+  RLA_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(p.smem)));
+  dim3 grid(static_cast<unsigned>(p.slabs), static_cast<unsigned>(p.chunks));
+  kern<<<grid, kSjltThreads, p.smem, st>>>(d, m, n, nnz, p.W, p.rows_per_chunk, rows, signs,
+                                           static_cast<const T*>(A), lda, scratch);
+  RLA_LAUNCH_CHECK();
+  sjlt_reduce_kernel<T><<<static_cast<unsigned>(ceil_div(d * n, 256)), 256, 0, st>>>(
+      d, n, p.clusters, scale, scratch, static_cast<T*>(Y), ldy);
+  RLA_LAUNCH_CHECK();
+  return RLA_OK;
+}
+}  // namespace
+}  // namespace rla
+
+extern "C" int rla_sjlt_apply_noalloc(int dtype, int64_t d, int64_t m, int64_t n, int nnz, const int32_t* rows,
+                                      const int8_t* signs, double scale, const void* A, int64_t lda, void* Y,
+                                      int64_t ldy, rla_stream_t stream) {
+  if (d < 0 || m < 0 || n < 0 || nnz <= 0 || nnz > 64 || lda < n || ldy < n) return RLA_ERR_ARG;
+  if ((m > 0 && (!rows || !signs || !A)) || (d * n > 0 && !Y)) return RLA_ERR_ARG;
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  switch (dtype) {
+    case RLA_F64: return rla::sjlt_apply_noalloc_impl<double>(d, m, n, nnz, rows, signs, scale, A, lda, Y, ldy, st);
+    case RLA_F32: return rla::sjlt_apply_noalloc_impl<float>(d, m, n, nnz, rows, signs, scale, A, lda, Y, ldy, st);
+    default: return RLA_ERR_ARG;
+  }
+}
