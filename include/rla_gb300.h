@@ -131,6 +131,25 @@ int rla_gemm(int dtype, int transa, int transb, int64_t M, int64_t N, int64_t K,
              int64_t ldb, double beta, void* C, int64_t ldc, void* ws,
              size_t* ws_bytes, rla_stream_t stream);
 
+/* Tensor-core GEMM (tcgen05.mma kind::f16, TMA-fed, FP32 accumulation in
+ * TMEM): D (M x N, fp32) = alpha X W^T + beta D with X (M x K) and W (N x K)
+ * bf16 row-major (both K-major; ldx, ldw multiples of 8, 16-byte aligned
+ * bases).  out_trans != 0 stores D^T (N x M, leading dimension ldd).
+ * splits = 0 picks split-K automatically (partials in ws, summed in a fixed
+ * order); ws holds a device error flag in its first 4 bytes
+ * (rla_gemm_bf16_tc_status).  Replaces the dense products of the randomized
+ * SVD chain: A @ S and A.T @ S (parla/comps/sketchers/aware.py:175,179),
+ * A @ S (parla/comps/rangefinders.py:186), Q.T @ A (parla/comps/qb.py:351). */
+int rla_gemm_bf16_tc(int64_t M, int64_t N, int64_t K, const void* X,
+                     int64_t ldx, const void* W, int64_t ldw, float* D,
+                     int64_t ldd, int out_trans, float alpha, float beta,
+                     int splits, void* ws, size_t* ws_bytes,
+                     rla_stream_t stream);
+
+/* Reads the device error flag (0 or RLA_ERR_TIMEOUT) left in `ws` by the
+ * last rla_gemm_bf16_tc on that workspace; synchronises `stream`. */
+int rla_gemm_bf16_tc_status(const void* ws, int* status, rla_stream_t stream);
+
 /* ------------------------------------------------- small dense factorizations */
 
 /* Householder QR of the first n columns of A (m x (n + nrhs), m >= n),

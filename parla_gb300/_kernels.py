@@ -124,6 +124,33 @@ def gemm(A, B, transa=False, transb=False, alpha=1.0, beta=0.0, out=None, mode=N
     return out
 
 
+def gemm_tc(X, W, out=None, out_trans=False, alpha=1.0, beta=0.0, splits=0, check=False):
+    """fp32 D = alpha X W^T (+ beta D) on the tensor cores; X, W bf16 row-major.
+
+    Returns D (M x N) or, with out_trans, D^T (N x M).
+    """
+    assert X.dtype == torch.bfloat16 and W.dtype == torch.bfloat16
+    M, Kx = X.shape
+    N, Kw = W.shape
+    if Kx != Kw:
+        raise ValueError(f"gemm_tc: K differs ({Kx} vs {Kw})")
+    if out is None:
+        out = torch.empty((N, M) if out_trans else (M, N), dtype=torch.float32, device=X.device)
+        beta = 0.0
+    head = (M, N, Kx, ptr(X), X.stride(0), ptr(W), W.stride(0), ptr(out), out.stride(0), int(out_trans),
+            C.c_float(alpha), C.c_float(beta), int(splits))
+    need = size_query("rla_gemm_bf16_tc", *head)
+    ws = workspace(need)
+    nb = C.c_size_t(need)
+    _timed("gemm_tc", 2, call, "rla_gemm_bf16_tc", *head, ptr(ws), C.byref(nb), stream())
+    if check:
+        st = C.c_int(0)
+        call("rla_gemm_bf16_tc_status", ptr(ws), C.byref(st), stream())
+        if st.value:
+            raise _lib.RlaError("rla_gemm_bf16_tc", st.value, "device wait timed out")
+    return out
+
+
 # ------------------------------------------------------------- sketches
 def gaussian_fill(rows, cols, seed, scale, dtype=torch.float64):
     S = torch.empty((rows, cols), dtype=dtype, device=device())
