@@ -186,6 +186,16 @@ int rla_potrf_upper(int dtype, int64_t n, void* G, int64_t ldg, int* info,
 int rla_trtri_upper(int dtype, int64_t n, const void* R, int64_t ldr, void* X,
                     int64_t ldx, rla_stream_t stream);
 
+/* Rinv = R^-1 where G = R^T R (upper Cholesky), FP32, n <= 216, in one CTA
+ * with G resident in shared memory; R is also written when R != NULL.
+ * *info (device) = j+1 if pivot j was not positive, else 0.  Used by the
+ * CholeskyQR stabilizer of the tensor-core range finder (replaces orth,
+ * parla/utils/linalg_wrappers.py:6-7, and the la.qr of
+ * parla/comps/rangefinders.py:187). */
+int rla_chol_inv_f32(int64_t n, const float* G, int64_t ldg, float* Rinv,
+                     int64_t ldr, float* R, int64_t ldro, int* info,
+                     rla_stream_t stream);
+
 /* ------------------------------------------------------------- LSQR */
 
 /* Preconditioned LSQR on Abar = [A; sqrt_delta I] M, run as one cooperative
@@ -215,6 +225,14 @@ int rla_lsqr_run(int dtype, int64_t m, int64_t n, int64_t p, const double* A,
 int rla_convert(int src_dtype, int dst_dtype, int transpose, int64_t rows,
                 int64_t cols, const void* x, int64_t ldx, void* y, int64_t ldy,
                 rla_stream_t stream);
+
+/* One read of x (rows x cols, RLA_F32 or RLA_F64), two bf16 writes: y = x
+ * (leading dimension ldy) and yt = x^T (cols x rows, ldyt); either output may
+ * be NULL.  Produces the tensor-core operands A and A^T of the randomized SVD
+ * passes (no reference counterpart: the reference keeps A in float64). */
+int rla_convert_bf16_pair(int src_dtype, int64_t rows, int64_t cols,
+                          const void* x, int64_t ldx, void* y, int64_t ldy,
+                          void* yt, int64_t ldyt, rla_stream_t stream);
 
 /* hi (float) + lo (float) = x (double) to about 2^-48 relative; the planes
  * share the row stride ldh.  Prepares A for the double-float LSQR and GEMM

@@ -26,10 +26,12 @@ class _Stats:
         self.launches = 0
         self.timing = False
         self.events = []
+        self.meta = []      # (M, N, K) of each timed tensor-core GEMM, in order
 
     def reset(self):
         self.launches = 0
         self.events = []
+        self.meta = []
 
 
 STATS = _Stats()
@@ -130,6 +132,7 @@ def gemm_tc(X, W, out=None, out_trans=False, alpha=1.0, beta=0.0, splits=0, chec
     Returns D (M x N) or, with out_trans, D^T (N x M).
     """
     assert X.dtype == torch.bfloat16 and W.dtype == torch.bfloat16
+    assert X.stride(1) == 1 and W.stride(1) == 1
     M, Kx = X.shape
     N, Kw = W.shape
     if Kx != Kw:
@@ -142,6 +145,8 @@ def gemm_tc(X, W, out=None, out_trans=False, alpha=1.0, beta=0.0, splits=0, chec
     need = size_query("rla_gemm_bf16_tc", *head)
     ws = workspace(need)
     nb = C.c_size_t(need)
+    if STATS.timing:
+        STATS.meta.append((M, N, Kx))
     _timed("gemm_tc", 2, call, "rla_gemm_bf16_tc", *head, ptr(ws), C.byref(nb), stream())
     if check:
         st = C.c_int(0)
@@ -250,6 +255,29 @@ def potrf_upper(G, mode=None):
     return G
 
 
+def chol_inv_f32(G, want_r=False, info=None):
+    """R^-1 (and optionally R) for G = R^T R, FP32, n <= 216, one CTA.
+
+    Returns None when n is too large for the single-CTA kernel.  With
+    ``info=None`` the call synchronises and raises RlaError(NOT_SPD) on a
+    non-positive pivot; with a caller-provided int32 device tensor it does not
+    synchronise and leaves the pivot index (+1, or 0) there.
+    """
+    n = G.shape[0]
+    if n > 216:
+        return None
+    Rinv = torch.empty((n, n), dtype=torch.float32, device=G.device)
+    R = torch.empty((n, n), dtype=torch.float32, device=G.device) if want_r else None
+    inf = info if info is not None else torch.zeros(1, dtype=torch.int32, device=G.device)
+    _timed("chol_inv", 1, call, "rla_chol_inv_f32", n, ptr(G), G.stride(0), ptr(Rinv), n, ptr(R), n, ptr(inf),
+           stream())
+    if info is None:
+        bad = int(inf.item())
+        if bad:
+            raise _lib.RlaError("rla_chol_inv_f32", 3, f"pivot {bad - 1} not positive")
+    return (Rinv, R) if want_r else Rinv
+
+
 def trtri_upper(R, mode=None):
     if mode is None:
         mode = "f32" if R.dtype == torch.float32 else "f64"
@@ -267,12 +295,34 @@ def split_f64(A):
     return hi, lo
 
 
+def _pad8(n):
+    return (n + 7) // 8 * 8
+
+
+def empty_bf16(rows, cols, dev):
+    """bf16 (rows x cols) view whose row stride is a multiple of 8 elements
+    (16 bytes), as the tensor-core GEMM's TMA descriptors require."""
+    return torch.empty((rows, _pad8(cols)), dtype=torch.bfloat16, device=dev)[:, :cols]
+
+
 def convert(x, dtype, transpose=False):
     rows, cols = x.shape
-    y = torch.empty((cols, rows) if transpose else (rows, cols), dtype=dtype, device=x.device)
-    _timed("convert", 1, call, "rla_convert", _TORCH_CODE[x.dtype], _TORCH_CODE[dtype], int(transpose), rows, cols, ptr(x),
-         x.stride(0), ptr(y), y.stride(0), stream())
+    oshape = (cols, rows) if transpose else (rows, cols)
+    y = empty_bf16(*oshape, x.device) if dtype == torch.bfloat16 else torch.empty(oshape, dtype=dtype, device=x.device)
+    _timed("convert", 1, call, "rla_convert", _TORCH_CODE[x.dtype], _TORCH_CODE[dtype], int(transpose), rows, cols,
+           ptr(x), x.stride(0), ptr(y), y.stride(0), stream())
     return y
+
+
+def convert_bf16_pair(x, want_y=True, want_t=True):
+    """(bf16(x), bf16(x)^T) from one pass over x (float32/float64)."""
+    rows, cols = x.shape
+    y = empty_bf16(rows, cols, x.device) if want_y else None
+    yt = empty_bf16(cols, rows, x.device) if want_t else None
+    _timed("convert_bf16_pair", 1, call, "rla_convert_bf16_pair", _TORCH_CODE[x.dtype], rows, cols, ptr(x),
+           x.stride(0), ptr(y), y.stride(0) if y is not None else 0, ptr(yt),
+           yt.stride(0) if yt is not None else 0, stream())
+    return y, yt
 
 
 def lsqr_run(A, M, b, z0, sqrt_delta, atol, btol, conlim, iter_lim, mode="f64", split=None):

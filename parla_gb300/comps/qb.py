@@ -3,7 +3,9 @@ import numpy as np
 import torch
 
 from .. import _kernels as K
+from ..utils import operand as opd
 from .rangefinders import RangeFinder
+from .sketchers.aware import _times_t
 
 
 class QBDecomposer:
@@ -18,8 +20,9 @@ class QB1(QBDecomposer):
 
     TOL_CONTROL = "unknown"
 
-    def __init__(self, rf: RangeFinder):
+    def __init__(self, rf: RangeFinder, precision=None):
         self.rangefinder = rf
+        self.precision = precision
 
     def __call__(self, A, k, tol, rng):
         assert k > 0
@@ -28,7 +31,11 @@ class QB1(QBDecomposer):
             assert tol >= 0
             assert tol < 1
         rng = np.random.default_rng(rng)
-        Ad = A if isinstance(A, torch.Tensor) and A.is_cuda else K.to_dev(A, torch.float64)
-        Q = self.rangefinder(Ad, k, tol, rng)
-        B = K.gemm(Q, Ad, transa=True)
+        Am = opd.wrap(A, self.precision)
+        Q = self.rangefinder(Am, k, tol, rng)
+        B = _times_t(Am, Q).t()            # B = (A^T Q)^T
+        if not Am.tc:
+            B = B.contiguous()
+        if isinstance(A, (torch.Tensor, opd.DeviceMatrix)):
+            return Q, B
         return K.like_input(Q, A), K.like_input(B, A)

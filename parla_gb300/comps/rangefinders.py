@@ -6,6 +6,7 @@ import torch
 
 from .. import _kernels as K
 from ..utils import linalg_wrappers as law
+from ..utils import operand as opd
 from .sketchers.aware import RowSketcher, _times
 
 
@@ -18,8 +19,9 @@ class RangeFinder:
 
 class RF1(RangeFinder):
 
-    def __init__(self, rso: RowSketcher):
+    def __init__(self, rso: RowSketcher, precision=None):
         self.rso = rso
+        self.precision = precision
 
     def __call__(self, A, k, tol, rng):
         assert k > 0
@@ -30,8 +32,8 @@ class RF1(RangeFinder):
             approximation error. Parameter "tol" is being ignored.
             """)
         rng = np.random.default_rng(rng)
-        Ad = A if isinstance(A, torch.Tensor) and A.is_cuda else K.to_dev(A, torch.float64)
-        S = self.rso(Ad, k, rng)
-        Y = _times(Ad, S)
-        Q = law.orth(Y)
-        return K.like_input(Q, A)
+        Am = opd.wrap(A, self.precision)
+        S = self.rso(Am, k, rng)
+        Y = _times(Am, S)
+        Q = law.orth_tc(Y, passes=2) if Am.tc else law.orth(Y)
+        return Q if isinstance(A, (torch.Tensor, opd.DeviceMatrix)) else K.like_input(Q, A)

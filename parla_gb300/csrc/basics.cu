@@ -209,3 +209,95 @@ extern "C" int rla_split_f64(int64_t rows, int64_t cols, const double* x, int64_
   RLA_LAUNCH_CHECK();
   return RLA_OK;
 }
+
+namespace rla {
+namespace {
+// y = bf16(x) (rows x cols) and yt = bf16(x)^T (cols x rows) from one read of x.
+// 64 x 64 tiles, 256 threads: each thread reads 4 rows x 4 columns as four
+// 16-byte loads, writes 4 x 8-byte bf16 packets to y, and after a shared-memory
+// transpose 4 x 8-byte packets to yt.  Ragged edges fall back to scalar code.
+template <typename S>
+__global__ void __launch_bounds__(256) convert_bf16_pair_kernel(int64_t rows, int64_t cols, const S* __restrict__ x,
+                                                                int64_t ldx, __nv_bfloat16* __restrict__ y, int64_t ldy,
+                                                                __nv_bfloat16* __restrict__ yt, int64_t ldyt) {
+  __shared__ __nv_bfloat16 tile[64][72];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const int64_t i0 = static_cast<int64_t>(blockIdx.y) * 64, j0 = static_cast<int64_t>(blockIdx.x) * 64;
+  const bool full = (i0 + 64 <= rows) && (j0 + 64 <= cols) && (ldx % 4 == 0) && (ldy % 4 == 0) && (ldyt % 4 == 0) &&
+                    sizeof(S) == 4 && ((reinterpret_cast<uintptr_t>(x) & 15) == 0);
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const int li = ty * 4 + r;
+    const int64_t i = i0 + li;
+    __nv_bfloat16 v[4];
+    if (full) {
+      float4 f = *reinterpret_cast<const float4*>(reinterpret_cast<const float*>(x) + i * ldx + j0 + tx * 4);
+      v[0] = __float2bfloat16_rn(f.x); v[1] = __float2bfloat16_rn(f.y);
+      v[2] = __float2bfloat16_rn(f.z); v[3] = __float2bfloat16_rn(f.w);
+      if (y) {
+        uint2 pk;
+        pk.x = (static_cast<uint32_t>(__bfloat16_as_ushort(v[1])) << 16) | __bfloat16_as_ushort(v[0]);
+        pk.y = (static_cast<uint32_t>(__bfloat16_as_ushort(v[3])) << 16) | __bfloat16_as_ushort(v[2]);
+        *reinterpret_cast<uint2*>(y + i * ldy + j0 + tx * 4) = pk;
+      }
+    } else {
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const int64_t j = j0 + tx * 4 + c;
+        v[c] = __float2bfloat16_rn(0.f);
+        if (i < rows && j < cols) {
+          v[c] = conv<S, __nv_bfloat16>(x[i * ldx + j]);
+          if (y) y[i * ldy + j] = v[c];
+        }
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < 4; ++c) tile[li][tx * 4 + c] = v[c];
+  }
+  __syncthreads();
+  if (!yt) return;
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const int lj = ty * 4 + r;  // row of yt inside the tile
+    const int64_t j = j0 + lj;
+    __nv_bfloat16 v[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) v[c] = tile[tx * 4 + c][lj];
+    if (full) {
+      uint2 pk;
+      pk.x = (static_cast<uint32_t>(__bfloat16_as_ushort(v[1])) << 16) | __bfloat16_as_ushort(v[0]);
+      pk.y = (static_cast<uint32_t>(__bfloat16_as_ushort(v[3])) << 16) | __bfloat16_as_ushort(v[2]);
+      *reinterpret_cast<uint2*>(yt + j * ldyt + i0 + tx * 4) = pk;
+    } else {
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const int64_t i = i0 + tx * 4 + c;
+        if (i < rows && j < cols) yt[j * ldyt + i] = v[c];
+      }
+    }
+  }
+}
+}  // namespace
+}  // namespace rla
+
+// bf16 copy and bf16 transposed copy of a float32/float64 matrix in one pass
+// (tensor-core operands for X = A and X = A^T).  Either output may be NULL.
+extern "C" int rla_convert_bf16_pair(int src_dtype, int64_t rows, int64_t cols, const void* x, int64_t ldx, void* y,
+                                     int64_t ldy, void* yt, int64_t ldyt, rla_stream_t stream) {
+  if (rows < 0 || cols < 0 || ldx < cols || (y && ldy < cols) || (yt && ldyt < rows)) return RLA_ERR_ARG;
+  if (rows * cols == 0) return RLA_OK;
+  if (!x || (!y && !yt)) return RLA_ERR_ARG;
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  dim3 grid(static_cast<unsigned>(rla::ceil_div(cols, 64)), static_cast<unsigned>(rla::ceil_div(rows, 64)));
+  dim3 block(256);
+  auto* yb = static_cast<__nv_bfloat16*>(y);
+  auto* ytb = static_cast<__nv_bfloat16*>(yt);
+  if (src_dtype == RLA_F32)
+    rla::convert_bf16_pair_kernel<float><<<grid, block, 0, st>>>(rows, cols, static_cast<const float*>(x), ldx, yb, ldy, ytb, ldyt);
+  else if (src_dtype == RLA_F64)
+    rla::convert_bf16_pair_kernel<double><<<grid, block, 0, st>>>(rows, cols, static_cast<const double*>(x), ldx, yb, ldy, ytb, ldyt);
+  else
+    return RLA_ERR_ARG;
+  RLA_LAUNCH_CHECK();
+  return RLA_OK;
+}

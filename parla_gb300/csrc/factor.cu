@@ -212,6 +212,45 @@ __global__ void trtri_kernel(int64_t n, const typename Ar<V>::S* __restrict__ Rm
   for (int64_t i = lane; i < n; i += 32) R::st(X + i * ldx + c, i <= c ? x[i] : R::zero());
 }
 
+// Single-CTA Cholesky for small FP32 matrices held entirely in shared memory
+// (n <= 238): no grid barriers, one __syncthreads per stage.
+__global__ void __launch_bounds__(1024) potrf_small_f32_kernel(int n, float* __restrict__ G, int64_t ldg,
+                                                               int* __restrict__ info) {
+  extern __shared__ __align__(16) float a[];
+  __shared__ float s_piv;
+  __shared__ int s_bad;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, nw = blockDim.x >> 5;
+  for (int e = tid; e < n * n; e += blockDim.x) a[e] = G[static_cast<int64_t>(e / n) * ldg + (e % n)];
+  if (tid == 0) s_bad = 0;
+  __syncthreads();
+  for (int j = 0; j < n; ++j) {
+    if (tid == 0) {
+      float d = a[j * n + j];
+      int bad = !(d > 0.f && isfinite(d));
+      s_bad = bad;
+      s_piv = bad ? 1.f : sqrtf(d);
+      a[j * n + j] = s_piv;
+      if (bad) *info = j + 1;
+    }
+    __syncthreads();
+    if (s_bad) return;
+    const float ip = 1.f / s_piv;
+    for (int c = j + 1 + tid; c < n; c += blockDim.x) a[j * n + c] *= ip;
+    __syncthreads();
+    for (int c1 = j + 1 + warp; c1 < n; c1 += nw) {
+      const float r1 = a[j * n + c1];
+      for (int c2 = c1 + lane; c2 < n; c2 += 32) a[c1 * n + c2] = fmaf(-r1, a[j * n + c2], a[c1 * n + c2]);
+    }
+    __syncthreads();
+  }
+  for (int e = tid; e < n * n; e += blockDim.x) {
+    int r = e / n, c = e % n;
+    G[static_cast<int64_t>(r) * ldg + c] = c >= r ? a[e] : 0.f;
+  }
+}
+
+constexpr int kSmallPotrfMax = 238;
+
 }  // namespace
 }  // namespace rla
 
@@ -266,7 +305,16 @@ int rla_potrf_upper(int dtype, int64_t n, void* G, int64_t ldg, int* info, void*
   switch (dtype) {
     case RLA_F64: return coop_launch(potrf_kernel<double>, want, kFactThreads, 0, args, st);
     case RLA_DF: return coop_launch(potrf_kernel<df>, want, kFactThreads, 0, args, st);
-    case RLA_F32: return coop_launch(potrf_kernel<float>, want, kFactThreads, 0, args, st);
+    case RLA_F32:
+      if (n <= kSmallPotrfMax) {
+        size_t smem = static_cast<size_t>(n) * n * sizeof(float);
+        RLA_CUDA_TRY(cudaFuncSetAttribute(potrf_small_f32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          static_cast<int>(kSmallPotrfMax * kSmallPotrfMax * sizeof(float))));
+        potrf_small_f32_kernel<<<1, 1024, smem, st>>>(static_cast<int>(n), static_cast<float*>(G), ldg, info);
+        RLA_LAUNCH_CHECK();
+        return RLA_OK;
+      }
+      return coop_launch(potrf_kernel<float>, want, kFactThreads, 0, args, st);
     default: return RLA_ERR_ARG;
   }
 }

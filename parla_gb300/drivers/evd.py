@@ -10,6 +10,7 @@ import torch
 from .. import _kernels as K
 from ..comps.sketchers.aware import _times
 from ..utils import linalg_wrappers as law
+from ..utils import operand as opd
 
 EPS = np.finfo(float).eps
 
@@ -36,10 +37,10 @@ class EVD1(EVDecomposer):
             assert tol >= 0
             assert tol < np.inf
         rng = np.random.default_rng(rng)
-        Ad = A if isinstance(A, torch.Tensor) and A.is_cuda else K.to_dev(A, torch.float64)
-        Q, B = self.qb(Ad, k + over, tol / 2, rng)
-        Q64 = Q.to(torch.float64) if Q.dtype != torch.float64 else Q
-        B64 = B.to(torch.float64) if B.dtype != torch.float64 else B
+        Am = opd.wrap(A)
+        Q, B = self.qb(Am, k + over, tol / 2, rng)
+        Q64 = opd.panel_t(Q).to(torch.float64).t().contiguous()
+        B64 = B.to(torch.float64).contiguous()
         C = K.gemm(B64, Q64, mode="df")
         lam, U = law.sym_eig(C)
         alam = torch.abs(lam)

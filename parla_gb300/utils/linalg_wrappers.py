@@ -69,7 +69,7 @@ def small_svd_wide(B):
     lam, U = lam.flip(0), U.flip(1).contiguous()
     s = torch.sqrt(torch.clamp(lam, min=0.0))
     inv = torch.where(s > 0, 1.0 / s, torch.zeros_like(s))
-    Vh = K.gemm(U, B64, transa=True) * inv[:, None]
+    Vh = K.gemm(U.contiguous(), B64, transa=True, mode="df") * inv[:, None]
     return U, s, Vh.to(B.dtype) if B.dtype != torch.float64 else Vh
 
 
@@ -81,5 +81,59 @@ def small_svd_tall(B):
     lam, V = lam.flip(0), V.flip(1).contiguous()
     s = torch.sqrt(torch.clamp(lam, min=0.0))
     inv = torch.where(s > 0, 1.0 / s, torch.zeros_like(s))
-    U = K.gemm(B64, V) * inv[None, :]
+    U = K.gemm(B64, V.contiguous(), mode="df") * inv[None, :]
     return U.to(B.dtype) if B.dtype != torch.float64 else U, s, V.t().contiguous()
+
+
+def _chol_inv_f32(G):
+    """R^-1 of the Cholesky factor of an fp32 Gram; shifted once if not SPD.
+
+    The optimistic path does not synchronise: the kernel's pivot flag is read
+    by ``flush_checks`` once per driver call (see ``operand.DeviceMatrix``).
+    """
+    from .operand import current_checks
+    l = G.shape[0]
+    chk = current_checks()
+    if chk is not None and l <= 216:
+        flag = chk.new_flag()
+        return K.chol_inv_f32(G, info=flag)
+    for attempt in range(2):
+        Gs = G if attempt == 0 else G + (1e-5 * float(torch.trace(G)) / l + 1e-30) * torch.eye(
+            l, dtype=G.dtype, device=G.device)
+        try:
+            Rinv = K.chol_inv_f32(Gs)
+            if Rinv is None:
+                R = K.potrf_upper(Gs.clone(), mode="f32")
+                Rinv = K.trtri_upper(R, mode="f32")
+            return Rinv
+        except RlaError:
+            if attempt == 1:
+                raise
+    return None
+
+
+def orth_tc(Y, passes=1):
+    """CholeskyQR of an (m x l) panel stored transposed, Gram on the tensor cores.
+
+    Pass 1 forms G = Y^T Y from bf16 images of Y with fp32 accumulation
+    (tcgen05), factors it with the single-CTA fp32 Cholesky and applies
+    R^-1 in fp32.  The bf16 Gram is the exact Gram of a matrix within bf16
+    rounding of Y, so the result spans range(Y) with condition number O(10):
+    enough to stabilise the power iteration.  Further passes (passes >= 2)
+    use an fp32 Gram and bring the columns to fp32 orthonormality, which the
+    final range-finder basis needs.  Returns an (m x l) view of l x m storage.
+    """
+    from .operand import panel_t
+    Qt = panel_t(Y)
+    if Qt.dtype != torch.float32:
+        Qt = Qt.to(torch.float32)
+    l = Qt.shape[0]
+    for p in range(passes):
+        if p == 0:
+            Yb = K.convert(Qt, torch.bfloat16)
+            G = K.gemm_tc(Yb, Yb)
+        else:
+            G = K.gemm(Qt, Qt, transb=True, mode="f32")
+        Rinv = _chol_inv_f32(G)
+        Qt = K.gemm(Rinv, Qt, transa=True, mode="f32")
+    return Qt.t()

@@ -1,0 +1,119 @@
+"""A data matrix on the device together with the images the kernels need.
+
+The randomized SVD chain passes one ``DeviceMatrix`` down from the top-level
+driver, so the bf16 copies of A and A^T for the tensor-core passes are made
+once per driver call (one read of A, two bf16 writes) and shared by every
+pass of that call.  Nothing is cached across calls.
+
+``precision``:
+  'f64'  - binary64 SIMT products
+  'f32'  - binary32 SIMT products (the plain FP32 GPU path)
+  'bf16' - tcgen05 tensor-core products, bf16 operands, fp32 accumulation;
+           panels are kept transposed (l x m) so every product is K-major.
+"""
+import threading
+
+import torch
+
+from .. import _kernels as K
+
+
+class DeferredChecks:
+    """Device status flags of a driver call, read once at its end.
+
+    Small factorizations inside the chain run without synchronising; each
+    writes a pivot flag here.  ``failed()`` synchronises once and reports
+    whether any flag is set, in which case the driver repeats the call on the
+    guarded (synchronising, shift-on-failure) path.
+    """
+
+    def __init__(self):
+        self.flags = []
+
+    def new_flag(self):
+        f = torch.zeros(1, dtype=torch.int32, device=K.device())
+        self.flags.append(f)
+        return f
+
+    def failed(self):
+        if not self.flags:
+            return False
+        return bool(torch.cat(self.flags).any().item())
+
+
+_tls = threading.local()
+
+
+def current_checks():
+    return getattr(_tls, "checks", None)
+
+
+class deferred_checks:
+    """Context manager installing a DeferredChecks for the calling thread."""
+
+    def __enter__(self):
+        self.prev = current_checks()
+        _tls.checks = DeferredChecks()
+        return _tls.checks
+
+    def __exit__(self, *exc):
+        _tls.checks = self.prev
+
+
+class DeviceMatrix:
+
+    def __init__(self, A, precision=None):
+        self.A = A
+        if precision is None:
+            precision = "f32" if A.dtype == torch.float32 else "f64"
+        if precision not in ("f64", "f32", "bf16"):
+            raise ValueError(f"unknown precision {precision!r}")
+        self.precision = precision
+        self.shape = tuple(A.shape)
+        self.dtype = A.dtype if precision != "bf16" else torch.float32
+        self._pair = None
+
+    @property
+    def tc(self):
+        return self.precision == "bf16"
+
+    def bf16_pair(self):
+        if self._pair is None:
+            self._pair = K.convert_bf16_pair(self.A)
+        return self._pair
+
+    def t(self):
+        return self.A.t()
+
+
+def wrap(A, precision=None):
+    """DeviceMatrix for A (NumPy, tensor or DeviceMatrix)."""
+    if isinstance(A, DeviceMatrix):
+        return A
+    if isinstance(A, torch.Tensor) and A.is_cuda:
+        return DeviceMatrix(A.contiguous(), precision)
+    want = torch.float32 if precision in ("f32", "bf16") else None
+    import numpy as np
+    arr = np.asarray(A)
+    dt = want or (torch.float32 if arr.dtype == np.float32 else torch.float64)
+    return DeviceMatrix(K.to_dev(arr, dt), precision)
+
+
+def panel_t(S):
+    """Contiguous transposed storage (l x rows) of an (rows x l) panel."""
+    St = S.t()
+    return St if St.is_contiguous() else St.contiguous()
+
+
+def tc_times(Am, S):
+    """A @ S on the tensor cores; returns an (m x l) view of l x m storage."""
+    Ab, _ = Am.bf16_pair()
+    Wt = K.convert(panel_t(S), torch.bfloat16)
+    return K.gemm_tc(Ab, Wt, out_trans=True).t()
+
+
+def tc_times_t(Am, S):
+    """A.T @ S on the tensor cores; returns an (n x l) view of l x n storage."""
+    _, Abt = Am.bf16_pair()
+    Wt = K.convert(panel_t(S), torch.bfloat16)
+    return K.gemm_tc(Abt, Wt, out_trans=True).t()

@@ -162,3 +162,31 @@ def test_svd1_float32_accuracy(pg):
     err = float(torch.linalg.matrix_norm(Ad.double() - (Ug.double() * sg.double()) @ Vhg.double()))
     tail = np.sqrt(np.sum(s[k:] ** 2))
     assert err <= 1.01 * tail
+
+
+def test_svd1_bf16_tensor_core_path_within_one_percent(pg):
+    """bf16 tensor-core chain vs the plain fp32 chain on the same matrix."""
+    rng = np.random.default_rng(1)
+    m, n, k = 4096, 2048, 100
+    U, _ = np.linalg.qr(rng.standard_normal((m, n)))
+    V, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    s = np.arange(1, n + 1, dtype=float) ** -1.5 + 1e-4
+    A = ((U * s) @ V.T).astype(np.float32)
+    Ad = torch.from_numpy(A).cuda()
+    tail = np.sqrt(np.sum(s[k:] ** 2))
+    errs = {}
+    for prec in ("f32", "bf16"):
+        chain = pg.SVD1(pg.QB1(pg.RF1(pg.RS1(pg.SkOpGA(), 4))), precision=prec)
+        Ug, sg, Vhg = chain(Ad, k, np.nan, 10, 2)
+        errs[prec] = float(torch.linalg.matrix_norm(Ad.double() - (Ug.double() * sg.double()) @ Vhg.double()))
+    assert errs["f32"] <= 1.01 * tail
+    assert errs["bf16"] <= 1.01 * errs["f32"]
+
+
+def test_qb1_bf16_orthonormal_basis(pg):
+    rng = np.random.default_rng(3)
+    A = torch.from_numpy(rng.standard_normal((3000, 1500)).astype(np.float32)).cuda()
+    Q, B = pg.QB1(pg.RF1(pg.RS1(pg.SkOpGA(), 2)), precision="bf16")(A, 150, np.nan, 4)
+    Qd = Q.double()
+    assert float((Qd.t() @ Qd - torch.eye(150, dtype=torch.float64, device="cuda")).abs().max()) <= 1e-4
+    assert B.shape == (150, 1500)

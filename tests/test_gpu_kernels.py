@@ -234,3 +234,26 @@ def test_split_and_convert(K):
     assert rel(hi.double().cpu().numpy() + lo.double().cpu().numpy(), A) <= 2 ** -46
     At = K.convert(dev(A), torch.float32, transpose=True).cpu().numpy()
     assert rel(At, A.T.astype(np.float32)) <= 1e-7
+
+
+@pytest.mark.parametrize("n", [1, 17, 32, 33, 100, 210, 216])
+def test_chol_inv_f32(K, n):
+    rng = np.random.default_rng(n)
+    X = rng.standard_normal((3 * n + 5, n))
+    G = (X.T @ X + 0.5 * n * np.eye(n)).astype(np.float32)
+    Rinv, R = K.chol_inv_f32(dev(G), want_r=True)
+    R = R.cpu().numpy().astype(np.float64)
+    Rinv = Rinv.cpu().numpy().astype(np.float64)
+    Rref = la.cholesky(G.astype(np.float64), lower=False)
+    assert rel(R, Rref) <= 1e-5
+    assert rel(Rinv, la.inv(Rref)) <= 1e-5
+    assert np.allclose(np.tril(Rinv, -1), 0)
+
+
+def test_chol_inv_reports_not_spd(K):
+    from parla_gb300._lib import RlaError
+    G = np.eye(40, dtype=np.float32)
+    G[37, 37] = -1.0
+    with pytest.raises(RlaError) as ei:
+        K.chol_inv_f32(dev(G))
+    assert ei.value.status == 3 and "37" in str(ei.value)
