@@ -220,7 +220,88 @@ def run_ours(args):
     }
     if args.cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(A.cpu().numpy(), budget_s=args.cpu_budget)
+    del A, Ad_, A_host
+    torch.cuda.empty_cache()
+    if args.ls:
+        line["ls_single"] = bench_ls_single(torch, pg)
+        line["ls_batched"] = bench_ls_batched(torch, pg, args.ls_problems)
     print(json.dumps(line))
+
+
+def bench_ls_single(torch, pg):
+    """Sketch-and-precondition LS as the reference runs it (configs[0]):
+    A 20000 x 200, kappa 1e8, Gaussian sketch d = 4n, QR preconditioner,
+    tolerance 1e-12; plain FP64 GPU path vs the double-float path.
+    Gated error: ||A (x - x_lapack)|| / ||A x_lapack|| (x_lapack: FP64 LAPACK on the host)."""
+    import scipy.linalg as la
+    from parla_gb300.drivers.batched import make_problem
+    A, b, _ = make_problem(20000, 200, 1e8, 1e-6, 11)
+    An, bn = A.cpu().numpy(), b.cpu().numpy()
+    xr = la.lstsq(An, bn)[0]
+    out = {"workload": "SPO(SkOpGA, 4, 'qr') 20000x200 kappa=1e8, tol 1e-12"}
+    for prec in ("f64", "df"):
+        solver = pg.SPO(pg.SkOpGA(), 4, "qr", prec)
+        solver(A, b, 0.0, 1e-12, 200, 1, logging=False)
+        torch.cuda.synchronize()
+        reps = 5
+        t0 = time.perf_counter()
+        for r in range(reps):
+            x, log = solver(A, b, 0.0, 1e-12, 200, 2 + r, logging=False)
+        torch.cuda.synchronize()
+        dt = (time.perf_counter() - t0) / reps
+        xh = x.cpu().numpy()
+        out[prec] = {"solves_per_s": 1.0 / dt, "ms": dt * 1e3, "lsqr_itn": log.itn,
+                     "pred_err": float(la.norm(An @ (xh - xr)) / la.norm(An @ xr)),
+                     "x_err": float(la.norm(xh - xr) / la.norm(xr))}
+    out["speedup_df_vs_f64"] = out["df"]["solves_per_s"] / out["f64"]["solves_per_s"]
+    return out
+
+
+def bench_ls_batched(torch, pg, count):
+    """Batched LS (configs[2]): `count` problems, m log-uniform [2048, 65536],
+    n uniform [16, 512], m >= 16 n, kappa log-uniform [1e4, 1e10], noise 1e-8;
+    SJLT d = 4n, 8 nonzeros; stop at prediction error ~3e-11.  The batched
+    solver replays one CUDA graph; the plain FP64 GPU path solves the problems
+    one at a time with binary64 kernels."""
+    import scipy.linalg as la
+    from parla_gb300.drivers.batched import batch_shapes, make_problem
+    shapes = batch_shapes(count, 7)
+    probs = [make_problem(m, n, kap, 1e-8, 1000 + i)[:2] for i, (m, n, kap) in enumerate(shapes)]
+    torch.cuda.synchronize()
+    out = {"workload": f"{count} LS problems, SJLT d=4n nnz=8, target rel. prediction error 1e-10",
+           "problems": count, "total_A_GB": sum(A.numel() * 8 for A, _ in probs) / 1e9}
+    solver = pg.BatchedSPO(precision="mixed", streams=16)
+    replay = solver.capture(probs, rng=5)
+    replay()
+    torch.cuda.synchronize()
+    s_, e_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s_.record()
+    xs = replay()
+    e_.record()
+    torch.cuda.synchronize()
+    dt = s_.elapsed_time(e_) / 1e3
+    info = solver.info_from_plan(replay.plan)
+    out["batched"] = {"solves_per_s": count / dt, "ms": dt * 1e3,
+                      "lsqr_itn_mean": float(np.mean([i["itn"] for i in info])),
+                      "barrier_errors": int(sum(i["err"] != 0 for i in info))}
+    plain = pg.BatchedSPO(precision="f64")
+    plain(probs[:2], rng=1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    xp = plain(probs, rng=6)
+    torch.cuda.synchronize()
+    dtp = time.perf_counter() - t0
+    out["plain_fp64"] = {"solves_per_s": count / dtp, "ms": dtp * 1e3}
+    out["speedup"] = out["batched"]["solves_per_s"] / out["plain_fp64"]["solves_per_s"]
+    worst, worst_p = 0.0, 0.0
+    idx = [i for i in range(count) if shapes[i][0] * shapes[i][1] <= 4e6][:12]
+    for i in idx:
+        An = probs[i][0].cpu().numpy()
+        xr = la.lstsq(An, probs[i][1].cpu().numpy())[0]
+        worst = max(worst, float(la.norm(An @ (xs[i].cpu().numpy() - xr)) / la.norm(An @ xr)))
+        worst_p = max(worst_p, float(la.norm(An @ (xp[i].cpu().numpy() - xr)) / la.norm(An @ xr)))
+    out["pred_err_sampled"] = {"batched": worst, "plain_fp64": worst_p, "problems_checked": len(idx)}
+    return out
 
 
 def cpu_baseline(A, budget_s=30.0, steps=None):
@@ -294,6 +375,15 @@ def run_case(args):
         W = torch.randn((K_RANK + OVER, N_COLS), generator=g, device="cuda").to(torch.bfloat16)
         for _ in range(3):
             K.gemm_tc(X, W, out_trans=True)
+    elif args.case == "lsqr":
+        # one sketch-and-precondition LSQR solve, A 40000 x 300 (double-float on hi/lo planes)
+        A = torch.randn((40000, 300), generator=g, device="cuda", dtype=torch.float64)
+        b = torch.randn(40000, generator=g, device="cuda", dtype=torch.float64)
+        hi, lo = K.split_f64(A)
+        M = torch.eye(300, dtype=torch.float64, device="cuda") / 200.0
+        for _ in range(3):
+            h = K.lsqr_launch(None, M, b, None, 0.0, 0.0, 0.0, 0.0, 8, "df", (hi, lo), 0, 0.0)
+        torch.cuda.synchronize()
     elif args.case == "sjlt":
         m, n, d = 65536, 512, 2048
         A = torch.randn((m, n), generator=g, device="cuda", dtype=torch.float64)
@@ -305,7 +395,7 @@ def run_case(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--case", default=None, choices=["tc_pass", "sjlt"],
+    ap.add_argument("--case", default=None, choices=["tc_pass", "sjlt", "lsqr"],
                     help="run one small kernel case for a profiler capture and exit")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
@@ -314,6 +404,9 @@ def main():
     ap.add_argument("--cpu-baseline", dest="cpu_baseline", action="store_true", default=True)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--no-ls", dest="ls", action="store_false", default=True,
+                    help="skip the least-squares measurements (configs[0] and configs[2])")
+    ap.add_argument("--ls-problems", type=int, default=1024)
     args = ap.parse_args()
     if args.case:
         run_case(args)

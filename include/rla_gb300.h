@@ -164,6 +164,12 @@ int rla_geqrf(int dtype, int64_t m, int64_t n, int64_t nrhs, double* A,
               int64_t lda, double* tau, void* ws, size_t* ws_bytes,
               rla_stream_t stream);
 
+/* rla_geqrf with the cooperative grid capped at max_ctas CTAs (0 = no cap),
+ * so that the QRs of a batch of sketches can run concurrently. */
+int rla_geqrf_ctas(int dtype, int64_t m, int64_t n, int64_t nrhs, double* A,
+                   int64_t lda, double* tau, int max_ctas, void* ws,
+                   size_t* ws_bytes, rla_stream_t stream);
+
 /* Q (m x n, column-major) = thin orthonormal factor of rla_geqrf's result.
  * Replaces la.qr(Y)[0] at parla/comps/rangefinders.py:187 and orth,
  * parla/utils/linalg_wrappers.py:6-7. */
@@ -217,6 +223,76 @@ int rla_lsqr_run(int dtype, int64_t m, int64_t n, int64_t p, const double* A,
                  double btol, double conlim, int iter_lim, double* arnorms,
                  int* itn, int* istop, void* ws, size_t* ws_bytes,
                  rla_stream_t stream);
+
+/* Asynchronous form of rla_lsqr_run for batched solves: nothing is copied to
+ * the host and the stream is not synchronised.  out (device int[3]) receives
+ * itn, istop and the grid-barrier status; arnorms is a DEVICE array of
+ * iter_lim doubles.  max_ctas (0 = all SMs) caps the cooperative grid so that
+ * several problems can run concurrently on different streams.  ptol > 0 adds
+ * a stopping rule on the prediction error: stop (istop = 9) once the change
+ * ||Abar (z_k - z_{k-1})|| <= ptol ||b|| (at LSQR's linear rate this bounds
+ * the remaining ||Abar (z - z*)||).  dtype RLA_F64,
+ * RLA_DF, or RLA_F32 (A_hi read as binary32, binary32 arithmetic: the
+ * low-precision inner solve of iterative refinement). */
+int rla_lsqr_launch(int dtype, int64_t m, int64_t n, int64_t p, const double* A,
+                    const float* A_hi, const float* A_lo, int64_t lda,
+                    const double* M, int64_t ldm, double sqrt_delta,
+                    const double* b, double* z, int has_x0, double atol,
+                    double btol, double conlim, double ptol, int iter_lim,
+                    int max_ctas, int* out, double* arnorms, void* ws,
+                    size_t* ws_bytes, rla_stream_t stream);
+
+/* ---------------------------------------------- batched least squares */
+
+/* Batched forms for many independent problems of uneven shape: ONE launch of
+ * a persistent kernel whose CTAs take problems from an atomic queue, largest
+ * first (`order`, device int[nprob]), each problem solved by one CTA with
+ * block-level synchronisation only.  `next` is a device int used as the
+ * queue head (reset by the call).  Records are built on the host with
+ * rla_lsqr_record / the QR record layout {int64 m, n, nrhs, lda; double* A;
+ * double* tau} (rla_qr_record_size bytes) and copied to the device.
+ * Replace a Python loop of SPO calls (parla/drivers/least_squares.py:284-369). */
+size_t rla_qr_record_size(void);
+int rla_geqrf_batched(int dtype, const void* probs, const int* order,
+                      int nprob, int* next, rla_stream_t stream);
+
+/* Batched double-float Householder QR whose matrices are stored as FP32
+ * hi/lo planes (rla_split_f64 layout): records {int64 m, n, nrhs, lda;
+ * float* hi; float* lo; double* tau} (rla_qr_hl_record_size bytes), column
+ * major; mmax = largest m in the batch.  One CTA per problem, no grid
+ * barrier; the nrhs trailing columns receive Q^T times themselves. */
+size_t rla_qr_hl_record_size(void);
+int rla_geqrf_hl_batched(const void* probs, const int* order, int nprob,
+                         int64_t mmax, int* next, rla_stream_t stream);
+
+/* Batched X_p = R_p^-1 (binary64 output) for upper-triangular factors held
+ * as FP32 hi/lo planes (column-major, column stride ld, as rla_geqrf_hl_batched
+ * leaves them): records {int64 n, ld, ldx; float* hi;
+ * float* lo; double* X; int64 col0} (rla_trtri_record_size bytes), col0 =
+ * running sum of the preceding n; one warp per (problem, column), one launch. */
+size_t rla_trtri_record_size(void);
+int rla_trtri_hl_batched(const void* probs, int nprob, int64_t total_cols,
+                         int64_t nmax, rla_stream_t stream);
+
+/* (x, when not NULL, receives M z at the end of the solve.) */
+size_t rla_lsqr_record_size(void);
+size_t rla_lsqr_problem_ws(int64_t m, int64_t n, int64_t p, int iter_lim);
+int rla_lsqr_record(void* rec, int64_t m, int64_t n, int64_t p,
+                    const double* A, const float* A_hi, const float* A_lo,
+                    int64_t lda, const double* M, int64_t ldm,
+                    double sqrt_delta, const double* b, double* z, int has_x0,
+                    double atol, double btol, double conlim, double ptol,
+                    int iter_lim, int* out, double* arnorms, double* x,
+                    void* ws);
+int rla_lsqr_batched(int dtype, const void* probs, const int* order,
+                     int nprob, int64_t nmax, int* next, rla_stream_t stream);
+
+/* r = b - A x (m rows) in double-float from the hi/lo planes of A
+ * (rla_split_f64): the FP64-class residual of the refinement loop, replacing
+ * `A @ x_ske - b` at parla/drivers/least_squares.py:344. */
+int rla_residual_df(int64_t m, int64_t n, const float* A_hi, const float* A_lo,
+                    int64_t lda, const double* x, const double* b, double* r,
+                    rla_stream_t stream);
 
 /* ------------------------------------------------- elementwise helpers */
 

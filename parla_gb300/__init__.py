@@ -18,6 +18,8 @@ from .comps.determiter.logging import SketchAndPrecondLog
 from .comps.determiter.saddle import PrecondSaddleSolver, PcSS2
 from .comps.determiter.lsqr import lsqr, PrecondOperator
 from .drivers.least_squares import OverLstsqSolver, SPO, SSO1, dim_checks
+from .drivers.batched import BatchedSPO
 from .drivers.svd import SVDecomposer, SVD1
 from .drivers.evd import EVDecomposer, EVD1, EVD2
 from .utils.linalg_wrappers import orth, cholqr
+from .autotune import Tuner

@@ -345,3 +345,56 @@ def lsqr_run(A, M, b, z0, sqrt_delta, atol, btol, conlim, iter_lim, mode="f64", 
     nb = C.c_size_t(need)
     _timed("lsqr", 1, call, "rla_lsqr_run", *head, ptr(ws), C.byref(nb), stream())
     return z, istop.value, itn.value, arn[:itn.value].copy()
+
+
+def geqrf_colmajor_async(T, n, mode="df", max_ctas=0):
+    """Householder QR (column-major T, (n + nrhs) x m) with a capped grid; no sync."""
+    ncols, m = T.shape
+    tau = torch.empty(max(n, 1), dtype=torch.float64, device=T.device)
+    head = (MODES[mode], m, n, ncols - n, ptr(T), T.stride(0), ptr(tau), int(max_ctas))
+    need = size_query("rla_geqrf_ctas", *head)
+    ws = workspace(need)
+    nb = C.c_size_t(need)
+    _timed("geqrf", 1, call, "rla_geqrf_ctas", *head, ptr(ws), C.byref(nb), stream())
+    return tau
+
+
+class LsqrHandle:
+    """Device-side results of an asynchronous LSQR launch."""
+
+    def __init__(self, z, out, arn):
+        self.z, self.out, self.arn = z, out, arn
+
+    def result(self):
+        o = self.out.cpu().numpy()
+        itn = int(o[0])
+        return int(o[1]), itn, self.arn[:itn].cpu().numpy(), int(o[2])
+
+
+def lsqr_launch(A, M, b, z0, sqrt_delta, atol, btol, conlim, iter_lim, mode="df", split=None, max_ctas=0,
+                ptol=0.0):
+    """Asynchronous device LSQR; returns a LsqrHandle (nothing is synchronised)."""
+    m, n = A.shape if A is not None else split[0].shape
+    p = M.shape[1]
+    dev = M.device
+    z = torch.zeros(p, dtype=torch.float64, device=dev) if z0 is None else z0.clone().contiguous()
+    out = torch.zeros(3, dtype=torch.int32, device=dev)
+    arn = torch.zeros(max(iter_lim, 1), dtype=torch.float64, device=dev)
+    hi, lo = split if split is not None else (None, None)
+    lda = A.stride(0) if A is not None else hi.stride(0)
+    head = (MODES[mode], m, n, p, ptr(A), ptr(hi), ptr(lo), lda, ptr(M), M.stride(0), float(sqrt_delta), ptr(b),
+            ptr(z), int(z0 is not None), float(atol), float(btol), float(conlim), float(ptol), int(iter_lim),
+            int(max_ctas), ptr(out), ptr(arn))
+    need = size_query("rla_lsqr_launch", *head)
+    ws = workspace(need)
+    nb = C.c_size_t(need)
+    _timed("lsqr", 1, call, "rla_lsqr_launch", *head, ptr(ws), C.byref(nb), stream())
+    return LsqrHandle(z, out, arn)
+
+
+def residual_df(hi, lo, x, b):
+    m, n = hi.shape
+    r = torch.empty(m, dtype=torch.float64, device=hi.device)
+    _timed("residual_df", 1, call, "rla_residual_df", m, n, ptr(hi), ptr(lo), hi.stride(0), ptr(x), ptr(b), ptr(r),
+           stream())
+    return r

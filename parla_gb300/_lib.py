@@ -49,6 +49,16 @@ SIGNATURES = {
                          _p, _psz, _p],
     "rla_gemm_bf16_tc_status": [_p, C.POINTER(C.c_int), _p],
     "rla_geqrf": [_i32, _i64, _i64, _i64, _p, _i64, _p, _p, _psz, _p],
+    "rla_geqrf_ctas": [_i32, _i64, _i64, _i64, _p, _i64, _p, _i32, _p, _psz, _p],
+    "rla_lsqr_launch": [_i32, _i64, _i64, _i64, _p, _p, _p, _i64, _p, _i64, _f64, _p, _p, _i32, _f64, _f64,
+                        _f64, _f64, _i32, _i32, _p, _p, _p, _psz, _p],
+    "rla_residual_df": [_i64, _i64, _p, _p, _i64, _p, _p, _p, _p],
+    "rla_geqrf_batched": [_i32, _p, _p, _i32, _p, _p],
+    "rla_geqrf_hl_batched": [_p, _p, _i32, _i64, _p, _p],
+    "rla_trtri_hl_batched": [_p, _i32, _i64, _i64, _p],
+    "rla_lsqr_batched": [_i32, _p, _p, _i32, _i64, _p, _p],
+    "rla_lsqr_record": [_p, _i64, _i64, _i64, _p, _p, _p, _i64, _p, _i64, _f64, _p, _p, _i32, _f64, _f64, _f64,
+                        _f64, _i32, _p, _p, _p, _p],
     "rla_orgqr": [_i32, _i64, _i64, _p, _i64, _p, _p, _i64, _p, _psz, _p],
     "rla_potrf_upper": [_i32, _i64, _p, _i64, _p, _p, _psz, _p],
     "rla_chol_inv_f32": [_i64, _p, _i64, _p, _i64, _p, _i64, _p, _p],
@@ -75,6 +85,10 @@ def load(path=LIB_PATH):
                 f"{path} is not built; run `python -c 'import __graft_entry__ as g; g.build()'` "
                 "or `python -m parla_gb300._build` (needs nvcc)")
         lib = C.CDLL(path)
+        for name in ("rla_lsqr_problem_ws",):
+            getattr(lib, name).argtypes, getattr(lib, name).restype = [_i64, _i64, _i64, _i32], C.c_size_t
+        for name in ("rla_lsqr_record_size", "rla_qr_record_size", "rla_qr_hl_record_size", "rla_trtri_record_size"):
+            getattr(lib, name).argtypes, getattr(lib, name).restype = [], C.c_size_t
         for name, args in SIGNATURES.items():
             fn = getattr(lib, name)
             if name in ("rla_status_string",):

@@ -43,20 +43,22 @@ inline GridBar bar_from_ws(void* ws) {
 
 // ------------------------------------------------------------------ QR
 // A: m x (n + nrhs), column-major, column stride lda.
-template <typename V>
-__global__ void __launch_bounds__(kFactThreads)
-geqrf_kernel(int64_t m, int64_t n, int64_t nrhs, double* __restrict__ A, int64_t lda, double* __restrict__ tau,
-             GridBar bar) {
+// Householder QR of one column-major matrix by a grid of G CTAs (Coop: one
+// column per CTA cyclically, bounded grid barrier between columns) or by a
+// single CTA (G = 1, __syncthreads only: the batched one-CTA-per-problem form).
+template <typename V, bool Coop>
+__device__ __forceinline__ void geqrf_body(int64_t m, int64_t n, int64_t nrhs, double* __restrict__ A, int64_t lda,
+                                           double* __restrict__ tau, const GridBar& bar, const int G,
+                                           const unsigned blk) {
   using R = Ar<V>;
   __shared__ V red[32];
   __shared__ V s_beta, s_tau, s_scale;
   const int64_t ncols = n + nrhs;
-  const int G = gridDim.x;
   V beta_prev = R::zero(), scale_prev = R::zero();
   for (int64_t j = 0; j < n; ++j) {
     const double* colj = A + j * lda;
     // deferred write of the previous reflector (nobody reads column j-1 now)
-    if (j > 0 && ((j - 1) % G) == blockIdx.x) {
+    if (j > 0 && ((j - 1) % G) == blk) {
       double* cp = A + (j - 1) * lda;
       for (int64_t i = j + threadIdx.x; i < m; i += blockDim.x) R::st(cp + i, R::mul(R::ldcg(cp + i), scale_prev));
       if (threadIdx.x == 0) { R::st(cp + (j - 1), beta_prev); }
@@ -80,14 +82,14 @@ geqrf_kernel(int64_t m, int64_t n, int64_t nrhs, double* __restrict__ A, int64_t
         sc = R::div(R::one(), R::sub(alpha, beta));
       }
       s_beta = beta; s_tau = t; s_scale = sc;
-      if ((j % G) == blockIdx.x) R::st(tau + j, t);
+      if ((j % G) == blk) R::st(tau + j, t);
     }
     __syncthreads();
     const V beta = s_beta, t = s_tau, sc = s_scale;
     beta_prev = beta; scale_prev = sc;
     // apply H_j = I - tau v v^T (v = [1; sc * x_{j+1:}]) to owned trailing columns
     if (!R::is_zero(t)) {
-      for (int64_t c = j + 1 + ((blockIdx.x - (j + 1) % G + G) % G); c < ncols; c += G) {
+      for (int64_t c = j + 1 + ((blk - (j + 1) % G + G) % G); c < ncols; c += G) {
         double* cc = A + c * lda;
         V dot = R::zero();
         for (int64_t i = j + 1 + threadIdx.x; i < m; i += blockDim.x) dot = R::fma(dot, R::ldcg(colj + i), R::ldcg(cc + i));
@@ -100,12 +102,48 @@ geqrf_kernel(int64_t m, int64_t n, int64_t nrhs, double* __restrict__ A, int64_t
         __syncthreads();
       }
     }
-    if (!grid_sync(bar)) return;
+    if (Coop) {
+      if (!grid_sync(bar)) return;
+    } else {
+      __syncthreads();
+    }
   }
-  if (n > 0 && ((n - 1) % G) == blockIdx.x) {
+  if (n > 0 && ((n - 1) % G) == blk) {
     double* cp = A + (n - 1) * lda;
     for (int64_t i = n + threadIdx.x; i < m; i += blockDim.x) R::st(cp + i, R::mul(R::ldcg(cp + i), scale_prev));
     if (threadIdx.x == 0) R::st(cp + (n - 1), beta_prev);
+  }
+}
+
+template <typename V>
+__global__ void __launch_bounds__(kFactThreads)
+geqrf_kernel(int64_t m, int64_t n, int64_t nrhs, double* __restrict__ A, int64_t lda, double* __restrict__ tau,
+             GridBar bar) {
+  geqrf_body<V, true>(m, n, nrhs, A, lda, tau, bar, static_cast<int>(gridDim.x), blockIdx.x);
+}
+
+// One problem of a batched QR: column-major (n + nrhs) x m matrix at A.
+struct QrProblem {
+  int64_t m, n, nrhs, lda;
+  double* A;
+  double* tau;
+};
+
+template <typename V>
+__global__ void __launch_bounds__(kFactThreads)
+geqrf_batched_kernel(const QrProblem* __restrict__ probs, const int* __restrict__ order, int nprob,
+                     int* __restrict__ next) {
+  __shared__ int s_i;
+  const GridBar nobar{nullptr, nullptr, nullptr};
+  for (;;) {
+    if (threadIdx.x == 0) s_i = atomicAdd(next, 1);
+    __syncthreads();
+    const int i = s_i;
+    __syncthreads();
+    if (i >= nprob) return;
+    const QrProblem q = probs[order[i]];
+    geqrf_body<V, false>(q.m, q.n, q.nrhs, q.A, q.lda, q.tau, nobar, 1, 0u);
+    __syncthreads();
   }
 }
 
@@ -258,8 +296,16 @@ using namespace rla;
 
 extern "C" {
 
+int rla_geqrf_ctas(int dtype, int64_t m, int64_t n, int64_t nrhs, double* A, int64_t lda, double* tau, int max_ctas,
+                   void* ws, size_t* ws_bytes, rla_stream_t stream);
+
 int rla_geqrf(int dtype, int64_t m, int64_t n, int64_t nrhs, double* A, int64_t lda, double* tau, void* ws,
               size_t* ws_bytes, rla_stream_t stream) {
+  return rla_geqrf_ctas(dtype, m, n, nrhs, A, lda, tau, 0, ws, ws_bytes, stream);
+}
+
+int rla_geqrf_ctas(int dtype, int64_t m, int64_t n, int64_t nrhs, double* A, int64_t lda, double* tau, int max_ctas,
+                   void* ws, size_t* ws_bytes, rla_stream_t stream) {
   if (ws == nullptr && ws_bytes != nullptr) { *ws_bytes = kBarBytes; return RLA_OK; }
   if (m < n || n < 0 || nrhs < 0 || lda < m) return RLA_ERR_ARG;
   if (n == 0) return RLA_OK;
@@ -269,6 +315,7 @@ int rla_geqrf(int dtype, int64_t m, int64_t n, int64_t nrhs, double* A, int64_t 
   GridBar bar = bar_from_ws(ws);
   void* args[] = {&m, &n, &nrhs, &A, &lda, &tau, &bar};
   int want = static_cast<int>(imin(n + nrhs, 2LL * sm_count()));
+  if (max_ctas > 0) want = min(want, max_ctas);
   if (dtype == RLA_F64) return coop_launch(geqrf_kernel<double>, want, kFactThreads, 0, args, st);
   if (dtype == RLA_DF) return coop_launch(geqrf_kernel<df>, want, kFactThreads, 0, args, st);
   return RLA_ERR_ARG;
@@ -329,17 +376,23 @@ int rla_trtri_upper(int dtype, int64_t n, const void* R, int64_t ldr, void* X, i
   size_t vsz = dtype == RLA_F32 ? 4 : 8;
   size_t smem = static_cast<size_t>(warps) * n * vsz;
   if (smem > 200 * 1024) return RLA_ERR_UNSUPPORTED;
+  static thread_local int attr_dev = -1;
+  int dev = 0;
+  RLA_CUDA_TRY(cudaGetDevice(&dev));
+  if (attr_dev != dev) {  // once per device and host thread: up to 200 KB of dynamic smem
+    RLA_CUDA_TRY(cudaFuncSetAttribute(trtri_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    RLA_CUDA_TRY(cudaFuncSetAttribute(trtri_kernel<df>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    RLA_CUDA_TRY(cudaFuncSetAttribute(trtri_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    attr_dev = dev;
+  }
   switch (dtype) {
     case RLA_F64:
-      RLA_CUDA_TRY(cudaFuncSetAttribute(trtri_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
       trtri_kernel<double><<<grid, warps * 32, smem, st>>>(n, static_cast<const double*>(R), ldr, static_cast<double*>(X), ldx);
       break;
     case RLA_DF:
-      RLA_CUDA_TRY(cudaFuncSetAttribute(trtri_kernel<df>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
       trtri_kernel<df><<<grid, warps * 32, smem, st>>>(n, static_cast<const double*>(R), ldr, static_cast<double*>(X), ldx);
       break;
     case RLA_F32:
-      RLA_CUDA_TRY(cudaFuncSetAttribute(trtri_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
       trtri_kernel<float><<<grid, warps * 32, smem, st>>>(n, static_cast<const float*>(R), ldr, static_cast<float*>(X), ldx);
       break;
     default: return RLA_ERR_ARG;
@@ -349,3 +402,252 @@ int rla_trtri_upper(int dtype, int64_t n, const void* R, int64_t ldr, void* X, i
 }
 
 }  // extern "C"
+
+// Batched Householder QR, one CTA per problem from an atomic queue (largest
+// first by `order`); probs is a device array of {m, n, nrhs, lda, A, tau}.
+extern "C" size_t rla_qr_record_size(void) { return sizeof(rla::QrProblem); }
+
+extern "C" int rla_geqrf_batched(int dtype, const void* probs, const int* order, int nprob, int* next,
+                                 rla_stream_t stream) {
+  using namespace rla;
+  if (nprob < 0 || !probs || !order || !next) return RLA_ERR_ARG;
+  if (nprob == 0) return RLA_OK;
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  const auto* q = static_cast<const QrProblem*>(probs);
+  int per_sm = 0;
+  if (dtype == RLA_DF) {
+    RLA_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, geqrf_batched_kernel<df>, kFactThreads, 0));
+  } else if (dtype == RLA_F64) {
+    RLA_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, geqrf_batched_kernel<double>, kFactThreads, 0));
+  } else {
+    return RLA_ERR_ARG;
+  }
+  int grid = static_cast<int>(imin(nprob, static_cast<int64_t>(imax(per_sm, 1)) * sm_count()));
+  RLA_CUDA_TRY(cudaMemsetAsync(next, 0, sizeof(int), st));
+  if (dtype == RLA_DF) geqrf_batched_kernel<df><<<grid, kFactThreads, 0, st>>>(q, order, nprob, next);
+  else geqrf_batched_kernel<double><<<grid, kFactThreads, 0, st>>>(q, order, nprob, next);
+  RLA_LAUNCH_CHECK();
+  return RLA_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Batched double-float Householder QR on FP32 hi/lo planes.
+//
+// The sketch is stored as two float planes (x = hi + lo), so loads and
+// stores never touch GB300's slow FP64 pipe (a binary64-stored matrix would
+// need two FP64 conversions per element access).  One CTA per problem from
+// an atomic queue; per column j: the column is staged in shared memory as
+// double-float, its norm reduced by the block, then each warp updates whole
+// trailing columns (warp-level dot product + axpy, no block barrier per
+// column).  A 1 CTA-per-problem schedule needs no grid barrier at all.
+namespace rla {
+namespace {
+
+struct QrProblemHL {
+  int64_t m, n, nrhs, lda;  // column-major (n + nrhs) columns of length m, column stride lda
+  float* hi;
+  float* lo;
+  double* tau;
+};
+
+constexpr int kQrHLThreads = 512;
+
+__global__ void __launch_bounds__(kQrHLThreads)
+geqrf_hl_batched_kernel(const QrProblemHL* __restrict__ probs, const int* __restrict__ order, int nprob,
+                        int* __restrict__ next) {
+  extern __shared__ __align__(16) df xcol[];
+  __shared__ df red[32];
+  __shared__ df s_tau;
+  __shared__ int s_i;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (;;) {
+    if (threadIdx.x == 0) s_i = atomicAdd(next, 1);
+    __syncthreads();
+    const int pi = s_i;
+    __syncthreads();
+    if (pi >= nprob) return;
+    const QrProblemHL q = probs[order[pi]];
+    const int64_t m = q.m, ncols = q.n + q.nrhs, lda = q.lda;
+    for (int64_t j = 0; j < q.n; ++j) {
+      float* chi = q.hi + j * lda;
+      float* clo = q.lo + j * lda;
+      // stage column j (rows j..m-1), norm of the part below the diagonal
+      df sig{0.f, 0.f};
+      for (int64_t i = j + threadIdx.x; i < m; i += blockDim.x) {
+        df x{chi[i], clo[i]};
+        xcol[i - j] = x;
+        if (i > j) sig = df_add(sig, df_mul(x, x));
+      }
+      sig = block_sum_df(sig, red);
+      if (threadIdx.x == 0) {
+        df alpha = xcol[0];
+        df beta, t, sc;
+        if (sig.hi == 0.f) {
+          beta = alpha; t = df{0.f, 0.f}; sc = df{0.f, 0.f};
+        } else {
+          df nrm = df_sqrt(df_add(sig, df_mul(alpha, alpha)));
+          beta = alpha.hi > 0.f ? df_neg(nrm) : nrm;   // beta = -sign(alpha) ||x||
+          t = df_div(df_sub(beta, alpha), beta);
+          sc = df_div(df{1.f, 0.f}, df_sub(alpha, beta));
+        }
+        s_tau = t;
+        q.tau[j] = df_to_double(t);
+        xcol[0] = beta;                                  // R(j, j)
+        red[0] = sc;
+      }
+      __syncthreads();
+      const df t = s_tau, sc = red[0];
+      // v = [1; sc * x_{j+1:}]: store into the column (below the diagonal) and smem
+      for (int64_t i = j + threadIdx.x; i < m; i += blockDim.x) {
+        df v = (i == j) ? xcol[0] : df_mul(xcol[i - j], sc);
+        chi[i] = v.hi;
+        clo[i] = v.lo;
+        if (i > j) xcol[i - j] = v;
+      }
+      __syncthreads();
+      if (t.hi != 0.f) {
+        if (threadIdx.x == 0) xcol[0] = df{1.f, 0.f};
+        __syncthreads();
+        // each warp applies H_j to two trailing columns at a time (two
+        // independent accumulation chains hide the load latency)
+        for (int64_t c = j + 1 + 2 * warp; c < ncols; c += 2 * nw) {
+          const bool two = c + 1 < ncols;
+          float* ahi0 = q.hi + c * lda;
+          float* alo0 = q.lo + c * lda;
+          float* ahi1 = two ? ahi0 + lda : ahi0;
+          float* alo1 = two ? alo0 + lda : alo0;
+          df d0{0.f, 0.f}, d1{0.f, 0.f};
+          for (int64_t i = j + lane; i < m; i += 32) {
+            const df v = xcol[i - j];
+            const df a0{ahi0[i], alo0[i]}, a1{ahi1[i], alo1[i]};
+            d0 = df_add(d0, df_mul(v, a0));
+            d1 = df_add(d1, df_mul(v, a1));
+          }
+          d0 = warp_sum_df(d0);
+          d1 = warp_sum_df(d1);
+          const df w0 = df_mul(t, d0), w1 = df_mul(t, d1);
+          for (int64_t i = j + lane; i < m; i += 32) {
+            const df v = xcol[i - j];
+            const df a0 = df_sub(df{ahi0[i], alo0[i]}, df_mul(w0, v));
+            ahi0[i] = a0.hi;
+            alo0[i] = a0.lo;
+            if (two) {
+              const df a1 = df_sub(df{ahi1[i], alo1[i]}, df_mul(w1, v));
+              ahi1[i] = a1.hi;
+              alo1[i] = a1.lo;
+            }
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
+}  // namespace
+}  // namespace rla
+
+extern "C" size_t rla_qr_hl_record_size(void) { return sizeof(rla::QrProblemHL); }
+
+// Batched QR on hi/lo planes: records {int64 m, n, nrhs, lda; float* hi;
+// float* lo; double* tau} (rla_qr_hl_record_size bytes), mmax = largest m.
+extern "C" int rla_geqrf_hl_batched(const void* probs, const int* order, int nprob, int64_t mmax, int* next,
+                                    rla_stream_t stream) {
+  using namespace rla;
+  if (nprob < 0 || !probs || !order || !next || mmax <= 0) return RLA_ERR_ARG;
+  if (nprob == 0) return RLA_OK;
+  const size_t smem = static_cast<size_t>(mmax) * sizeof(df);
+  if (smem > 200 * 1024) return RLA_ERR_UNSUPPORTED;
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  static thread_local int attr_dev = -1;
+  int dev = 0;
+  RLA_CUDA_TRY(cudaGetDevice(&dev));
+  if (attr_dev != dev) {
+    RLA_CUDA_TRY(cudaFuncSetAttribute(geqrf_hl_batched_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    attr_dev = dev;
+  }
+  int per_sm = 0;
+  RLA_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, geqrf_hl_batched_kernel, kQrHLThreads, smem));
+  const int grid = static_cast<int>(imin(nprob, static_cast<int64_t>(imax(per_sm, 1)) * sm_count()));
+  RLA_CUDA_TRY(cudaMemsetAsync(next, 0, sizeof(int), st));
+  geqrf_hl_batched_kernel<<<grid, kQrHLThreads, smem, st>>>(static_cast<const QrProblemHL*>(probs), order, nprob, next);
+  RLA_LAUNCH_CHECK();
+  return RLA_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Batched inverse of upper-triangular factors stored as FP32 hi/lo planes
+// (column-major n x n, column stride ld): X = R^-1 (row-major binary64).  One warp per
+// (problem, column) over the whole batch in a single launch; the column's
+// entries live in shared memory as double-float, no FP64 conversions.
+namespace rla {
+namespace {
+struct TriInvProblem {
+  int64_t n, ld, ldx;
+  const float* hi;
+  const float* lo;
+  double* X;
+  int64_t col0;  // first global column index of this problem
+};
+
+constexpr int kTriWarps = 8;
+
+__global__ void __launch_bounds__(kTriWarps * 32)
+trtri_hl_batched_kernel(const TriInvProblem* __restrict__ probs, int nprob, int64_t total_cols, int64_t nmax) {
+  extern __shared__ __align__(16) df xs_tri[];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  df* x = xs_tri + static_cast<int64_t>(w) * nmax;
+  const int64_t gc = static_cast<int64_t>(blockIdx.x) * kTriWarps + w;
+  if (gc >= total_cols) return;
+  // locate the problem of this global column (binary search over col0)
+  int lo_i = 0, hi_i = nprob - 1;
+  while (lo_i < hi_i) {
+    int mid = (lo_i + hi_i + 1) >> 1;
+    if (probs[mid].col0 <= gc) lo_i = mid; else hi_i = mid - 1;
+  }
+  const TriInvProblem q = probs[lo_i];
+  const int64_t c = gc - q.col0;
+  // R is column-major with column stride ld (the layout the QR leaves it in)
+  auto R = [&](int64_t i, int64_t k) { return df{q.hi[k * q.ld + i], q.lo[k * q.ld + i]}; };
+  for (int64_t i = lane; i <= c; i += 32) x[i] = df{0.f, 0.f};
+  __syncwarp();
+  if (lane == 0) x[c] = df_div(df{1.f, 0.f}, R(c, c));
+  __syncwarp();
+  for (int64_t i = c - 1; i >= 0; --i) {
+    df acc{0.f, 0.f};
+    for (int64_t k = i + 1 + lane; k <= c; k += 32) acc = df_add(acc, df_mul(R(i, k), x[k]));
+    acc = warp_sum_df(acc);
+    if (lane == 0) x[i] = df_neg(df_div(acc, R(i, i)));
+    __syncwarp();
+  }
+  for (int64_t i = lane; i < q.n; i += 32) q.X[i * q.ldx + c] = i <= c ? df_to_double(x[i]) : 0.0;
+}
+}  // namespace
+}  // namespace rla
+
+extern "C" size_t rla_trtri_record_size(void) { return sizeof(rla::TriInvProblem); }
+
+// Batched X_p = R_p^-1 for upper-triangular R_p given as hi/lo planes;
+// records {int64 n, ld, ldx; float* hi; float* lo; double* X; int64 col0}
+// with col0 the running sum of the n of the preceding records.
+extern "C" int rla_trtri_hl_batched(const void* probs, int nprob, int64_t total_cols, int64_t nmax,
+                                    rla_stream_t stream) {
+  using namespace rla;
+  if (nprob < 0 || total_cols < 0 || nmax <= 0 || (nprob > 0 && !probs)) return RLA_ERR_ARG;
+  if (nprob == 0 || total_cols == 0) return RLA_OK;
+  const size_t smem = static_cast<size_t>(kTriWarps) * nmax * sizeof(df);
+  if (smem > 200 * 1024) return RLA_ERR_UNSUPPORTED;
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  static thread_local int attr_dev = -1;
+  int dev = 0;
+  RLA_CUDA_TRY(cudaGetDevice(&dev));
+  if (attr_dev != dev) {
+    RLA_CUDA_TRY(cudaFuncSetAttribute(trtri_hl_batched_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    attr_dev = dev;
+  }
+  const unsigned grid = static_cast<unsigned>(ceil_div(total_cols, kTriWarps));
+  trtri_hl_batched_kernel<<<grid, kTriWarps * 32, smem, st>>>(static_cast<const TriInvProblem*>(probs), nprob,
+                                                               total_cols, nmax);
+  RLA_LAUNCH_CHECK();
+  return RLA_OK;
+}

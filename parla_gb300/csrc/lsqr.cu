@@ -32,10 +32,12 @@ struct LsqrArgs {
   const double* b;
   double* z; int has_x0;
   double atol, btol, conlim;
+  double ptol;      // > 0: stop once the prediction change per step is below ptol * ||b||
   int iter_lim;
   double* arn;      // [iter_lim] device
   int* out;         // [2] itn, istop
   double* u; double* uext; double* v; double* w; double* y; double* t;
+  double* x;        // optional: x = M z written at the end (null: skip)
   double* part;     // [G] per-CTA partial sums
   double* tpart;    // [G][n] per-CTA partial A^T u
   GridBar bar;
@@ -51,6 +53,15 @@ template <> struct RowA<double> {
     return warp_sum(s);
   }
   __device__ static double at(const LsqrArgs& a, int64_t i, int64_t j) { return a.A[i * a.lda + j]; }
+};
+template <> struct RowA<float> {
+  __device__ static float dot(const LsqrArgs& a, int64_t i, const float* x, int lane) {
+    const float* r = a.Ahi + i * a.lda;
+    float s = 0.f;
+    for (int64_t j = lane; j < a.n; j += 32) s = fmaf(r[j], x[j], s);
+    return warp_sum(s);
+  }
+  __device__ static float at(const LsqrArgs& a, int64_t i, int64_t j) { return a.Ahi[i * a.lda + j]; }
 };
 template <> struct RowA<df> {
   __device__ static df dot(const LsqrArgs& a, int64_t i, const df* x, int lane) {
@@ -74,45 +85,89 @@ template <> struct RowA<df> {
   __device__ static df at(const LsqrArgs& a, int64_t i, int64_t j) { return df{a.Ahi[i * a.lda + j], a.Alo[i * a.lda + j]}; }
 };
 
+// Element loaders and a lazily renormalised multiply-accumulate for the
+// one-pass (fused) products.
+template <typename V> struct Elem;
+template <> struct Elem<double> {
+  __device__ static double ld(const LsqrArgs& a, int64_t i, int64_t j) { return a.A[i * a.lda + j]; }
+  __device__ static void mac(double& acc, double x, double y) { acc = fma(x, y, acc); }
+  __device__ static void renorm(double&) {}
+};
+template <> struct Elem<float> {
+  __device__ static float ld(const LsqrArgs& a, int64_t i, int64_t j) { return a.Ahi[i * a.lda + j]; }
+  __device__ static void mac(float& acc, float x, float y) { acc = fmaf(x, y, acc); }
+  __device__ static void renorm(float&) {}
+};
+template <> struct Elem<df> {
+  __device__ static df ld(const LsqrArgs& a, int64_t i, int64_t j) {
+    return df{a.Ahi[i * a.lda + j], a.Alo[i * a.lda + j]};
+  }
+  // acc += x * y: exact leading product, two_sum into hi, lazy lo
+  __device__ static void mac(df& acc, df x, df y) {
+    float p = x.hi * y.hi;
+    float pe = fmaf(x.hi, y.hi, -p);
+    pe = fmaf(x.hi, y.lo, fmaf(x.lo, y.hi, pe));
+    float s = acc.hi + p, bb = s - acc.hi;
+    float e = (acc.hi - (s - bb)) + (p - bb);
+    acc.hi = s;
+    acc.lo += e + pe;
+  }
+  __device__ static void renorm(df& acc) { acc = quick_two_sum(acc.hi, acc.lo); }
+};
+
 struct Scal {  // LSQR scalar state (binary64, thread 0 of each CTA)
   double alfa, beta, rhobar, phibar, anorm, acond, ddnorm, res2, xnorm, xxnorm, zz, cs2, sn2, bnorm, arnorm;
   double t1, t2, rho;  // per-iteration update coefficients
 };
 
+// Sum of the G per-CTA partials, identical in every CTA: warp 0 reads them in
+// parallel (lane l sums entries l, l+32, ... in order, then a fixed xor tree)
+// and broadcasts through shared memory.  All threads of the CTA must call it.
 template <typename V>
 __device__ double sum_parts(const double* part, int G) {
-  double s = 0.0;
-  for (int g = 0; g < G; ++g) s += __ldcg(part + g);
-  return s;
+  __shared__ double s_sum;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double acc = 0.0;
+    for (int g = threadIdx.x; g < G; g += 32) acc += __ldcg(part + g);
+    acc = warp_sum(acc);
+    if (threadIdx.x == 0) s_sum = acc;
+  }
+  __syncthreads();
+  return s_sum;
 }
 
-template <typename V>
-__global__ void __launch_bounds__(kLsqrThreads) lsqr_kernel(LsqrArgs a) {
-  using R = Ar<V>;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+// The LSQR iteration for one problem, run either by a cooperative grid of G
+// CTAs (Coop, grid barriers between phases) or by a single CTA (G = 1,
+// __syncthreads between phases: the batched solver's one-CTA-per-problem
+// form).  `blk` is this CTA's rank in the problem's grid.
+template <class P, bool Coop, int NPL>
+__device__ __forceinline__ void lsqr_body(const LsqrArgs& a, const int G, const int blk, unsigned char* smem_raw) {
+  using R = P;
+  using V = typename P::V;
   V* xs = reinterpret_cast<V*>(smem_raw);             // n entries: y or u chunk staging
   __shared__ V red[32];
-  __shared__ double s_bcast[4];
-  __shared__ int s_stop;
-  const int G = gridDim.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
-  const int64_t gtid = static_cast<int64_t>(blockIdx.x) * blockDim.x + tid;
+  __shared__ double redd[32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+  const int64_t gtid = static_cast<int64_t>(blk) * blockDim.x + tid;
   const int64_t gthreads = static_cast<int64_t>(G) * blockDim.x;
   const int64_t chunk = ceil_div(a.m, G);
-  const int64_t r0 = min(a.m, static_cast<int64_t>(blockIdx.x) * chunk), r1 = min(a.m, r0 + chunk);
+  const int64_t r0 = min(a.m, static_cast<int64_t>(blk) * chunk), r1 = min(a.m, r0 + chunk);
   const bool ext = a.sd > 0.0;
   Scal s{};
 
   // ---- helpers ------------------------------------------------------
   // y = M x (x: p-vector in global), rows of M distributed over all warps.
-  auto mat_M = [&](const double* x, double scale) {
-    for (int64_t i = static_cast<int64_t>(blockIdx.x) * nw + warp; i < a.n; i += static_cast<int64_t>(G) * nw) {
+  auto mat_M_to = [&](const double* x, double scale, double* dst) {
+    for (int64_t i = static_cast<int64_t>(blk) * nw + warp; i < a.n; i += static_cast<int64_t>(G) * nw) {
       const double* mr = a.M + i * a.ldm;
       V acc = R::zero();
       for (int64_t c = lane; c < a.p; c += 32) acc = R::fma(acc, R::ld(mr + c), R::ldcg(x + c));
       acc = R::wsum(acc);
-      if (lane == 0) R::st(a.y + i, R::mul(acc, R::from_d(scale)));
+      if (lane == 0) R::st(dst + i, R::mul(acc, R::from_d(scale)));
     }
   };
+  auto mat_M = [&](const double* x, double scale) { mat_M_to(x, scale, a.y); };
   // u_i = (A y)_i * ca + u_i * cu for own rows; returns this CTA's partial ||u||^2
   auto apply_A = [&](double ca, double cu, bool with_b) -> double {
     for (int64_t j = tid; j < a.n; j += blockDim.x) xs[j] = R::ldcg(a.y + j);
@@ -127,7 +182,7 @@ __global__ void __launch_bounds__(kLsqrThreads) lsqr_kernel(LsqrArgs a) {
         part = R::fma(part, ui, ui);
       }
     }
-    if (ext && blockIdx.x == 0) {
+    if (ext && blk == 0) {
       for (int64_t j = tid; j < a.n; j += blockDim.x) {
         V ue = with_b ? R::zero() : R::mul(R::from_d(cu), R::ldcg(a.uext + j));
         ue = R::add(ue, R::mul(R::from_d(ca * a.sd), xs[j]));
@@ -141,61 +196,117 @@ __global__ void __launch_bounds__(kLsqrThreads) lsqr_kernel(LsqrArgs a) {
   // u /= beta (own rows) and this CTA's partial A^T u -> tpart[blockIdx]
   auto apply_At = [&](double inv_beta) {
     for (int64_t i = r0 + tid; i < r1; i += blockDim.x) R::st(a.u + i, R::mul(R::ldcg(a.u + i), R::from_d(inv_beta)));
-    if (ext && blockIdx.x == 0)
+    if (ext && blk == 0)
       for (int64_t j = tid; j < a.n; j += blockDim.x) R::st(a.uext + j, R::mul(R::ldcg(a.uext + j), R::from_d(inv_beta)));
     __syncthreads();
     for (int64_t j = tid; j < a.n; j += blockDim.x) {
       V acc = R::zero();
       for (int64_t i = r0; i < r1; ++i) acc = R::fma(acc, RowA<V>::at(a, i, j), R::ldcg(a.u + i));
-      a.tpart[static_cast<int64_t>(blockIdx.x) * a.n + j] = R::to_d(acc);
+      a.tpart[static_cast<int64_t>(blk) * a.n + j] = R::to_d(acc);
     }
   };
-  // t_j = sum_g tpart[g][j] + sd * uext_j
-  auto reduce_t = [&]() {
-    for (int64_t j = gtid; j < a.n; j += gthreads) {
-      double acc = 0.0;
-      for (int g = 0; g < G; ++g) acc += __ldcg(a.tpart + static_cast<int64_t>(g) * a.n + j);
-      if (ext) acc += a.sd * __ldcg(a.uext + j);
-      a.t[j] = acc;
-    }
-  };
-  // v'_c = (M^T t)_c + cv * v_c for a block of 32 columns per CTA; partial ||v'||^2
-  auto apply_Mt = [&](double cv) -> double {
+  // One pass over own rows: u_i = ca (A y)_i + (with_b ? b_i : cu u_i), and
+  // this CTA's partial A^T u (of the NEW u) -> tpart[blk]; returns the
+  // partial ||u||^2.  Each element of A is loaded once and used for both
+  // products (NPL columns per lane, n <= 32 NPL).
+  auto apply_A_fused = [&](double ca, double cu, bool with_b) -> double {
+    for (int64_t j = tid; j < a.n; j += blockDim.x) xs[j] = R::ldcg(a.y + j);
+    __syncthreads();
+    V acc[NPL > 0 ? NPL : 1];
+#pragma unroll
+    for (int q = 0; q < (NPL > 0 ? NPL : 1); ++q) acc[q] = R::zero();
     V part = R::zero();
-    for (int64_t c0 = static_cast<int64_t>(blockIdx.x) * 32; c0 < a.p; c0 += static_cast<int64_t>(G) * 32) {
-      int64_t c = c0 + lane;
-      V acc = R::zero();
-      if (c < a.p)
-        for (int64_t j = warp; j < a.n; j += nw) acc = R::fma(acc, R::ld(a.M + j * a.ldm + c), R::ldcg(a.t + j));
-      xs[warp * 32 + lane] = acc;
-      __syncthreads();
-      if (warp == 0 && c < a.p) {
-        V tot = R::zero();
-        for (int q = 0; q < nw; ++q) tot = R::add(tot, xs[q * 32 + lane]);
-        V vn = R::add(tot, R::mul(R::from_d(cv), R::ldcg(a.v + c)));
-        R::st(a.v + c, vn);
-        part = R::fma(part, vn, vn);
+    const V vca = R::from_d(ca), vcu = R::from_d(cu);
+    int cnt = 0;
+    for (int64_t i = r0 + warp; i < r1; i += nw) {
+      V av[NPL > 0 ? NPL : 1];
+      V dot = R::zero();
+#pragma unroll
+      for (int q = 0; q < (NPL > 0 ? NPL : 1); ++q) {
+        const int64_t j = lane + 32 * q;
+        av[q] = j < a.n ? Elem<V>::ld(a, i, j) : R::zero();
+        if (j < a.n) Elem<V>::mac(dot, av[q], xs[j]);
       }
-      __syncthreads();
+      Elem<V>::renorm(dot);
+      dot = R::wsum(dot);
+      V ui = with_b ? R::ld(a.b + i) : R::mul(vcu, R::ldcg(a.u + i));
+      ui = R::add(ui, R::mul(vca, dot));
+      if (lane == 0) {
+        R::st(a.u + i, ui);
+        part = R::fma(part, ui, ui);
+      }
+#pragma unroll
+      for (int q = 0; q < (NPL > 0 ? NPL : 1); ++q) Elem<V>::mac(acc[q], av[q], ui);
+      if ((++cnt & 15) == 0) {
+#pragma unroll
+        for (int q = 0; q < (NPL > 0 ? NPL : 1); ++q) Elem<V>::renorm(acc[q]);
+      }
+    }
+    if (ext && blk == 0) {
+      for (int64_t j = tid; j < a.n; j += blockDim.x) {
+        V ue = with_b ? R::zero() : R::mul(vcu, R::ldcg(a.uext + j));
+        ue = R::add(ue, R::mul(R::from_d(ca * a.sd), xs[j]));
+        R::st(a.uext + j, ue);
+        part = R::fma(part, ue, ue);
+      }
+    }
+    // cross-warp sum of the A^T u partials (region after the y stage)
+    V* W = xs + a.n;
+#pragma unroll
+    for (int q = 0; q < (NPL > 0 ? NPL : 1); ++q) {
+      Elem<V>::renorm(acc[q]);
+      const int64_t j = lane + 32 * q;
+      if (j < a.n) W[static_cast<int64_t>(warp) * a.n + j] = acc[q];
+    }
+    __syncthreads();
+    for (int64_t j = tid; j < a.n; j += blockDim.x) {
+      V tot = R::zero();
+      for (int w = 0; w < nw; ++w) tot = R::add(tot, W[static_cast<int64_t>(w) * a.n + j]);
+      a.tpart[static_cast<int64_t>(blk) * a.n + j] = R::to_d(tot);
     }
     part = R::bsum(part, red);
     return R::to_d(part);
   };
-  auto bcast = [&](double v0, int slot) -> double {
-    if (tid == 0) s_bcast[slot] = v0;
-    __syncthreads();
-    double r = s_bcast[slot];
-    __syncthreads();
-    return r;
+  // t_j = scale * (sum_g tpart[g][j] + sd * uext_j): one warp per column,
+  // lanes split the G partials (fixed order), xor-tree reduction
+  auto reduce_t = [&](double scale) {
+    const int64_t gw = static_cast<int64_t>(blk) * nw + warp, nwarps_all = static_cast<int64_t>(G) * nw;
+    for (int64_t j = gw; j < a.n; j += nwarps_all) {
+      double acc = 0.0;
+      for (int g = lane; g < G; g += 32) acc += __ldcg(a.tpart + static_cast<int64_t>(g) * a.n + j);
+      acc = warp_sum(acc);
+      if (lane == 0) {
+        if (ext) acc += a.sd * __ldcg(a.uext + j);
+        a.t[j] = acc * scale;
+      }
+    }
   };
-#define RLA_SYNC() do { if (!grid_sync(a.bar)) return; } while (0)
+  // v'_c = (M^T t)_c + cv * v_c, one warp per column c over all CTAs (lanes
+  // split the n rows, fixed-order xor tree); returns this CTA's ||v'||^2
+  auto apply_Mt = [&](double cv) -> double {
+    V part = R::zero();
+    const int64_t gw = static_cast<int64_t>(blk) * nw + warp, nwarps_all = static_cast<int64_t>(G) * nw;
+    for (int64_t c = gw; c < a.p; c += nwarps_all) {
+      V acc = R::zero();
+      for (int64_t j = lane; j < a.n; j += 32) acc = R::fma(acc, R::ld(a.M + j * a.ldm + c), R::ldcg(a.t + j));
+      acc = R::wsum(acc);
+      if (lane == 0) {
+        V vn = R::add(acc, R::mul(R::from_d(cv), R::ldcg(a.v + c)));
+        R::st(a.v + c, vn);
+        part = R::fma(part, vn, vn);
+      }
+    }
+    part = R::bsum(part, red);
+    return R::to_d(part);
+  };
+#define RLA_SYNC() do { if (Coop) { if (!grid_sync(a.bar)) return; } else { __syncthreads(); } } while (0)
 
   // ---- initialisation -----------------------------------------------
   // The v buffer holds v' = alfa * v (unnormalised); readers scale by 1/alfa.
   double bnorm2 = 0.0;
   for (int64_t i = r0 + tid; i < r1; i += blockDim.x) { double bi = a.b[i]; bnorm2 = fma(bi, bi, bnorm2); }
-  bnorm2 = block_sum(bnorm2, reinterpret_cast<double*>(red));
-  if (tid == 0) a.part[blockIdx.x] = bnorm2;
+  bnorm2 = block_sum(bnorm2, redd);
+  if (tid == 0) a.part[blk] = bnorm2;
   if (a.has_x0) {
     mat_M(a.z, 1.0);
   } else {
@@ -205,25 +316,33 @@ __global__ void __launch_bounds__(kLsqrThreads) lsqr_kernel(LsqrArgs a) {
   s.bnorm = sqrt(sum_parts<V>(a.part, G));
   RLA_SYNC();
   double pu = 0.0;
-  if (a.has_x0) {
+  if (NPL > 0) {
+    // u = b - A y (y = M z0) or u = b (y unused), with A^T u in the same pass
+    pu = apply_A_fused(a.has_x0 ? -1.0 : 0.0, 0.0, true);
+  } else if (a.has_x0) {
     pu = apply_A(-1.0, 0.0, true);
   } else {
     for (int64_t i = r0 + tid; i < r1; i += blockDim.x) a.u[i] = a.b[i];
-    if (ext && blockIdx.x == 0) for (int64_t j = tid; j < a.n; j += blockDim.x) a.uext[j] = 0.0;
+    if (ext && blk == 0) for (int64_t j = tid; j < a.n; j += blockDim.x) a.uext[j] = 0.0;
     pu = bnorm2;
   }
-  if (tid == 0) a.part[blockIdx.x] = pu;
+  if (tid == 0) a.part[blk] = pu;
   RLA_SYNC();
   s.beta = a.has_x0 ? sqrt(sum_parts<V>(a.part, G)) : s.bnorm;
   s.alfa = 0.0;
+  double beta_prev = s.beta > 0.0 ? s.beta : 1.0;  // u is stored unnormalised (fused path)
   if (s.beta > 0.0) {
-    apply_At(1.0 / s.beta);
-    RLA_SYNC();
-    reduce_t();
+    if (NPL > 0) {
+      reduce_t(1.0 / s.beta);
+    } else {
+      apply_At(1.0 / s.beta);
+      RLA_SYNC();
+      reduce_t(1.0);
+    }
     for (int64_t c = gtid; c < a.p; c += gthreads) a.v[c] = 0.0;
     RLA_SYNC();
     double pv = apply_Mt(0.0);
-    if (tid == 0) a.part[blockIdx.x] = pv;
+    if (tid == 0) a.part[blk] = pv;
     RLA_SYNC();
     s.alfa = sqrt(sum_parts<V>(a.part, G));
   }
@@ -231,7 +350,11 @@ __global__ void __launch_bounds__(kLsqrThreads) lsqr_kernel(LsqrArgs a) {
   const double ctol = a.conlim > 0.0 ? 1.0 / a.conlim : 0.0;
   s.arnorm = s.alfa * s.beta;
   if (s.arnorm == 0.0) {
-    if (blockIdx.x == 0 && tid == 0) { a.out[0] = 0; a.out[1] = 0; }
+    if (blk == 0 && tid == 0) { a.out[0] = 0; a.out[1] = 0; }
+    if (a.x != nullptr) {
+      RLA_SYNC();
+      mat_M_to(a.z, 1.0, a.x);
+    }
     return;
   }
   {
@@ -244,31 +367,36 @@ __global__ void __launch_bounds__(kLsqrThreads) lsqr_kernel(LsqrArgs a) {
   s.anorm = s.acond = s.ddnorm = s.res2 = s.xnorm = s.xxnorm = s.zz = 0.0;
   s.cs2 = -1.0; s.sn2 = 0.0;
   int itn = 0, istop = 0;
+  double rnorm_prev = s.beta;
 
   // ---- main loop ----------------------------------------------------
   while (itn < a.iter_lim) {
-    if (blockIdx.x == 0 && tid == 0) a.arn[itn] = s.arnorm;
+    if (blk == 0 && tid == 0) a.arn[itn] = s.arnorm;
     ++itn;
-    // P2: u = A y - alfa u, and ||w||^2 for the ddnorm recurrence
-    double pu2 = apply_A(1.0, -s.alfa, false);
+    // P2: u = A y - alfa u (fused: with A^T u), and ||w||^2 for ddnorm
+    double pu2 = (NPL > 0) ? apply_A_fused(1.0, -s.alfa / beta_prev, false) : apply_A(1.0, -s.alfa, false);
     double pw = 0.0;
     for (int64_t c = gtid; c < a.p; c += gthreads) { double wc = a.w[c]; pw = fma(wc, wc, pw); }
-    pw = block_sum(pw, reinterpret_cast<double*>(red));
-    if (tid == 0) { a.part[blockIdx.x] = pu2; a.part[G + blockIdx.x] = pw; }
+    pw = block_sum(pw, redd);
+    if (tid == 0) { a.part[blk] = pu2; a.part[G + blk] = pw; }
     RLA_SYNC();
-    // P3: beta, u /= beta, partial A^T u
+    // P3/P4: beta, t = A^T u / beta
     s.beta = sqrt(sum_parts<V>(a.part, G));
     const double wnorm2 = sum_parts<V>(a.part + G, G);
     const double alfa_old = s.alfa;
     if (s.beta > 0.0) {
-      apply_At(1.0 / s.beta);
-      RLA_SYNC();
-      // P4
-      reduce_t();
+      if (NPL > 0) {
+        reduce_t(1.0 / s.beta);
+        beta_prev = s.beta;
+      } else {
+        apply_At(1.0 / s.beta);
+        RLA_SYNC();
+        reduce_t(1.0);
+      }
       RLA_SYNC();
       // P5: v' = M^T t - beta v, with v = v'_old / alfa_old
       double pv = apply_Mt(-s.beta / alfa_old);
-      if (tid == 0) a.part[blockIdx.x] = pv;
+      if (tid == 0) a.part[blk] = pv;
       RLA_SYNC();
       s.anorm = sqrt(s.anorm * s.anorm + s.alfa * s.alfa + s.beta * s.beta);
       s.alfa = sqrt(sum_parts<V>(a.part, G));
@@ -312,6 +440,9 @@ __global__ void __launch_bounds__(kLsqrThreads) lsqr_kernel(LsqrArgs a) {
     s.xxnorm += s.zz * s.zz;
     s.acond = s.anorm * sqrt(s.ddnorm);
     double rnorm = sqrt(s.phibar * s.phibar + s.res2);
+    // ||r_{k-1}||^2 - ||r_k||^2 = ||Abar (z_k - z_{k-1})||^2: the prediction change
+    const double dpred2 = fmax(rnorm_prev * rnorm_prev - rnorm * rnorm, 0.0);
+    rnorm_prev = rnorm;
     s.arnorm = s.alfa * fabs(tau);
     double test1 = rnorm / s.bnorm;
     double test2 = s.arnorm / (s.anorm * rnorm + eps);
@@ -325,13 +456,63 @@ __global__ void __launch_bounds__(kLsqrThreads) lsqr_kernel(LsqrArgs a) {
     if (test3 <= ctol) istop = 3;
     if (test2 <= a.atol) istop = 2;
     if (test1 <= rtol) istop = 1;
+    // prediction-error rule: with linear convergence at rate <= 1/2 the
+    // remaining ||Abar (z - z*)|| is at most the last change
+    if (a.ptol > 0.0 && itn >= 2 && sqrt(dpred2) <= a.ptol * s.bnorm) istop = 9;
     if (!isfinite(s.arnorm) || !isfinite(rnorm)) istop = 8;
     if (istop != 0) break;
     mat_M(a.v, vscale);
     RLA_SYNC();
   }
-  if (blockIdx.x == 0 && tid == 0) { a.out[0] = itn; a.out[1] = istop; }
+  if (blk == 0 && tid == 0) { a.out[0] = itn; a.out[1] = istop; }
+  if (a.x != nullptr) {  // x = M z
+    RLA_SYNC();
+    mat_M_to(a.z, 1.0, a.x);
+  }
 #undef RLA_SYNC
+}
+
+template <class P, int NPL>
+__device__ __forceinline__ void lsqr_dispatch(const LsqrArgs& a, int G, int blk, unsigned char* smem, bool coop) {
+  if (coop) lsqr_body<P, true, NPL>(a, G, blk, smem);
+  else lsqr_body<P, false, NPL>(a, G, blk, smem);
+}
+
+// NPL = columns per lane of the fused one-pass products (n <= 32 NPL);
+// 0 selects the two-pass form for wide problems.
+template <class P>
+__device__ __forceinline__ void lsqr_run_any(const LsqrArgs& a, int G, int blk, unsigned char* smem, bool coop) {
+  if (a.n <= 64) lsqr_dispatch<P, 2>(a, G, blk, smem, coop);
+  else if (a.n <= 128) lsqr_dispatch<P, 4>(a, G, blk, smem, coop);
+  else if (a.n <= 256) lsqr_dispatch<P, 8>(a, G, blk, smem, coop);
+  else if (a.n <= 512) lsqr_dispatch<P, 16>(a, G, blk, smem, coop);
+  else lsqr_dispatch<P, 0>(a, G, blk, smem, coop);
+}
+
+template <class P>
+__global__ void __launch_bounds__(kLsqrThreads) lsqr_kernel(LsqrArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  lsqr_run_any<P>(a, static_cast<int>(gridDim.x), static_cast<int>(blockIdx.x), smem_raw, true);
+}
+
+// Persistent batched form: each CTA takes the next problem (largest first,
+// `order`) from an atomic queue and solves it alone.
+template <class P>
+__global__ void __launch_bounds__(kLsqrThreads) lsqr_batched_kernel(const LsqrArgs* __restrict__ probs,
+                                                                     const int* __restrict__ order, int nprob,
+                                                                     int* __restrict__ next) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int s_i;
+  for (;;) {
+    if (threadIdx.x == 0) s_i = atomicAdd(next, 1);
+    __syncthreads();
+    const int i = s_i;
+    __syncthreads();
+    if (i >= nprob) return;
+    const LsqrArgs a = probs[order[i]];
+    lsqr_run_any<P>(a, 1, 0, smem_raw, false);
+    __syncthreads();
+  }
 }
 
 }  // namespace
@@ -360,14 +541,77 @@ inline LsqrWs lsqr_ws_layout(int64_t m, int64_t n, int64_t p, int G, int iter_li
   L.total = off;
   return L;
 }
-template <typename V>
+inline size_t lsqr_smem_bytes(int64_t n, size_t vsize) {
+  // y stage (n) + per-warp A^T u partials (8 warps x n), at least the
+  // 8 x 32 staging of the M^T t product
+  return static_cast<size_t>(imax(n + 8 * n, 256)) * vsize;
+}
+
+template <class P>
 int lsqr_grid(int64_t n, size_t* smem_out) {
-  size_t smem = static_cast<size_t>(imax(n, 256)) * sizeof(V);
+  size_t smem = lsqr_smem_bytes(n, sizeof(typename P::V));
   *smem_out = smem;
   int per_sm = 0;
-  if (smem > 48 * 1024) cudaFuncSetAttribute(lsqr_kernel<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lsqr_kernel<V>, kLsqrThreads, smem);
+  if (smem > 48 * 1024)
+    cudaFuncSetAttribute(lsqr_kernel<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lsqr_kernel<P>, kLsqrThreads, smem);
   return max(1, min(per_sm, 2)) * sm_count();
+}
+
+int lsqr_plan(int dtype, int64_t m, int64_t n, int max_ctas, size_t* smem) {
+  int G = 0;
+  if (dtype == RLA_DF) G = lsqr_grid<Ar<df>>(n, smem);
+  else if (dtype == RLA_F32) G = lsqr_grid<ArF32D>(n, smem);
+  else G = lsqr_grid<Ar<double>>(n, smem);
+  G = static_cast<int>(imin(G, imax(1, ceil_div(m, 8))));
+  if (max_ctas > 0) G = min(G, max_ctas);
+  return G;
+}
+
+// Enqueue the cooperative LSQR kernel.  out (device int[3]) receives itn,
+// istop and the barrier status; arn (device double[iter_lim]) the arnorms.
+int lsqr_enqueue(int dtype, int64_t m, int64_t n, int64_t p, const double* A, const float* A_hi, const float* A_lo,
+                 int64_t lda, const double* M, int64_t ldm, double sqrt_delta, const double* b, double* z, int has_x0,
+                 double atol, double btol, double conlim, double ptol, int iter_lim, int max_ctas, int* out,
+                 double* arn, void* ws, size_t* ws_bytes, cudaStream_t st) {
+  size_t smem = 0;
+  int G = lsqr_plan(dtype, m, n, max_ctas, &smem);
+  LsqrWs L = lsqr_ws_layout(m, n, p, G, iter_lim);
+  if (ws == nullptr && ws_bytes != nullptr) { *ws_bytes = L.total; return RLA_OK; }
+  if (!ws || (ws_bytes && *ws_bytes < L.total)) return RLA_ERR_WORKSPACE;
+  if (!b || !z || !M || !out || !arn) return RLA_ERR_ARG;
+  if (dtype == RLA_F64 && !A) return RLA_ERR_ARG;
+  if (dtype == RLA_DF && (!A_hi || !A_lo)) return RLA_ERR_ARG;
+  if (dtype == RLA_F32 && !A_hi) return RLA_ERR_ARG;
+  char* base = static_cast<char*>(ws);
+  RLA_CUDA_TRY(cudaMemsetAsync(base + L.bar, 0, 256, st));
+  RLA_CUDA_TRY(cudaMemsetAsync(out, 0, 3 * sizeof(int), st));
+  RLA_CUDA_TRY(cudaMemsetAsync(arn, 0, sizeof(double) * max(iter_lim, 1), st));
+  LsqrArgs a{};
+  a.m = m; a.n = n; a.p = p; a.A = A; a.Ahi = A_hi; a.Alo = A_lo; a.lda = lda; a.M = M; a.ldm = ldm;
+  a.sd = sqrt_delta; a.b = b; a.z = z; a.has_x0 = has_x0; a.atol = atol; a.btol = btol; a.conlim = conlim;
+  a.ptol = ptol;
+  a.iter_lim = iter_lim;
+  a.arn = arn;
+  a.out = out;
+  a.u = reinterpret_cast<double*>(base + L.u);
+  a.uext = reinterpret_cast<double*>(base + L.uext);
+  a.v = reinterpret_cast<double*>(base + L.v);
+  a.w = reinterpret_cast<double*>(base + L.w);
+  a.y = reinterpret_cast<double*>(base + L.y);
+  a.t = reinterpret_cast<double*>(base + L.t);
+  a.part = reinterpret_cast<double*>(base + L.part);
+  a.tpart = reinterpret_cast<double*>(base + L.tpart);
+  unsigned* barw = reinterpret_cast<unsigned*>(base + L.bar);
+  a.bar = GridBar{barw, barw + 1, out + 2};
+  void* args[] = {&a};
+  void* fn = nullptr;
+  if (dtype == RLA_DF) fn = reinterpret_cast<void*>(lsqr_kernel<Ar<df>>);
+  else if (dtype == RLA_F64) fn = reinterpret_cast<void*>(lsqr_kernel<Ar<double>>);
+  else if (dtype == RLA_F32) fn = reinterpret_cast<void*>(lsqr_kernel<ArF32D>);
+  else return RLA_ERR_ARG;
+  RLA_CUDA_TRY(cudaLaunchCooperativeKernel(fn, dim3(G), dim3(kLsqrThreads), args, smem, st));
+  return RLA_OK;
 }
 }  // namespace
 }  // namespace rla
@@ -379,25 +623,145 @@ extern "C" int rla_lsqr_run(int dtype, int64_t m, int64_t n, int64_t p, const do
                             rla_stream_t stream) {
   using namespace rla;
   if (m < 0 || n <= 0 || p <= 0 || iter_lim < 0 || lda < n || ldm < p) return RLA_ERR_ARG;
-  size_t smem = 0;
-  int G = (dtype == RLA_DF) ? lsqr_grid<df>(n, &smem) : lsqr_grid<double>(n, &smem);
-  G = static_cast<int>(imin(G, imax(1, ceil_div(m, 8))));
-  LsqrWs L = lsqr_ws_layout(m, n, p, G, iter_lim);
-  if (ws == nullptr && ws_bytes != nullptr) { *ws_bytes = L.total; return RLA_OK; }
-  if (!ws || (ws_bytes && *ws_bytes < L.total)) return RLA_ERR_WORKSPACE;
-  if (!b || !z || !M || !arnorms || !itn || !istop) return RLA_ERR_ARG;
-  if (dtype == RLA_F64 && !A) return RLA_ERR_ARG;
-  if (dtype == RLA_DF && (!A_hi || !A_lo)) return RLA_ERR_ARG;
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  // the sync entry point keeps its out/arn in the tail of the workspace
+  const size_t tail = 256 + sizeof(double) * static_cast<size_t>(max(iter_lim, 1));
+  size_t core = 0;
+  int rc = lsqr_enqueue(dtype, m, n, p, A, A_hi, A_lo, lda, M, ldm, sqrt_delta, b, z, has_x0, atol, btol, conlim,
+                        0.0, iter_lim, 0, nullptr, nullptr, nullptr, &core, st);
+  if (rc) return rc;
+  if (ws == nullptr && ws_bytes != nullptr) { *ws_bytes = core + tail; return RLA_OK; }
+  if (!ws || (ws_bytes && *ws_bytes < core + tail)) return RLA_ERR_WORKSPACE;
+  if (!arnorms || !itn || !istop) return RLA_ERR_ARG;
   char* base = static_cast<char*>(ws);
-  RLA_CUDA_TRY(cudaMemsetAsync(base + L.bar, 0, 256, st));
-  RLA_CUDA_TRY(cudaMemsetAsync(base + L.arn, 0, sizeof(double) * max(iter_lim, 1), st));
+  int* out = reinterpret_cast<int*>(base + core);
+  double* arn = reinterpret_cast<double*>(base + core + 256);
+  size_t cb = core;
+  rc = lsqr_enqueue(dtype, m, n, p, A, A_hi, A_lo, lda, M, ldm, sqrt_delta, b, z, has_x0, atol, btol, conlim,
+                    0.0, iter_lim, 0, out, arn, ws, &cb, st);
+  if (rc) return rc;
+  int hout[3] = {0, 0, 0};
+  RLA_CUDA_TRY(cudaMemcpyAsync(hout, out, sizeof(hout), cudaMemcpyDeviceToHost, st));
+  if (iter_lim > 0) RLA_CUDA_TRY(cudaMemcpyAsync(arnorms, arn, sizeof(double) * iter_lim, cudaMemcpyDeviceToHost, st));
+  RLA_CUDA_TRY(cudaStreamSynchronize(st));
+  *itn = hout[0];
+  *istop = hout[1];
+  if (hout[2] != 0) return hout[2];
+  if (hout[1] == 8) return RLA_ERR_NONFINITE;
+  return RLA_OK;
+}
+
+extern "C" int rla_lsqr_launch(int dtype, int64_t m, int64_t n, int64_t p, const double* A, const float* A_hi,
+                               const float* A_lo, int64_t lda, const double* M, int64_t ldm, double sqrt_delta,
+                               const double* b, double* z, int has_x0, double atol, double btol, double conlim,
+                               double ptol, int iter_lim, int max_ctas, int* out, double* arnorms, void* ws,
+                               size_t* ws_bytes, rla_stream_t stream) {
+  using namespace rla;
+  if (m < 0 || n <= 0 || p <= 0 || iter_lim < 0 || lda < n || ldm < p || max_ctas < 0 || ptol < 0) return RLA_ERR_ARG;
+  return lsqr_enqueue(dtype, m, n, p, A, A_hi, A_lo, lda, M, ldm, sqrt_delta, b, z, has_x0, atol, btol, conlim,
+                      ptol, iter_lim, max_ctas, out, arnorms, ws, ws_bytes, reinterpret_cast<cudaStream_t>(stream));
+}
+
+extern "C" int rla_split_f64(int64_t rows, int64_t cols, const double* x, int64_t ldx, float* hi, float* lo,
+                             int64_t ldh, rla_stream_t stream);
+
+namespace rla {
+namespace {
+// r = b - A x with A given as hi/lo FP32 planes, double-float dot products
+// (one warp per row); x is staged through shared memory as double-float.
+__global__ void residual_df_kernel(int64_t m, int64_t n, const float* __restrict__ Ahi, const float* __restrict__ Alo,
+                                   int64_t lda, const double* __restrict__ x, const double* __restrict__ b,
+                                   double* __restrict__ r) {
+  extern __shared__ __align__(16) df xs_res[];
+  for (int64_t j = threadIdx.x; j < n; j += blockDim.x) xs_res[j] = df_from_double(x[j]);
+  __syncthreads();
+  LsqrArgs a{};
+  a.n = n; a.Ahi = Ahi; a.Alo = Alo; a.lda = lda;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * nw + warp; i < m; i += static_cast<int64_t>(gridDim.x) * nw) {
+    df ax = RowA<df>::dot(a, i, xs_res, lane);
+    if (lane == 0) r[i] = df_to_double(df_sub(df_from_double(b[i]), ax));
+  }
+}
+}  // namespace
+}  // namespace rla
+
+extern "C" int rla_residual_df(int64_t m, int64_t n, const float* A_hi, const float* A_lo, int64_t lda,
+                               const double* x, const double* b, double* r, rla_stream_t stream) {
+  using namespace rla;
+  if (m < 0 || n <= 0 || lda < n) return RLA_ERR_ARG;
+  if (m == 0) return RLA_OK;
+  if (!A_hi || !A_lo || !x || !b || !r) return RLA_ERR_ARG;
+  size_t smem = static_cast<size_t>(n) * sizeof(df);
+  if (smem > 200 * 1024) return RLA_ERR_UNSUPPORTED;
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  if (smem > 48 * 1024)
+    RLA_CUDA_TRY(cudaFuncSetAttribute(residual_df_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+  unsigned grid = static_cast<unsigned>(imin(ceil_div(m, 8), 4LL * sm_count()));
+  residual_df_kernel<<<grid, 256, smem, st>>>(m, n, A_hi, A_lo, lda, x, b, r);
+  RLA_LAUNCH_CHECK();
+  return RLA_OK;
+}
+
+namespace rla {
+namespace {
+template <class P>
+int lsqr_batched_launch(const LsqrArgs* d_args, const int* d_order, int nprob, int* d_next, int64_t nmax,
+                        cudaStream_t st) {
+  size_t smem = lsqr_smem_bytes(nmax, sizeof(typename P::V));
+  if (smem > 200 * 1024) return RLA_ERR_UNSUPPORTED;
+  if (smem > 48 * 1024)
+    RLA_CUDA_TRY(cudaFuncSetAttribute(lsqr_batched_kernel<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      static_cast<int>(smem)));
+  int per_sm = 0;
+  RLA_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lsqr_batched_kernel<P>, kLsqrThreads, smem));
+  int grid = static_cast<int>(imin(nprob, static_cast<int64_t>(imax(per_sm, 1)) * sm_count()));
+  RLA_CUDA_TRY(cudaMemsetAsync(d_next, 0, sizeof(int), st));
+  lsqr_batched_kernel<P><<<grid, kLsqrThreads, smem, st>>>(d_args, d_order, nprob, d_next);
+  RLA_LAUNCH_CHECK();
+  return RLA_OK;
+}
+}  // namespace
+}  // namespace rla
+
+// Size of the per-problem LSQR workspace of the batched solver (one CTA per
+// problem): vectors u (m), v, w, z (p), y, t (n), partials and barrier words.
+extern "C" size_t rla_lsqr_problem_ws(int64_t m, int64_t n, int64_t p, int iter_lim) {
+  return rla::lsqr_ws_layout(m, n, p, 1, iter_lim).total;
+}
+
+// Batched LSQR: `probs` is a device array of nprob rla_lsqr_problem records
+// (one CTA per problem, largest first by `order`).
+extern "C" int rla_lsqr_batched(int dtype, const void* probs, const int* order, int nprob, int64_t nmax, int* next,
+                                rla_stream_t stream) {
+  using namespace rla;
+  if (nprob < 0 || !probs || !order || !next || nmax <= 0) return RLA_ERR_ARG;
+  if (nprob == 0) return RLA_OK;
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  const auto* a = static_cast<const LsqrArgs*>(probs);
+  if (dtype == RLA_DF) return lsqr_batched_launch<Ar<df>>(a, order, nprob, next, nmax, st);
+  if (dtype == RLA_F64) return lsqr_batched_launch<Ar<double>>(a, order, nprob, next, nmax, st);
+  if (dtype == RLA_F32) return lsqr_batched_launch<ArF32D>(a, order, nprob, next, nmax, st);
+  return RLA_ERR_ARG;
+}
+
+// Fill one LSQR problem record (host memory, sizeof = rla_lsqr_record_size())
+// from the same arguments as rla_lsqr_launch; ws must hold
+// rla_lsqr_problem_ws bytes.
+extern "C" size_t rla_lsqr_record_size(void) { return sizeof(rla::LsqrArgs); }
+
+extern "C" int rla_lsqr_record(void* rec, int64_t m, int64_t n, int64_t p, const double* A, const float* A_hi,
+                               const float* A_lo, int64_t lda, const double* M, int64_t ldm, double sqrt_delta,
+                               const double* b, double* z, int has_x0, double atol, double btol, double conlim,
+                               double ptol, int iter_lim, int* out, double* arnorms, double* x, void* ws) {
+  using namespace rla;
+  if (!rec || m < 0 || n <= 0 || p <= 0 || lda < n || ldm < p || !ws || !out || !arnorms) return RLA_ERR_ARG;
+  LsqrWs L = lsqr_ws_layout(m, n, p, 1, iter_lim);
+  char* base = static_cast<char*>(ws);
   LsqrArgs a{};
   a.m = m; a.n = n; a.p = p; a.A = A; a.Ahi = A_hi; a.Alo = A_lo; a.lda = lda; a.M = M; a.ldm = ldm;
   a.sd = sqrt_delta; a.b = b; a.z = z; a.has_x0 = has_x0; a.atol = atol; a.btol = btol; a.conlim = conlim;
-  a.iter_lim = iter_lim;
-  a.arn = reinterpret_cast<double*>(base + L.arn);
-  a.out = reinterpret_cast<int*>(base + L.out);
+  a.ptol = ptol; a.iter_lim = iter_lim; a.arn = arnorms; a.out = out; a.x = x;
   a.u = reinterpret_cast<double*>(base + L.u);
   a.uext = reinterpret_cast<double*>(base + L.uext);
   a.v = reinterpret_cast<double*>(base + L.v);
@@ -407,27 +771,7 @@ extern "C" int rla_lsqr_run(int dtype, int64_t m, int64_t n, int64_t p, const do
   a.part = reinterpret_cast<double*>(base + L.part);
   a.tpart = reinterpret_cast<double*>(base + L.tpart);
   unsigned* barw = reinterpret_cast<unsigned*>(base + L.bar);
-  a.bar = GridBar{barw, barw + 1, reinterpret_cast<int*>(barw + 2)};
-  void* args[] = {&a};
-  if (dtype == RLA_DF) {
-    RLA_CUDA_TRY(cudaLaunchCooperativeKernel(reinterpret_cast<void*>(lsqr_kernel<df>), dim3(G), dim3(kLsqrThreads), args, smem, st));
-  } else if (dtype == RLA_F64) {
-    RLA_CUDA_TRY(cudaLaunchCooperativeKernel(reinterpret_cast<void*>(lsqr_kernel<double>), dim3(G), dim3(kLsqrThreads), args, smem, st));
-  } else {
-    return RLA_ERR_ARG;
-  }
-  int hout[2] = {0, 0};
-  int herr = 0;
-  RLA_CUDA_TRY(cudaMemcpyAsync(hout, base + L.out, sizeof(hout), cudaMemcpyDeviceToHost, st));
-  RLA_CUDA_TRY(cudaMemcpyAsync(&herr, base + L.bar + 8, sizeof(int), cudaMemcpyDeviceToHost, st));
-  if (iter_lim > 0) RLA_CUDA_TRY(cudaMemcpyAsync(arnorms, base + L.arn, sizeof(double) * iter_lim, cudaMemcpyDeviceToHost, st));
-  RLA_CUDA_TRY(cudaStreamSynchronize(st));
-  *itn = hout[0];
-  *istop = hout[1];
-  if (herr != 0) return herr;
-  if (hout[1] == 8) return RLA_ERR_NONFINITE;
+  a.bar = GridBar{barw, barw + 1, out + 2};
+  *static_cast<LsqrArgs*>(rec) = a;
   return RLA_OK;
 }
-
-extern "C" int rla_split_f64(int64_t rows, int64_t cols, const double* x, int64_t ldx, float* hi, float* lo,
-                             int64_t ldh, rla_stream_t stream);
