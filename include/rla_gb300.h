@@ -192,6 +192,25 @@ int rla_potrf_upper(int dtype, int64_t n, void* G, int64_t ldg, int* info,
 int rla_trtri_upper(int dtype, int64_t n, const void* R, int64_t ldr, void* X,
                     int64_t ldx, rla_stream_t stream);
 
+/* Double-float Cholesky G = R^T R of a small binary64 SPD matrix (n <= 232),
+ * one CTA with the packed upper triangle in shared memory.  R (upper,
+ * row-major) is written rounded to binary32 (R32) and/or binary64 (R64);
+ * either may be NULL.  *info (device) = j+1 if pivot j was not positive.
+ * First step of the small SVD below (replaces the Gram side of la.svd(B),
+ * parla/drivers/svd.py:164, and la.eigh(C), parla/drivers/evd.py:279). */
+int rla_potrf_df_small(int64_t n, const double* G, int64_t ldg, float* R32, int64_t ldr,
+                       double* R64, int64_t ldr64, int* info, rla_stream_t stream);
+
+/* SVD of a small square matrix C (n <= 448) by one-sided Jacobi on one
+ * thread-block cluster.  Ct holds C^T row-major (row c = column c of C).
+ * Writes U (n x n row-major; column r = r-th left singular vector) and
+ * s (n, descending).  info[0] = 1 if max_sweeps ran out, info[1] = sweeps.
+ * dtype: RLA_F32.  cluster: CTAs in the cluster (1..8, 0 = automatic).
+ * With C = R^T from rla_potrf_df_small of G = B B^T this gives U and s of B
+ * (parla/drivers/svd.py:164; parla/drivers/evd.py:279). */
+int rla_svd_jacobi(int dtype, int64_t n, const void* Ct, int64_t ldc, void* U, int64_t ldu, void* s,
+                   int* info, int max_sweeps, int cluster, rla_stream_t stream);
+
 /* Rinv = R^-1 where G = R^T R (upper Cholesky), FP32, n <= 216, in one CTA
  * with G resident in shared memory; R is also written when R != NULL.
  * *info (device) = j+1 if pivot j was not positive, else 0.  Used by the

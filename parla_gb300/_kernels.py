@@ -278,6 +278,42 @@ def chol_inv_f32(G, want_r=False, info=None):
     return (Rinv, R) if want_r else Rinv
 
 
+def potrf_df_small(G, info=None, want64=False):
+    """Upper Cholesky factor of a binary64 SPD matrix (n <= 232) in double-float.
+
+    Returns R rounded to FP32 (and the binary64 R when ``want64``), or None when
+    n is too large for the single-CTA kernel.  ``info`` as in chol_inv_f32.
+    """
+    n = G.shape[0]
+    if n > 232:
+        return None
+    R32 = torch.empty((n, n), dtype=torch.float32, device=G.device)
+    R64 = torch.empty((n, n), dtype=torch.float64, device=G.device) if want64 else None
+    inf = info if info is not None else torch.zeros(1, dtype=torch.int32, device=G.device)
+    _timed("potrf_df_small", 1, call, "rla_potrf_df_small", n, ptr(G), G.stride(0), ptr(R32), n, ptr(R64), n,
+           ptr(inf), stream())
+    if info is None:
+        bad = int(inf.item())
+        if bad:
+            raise _lib.RlaError("rla_potrf_df_small", 3, f"pivot {bad - 1} not positive")
+    return (R32, R64) if want64 else R32
+
+
+def svd_jacobi(Ct, max_sweeps=40, info=None, cluster=0):
+    """U, s of C (n x n, FP32) from C^T by one-sided Jacobi on one CTA cluster.
+
+    ``info``: optional int32 device tensor of 2 (not-converged flag, sweeps);
+    ``cluster``: CTAs in the cluster (0 = automatic).
+    """
+    n = Ct.shape[0]
+    U = torch.empty((n, n), dtype=torch.float32, device=Ct.device)
+    s = torch.empty((n,), dtype=torch.float32, device=Ct.device)
+    inf = info if info is not None else torch.zeros(2, dtype=torch.int32, device=Ct.device)
+    _timed("svd_jacobi", 1, call, "rla_svd_jacobi", MODES["f32"], n, ptr(Ct), Ct.stride(0), ptr(U), n, ptr(s),
+           ptr(inf), max_sweeps, cluster, stream())
+    return U, s, inf
+
+
 def trtri_upper(R, mode=None):
     if mode is None:
         mode = "f32" if R.dtype == torch.float32 else "f64"

@@ -62,6 +62,8 @@ SIGNATURES = {
     "rla_orgqr": [_i32, _i64, _i64, _p, _i64, _p, _p, _i64, _p, _psz, _p],
     "rla_potrf_upper": [_i32, _i64, _p, _i64, _p, _p, _psz, _p],
     "rla_chol_inv_f32": [_i64, _p, _i64, _p, _i64, _p, _i64, _p, _p],
+    "rla_potrf_df_small": [_i64, _p, _i64, _p, _i64, _p, _i64, _p, _p],
+    "rla_svd_jacobi": [_i32, _i64, _p, _i64, _p, _i64, _p, _p, _i32, _i32, _p],
     "rla_trtri_upper": [_i32, _i64, _p, _i64, _p, _i64, _p],
     "rla_lsqr_run": [_i32, _i64, _i64, _i64, _p, _p, _p, _i64, _p, _i64, _f64, _p, _p, _i32, _f64, _f64,
                      _f64, _i32, _p, _p, _p, _p, _psz, _p],

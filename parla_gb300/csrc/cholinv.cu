@@ -6,9 +6,9 @@
 //   Cholesky (right-looking): warp-level factor of the 32 x 32 diagonal block,
 //     per-column forward substitution for the panel row, 4 x 4 register tiles
 //     for the symmetric trailing update;
-//   inverse (left-looking, in place): warp-level inverse of each diagonal
-//     block, W = X_tl R_blk with the already inverted leading block, then
-//     X_blk = -W D^-1.
+//   inverse (left-looking, in place): all diagonal blocks inverted at once,
+//     one warp per block; then per block column W = X_tl R_blk with the
+//     already inverted leading block, and X_blk = -W D^-1.
 // Replaces the pair potrf + trtri of the CholeskyQR stabilizer: one launch
 // instead of two grid-wide factorizations.
 #include "common.cuh"
@@ -17,7 +17,7 @@ namespace rla {
 namespace {
 
 constexpr int kCholInvMax = 216;
-constexpr int kCiThreads = 512;
+constexpr int kCiThreads = 384;
 constexpr int kNB = 32;
 
 __global__ void __launch_bounds__(kCiThreads, 1)
@@ -27,10 +27,11 @@ chol_inv_kernel(int n, const float* __restrict__ G, int64_t ldg, float* __restri
   const int LD = n + 1;
   float* a = smem;                        // n x LD
   float* W = a + n * LD;                  // n x kNB scratch
-  float* Dinv = W + n * kNB;              // kNB x kNB
+  float* dinv = W + n * kNB;              // kNB reciprocal pivots of the current block
   __shared__ int s_bad;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nthreads = blockDim.x;
+  const int nblk = (n + kNB - 1) / kNB;
 
   for (int e = tid; e < n * n; e += nthreads) {
     int r = e / n, c = e % n;
@@ -66,26 +67,29 @@ chol_inv_kernel(int n, const float* __restrict__ G, int64_t ldg, float* __restri
 #pragma unroll
       for (int r = 0; r < kNB; ++r)
         if (r < nb && lane < nb && lane >= r) a[(jb + r) * LD + jb + lane] = col[r];
+      if (lane < nb) dinv[lane] = 1.f / col[lane];
       if (lane == 0 && bad) { s_bad = bad; *info = bad; }
     }
     __syncthreads();
     if (s_bad) return;
-    // panel row: rows jb..jb+nb, columns c >= jb+nb: R_d^T X = G_panel
+    // panel row: rows jb..jb+nb, columns c >= jb+nb: solve R_d^T X = G_panel,
+    // column-oriented so each step is one multiply plus independent FMAs
     for (int c = jb + nb + tid; c < n; c += nthreads) {
-      float x[kNB];
+      float v[kNB];
 #pragma unroll
-      for (int i = 0; i < kNB; ++i) {
-        if (i < nb) {
-          float v = a[(jb + i) * LD + c];
+      for (int i = 0; i < kNB; ++i) v[i] = i < nb ? a[(jb + i) * LD + c] : 0.f;
 #pragma unroll
-          for (int p = 0; p < kNB; ++p)
-            if (p < i) v = fmaf(-a[(jb + p) * LD + jb + i], x[p], v);
-          x[i] = v / a[(jb + i) * LD + jb + i];
+      for (int p = 0; p < kNB; ++p) {
+        if (p < nb) {
+          v[p] *= dinv[p];
+#pragma unroll
+          for (int i = p + 1; i < kNB; ++i)
+            if (i < nb) v[i] = fmaf(-a[(jb + p) * LD + jb + i], v[p], v[i]);
         }
       }
 #pragma unroll
       for (int i = 0; i < kNB; ++i)
-        if (i < nb) a[(jb + i) * LD + c] = x[i];
+        if (i < nb) a[(jb + i) * LD + c] = v[i];
     }
     __syncthreads();
     // trailing update on 4 x 4 register tiles of the upper triangle
@@ -99,23 +103,23 @@ chol_inv_kernel(int n, const float* __restrict__ G, int64_t ldg, float* __restri
         float acc[4][4] = {};
         for (int p = 0; p < nb; ++p) {
           const float* prow = a + (jb + p) * LD;
-          float u[4], v[4];
+          float u[4], w[4];
 #pragma unroll
           for (int q = 0; q < 4; ++q) {
             u[q] = (r0 + q < n) ? prow[r0 + q] : 0.f;
-            v[q] = (c0 + q < n) ? prow[c0 + q] : 0.f;
+            w[q] = (c0 + q < n) ? prow[c0 + q] : 0.f;
           }
 #pragma unroll
           for (int q = 0; q < 4; ++q)
 #pragma unroll
-            for (int w = 0; w < 4; ++w) acc[q][w] = fmaf(u[q], v[w], acc[q][w]);
+            for (int z = 0; z < 4; ++z) acc[q][z] = fmaf(u[q], w[z], acc[q][z]);
         }
 #pragma unroll
         for (int q = 0; q < 4; ++q)
 #pragma unroll
-          for (int w = 0; w < 4; ++w) {
-            const int r = r0 + q, c = c0 + w;
-            if (r < n && c < n && c >= r) a[r * LD + c] -= acc[q][w];
+          for (int z = 0; z < 4; ++z) {
+            const int r = r0 + q, c = c0 + z;
+            if (r < n && c < n && c >= r) a[r * LD + c] -= acc[q][z];
           }
       }
     }
@@ -129,26 +133,32 @@ chol_inv_kernel(int n, const float* __restrict__ G, int64_t ldg, float* __restri
   }
 
   // ------------------------------------------- in-place inverse (upper)
-  for (int jb = 0; jb < n; jb += kNB) {
-    const int nb = min(kNB, n - jb);
-    if (warp == 0) {
-      // Dinv = inverse of the diagonal block; lane c computes column c
-      float x[kNB];
-      const int c = lane;
+  // All diagonal blocks are inverted at once (warp b inverts block b, lane c
+  // solves R_bb x = e_c column-oriented from the bottom), written over R_bb.
+  if (warp < nblk) {
+    const int jb = warp * kNB, nb = min(kNB, n - jb);
+    float x[kNB];
 #pragma unroll
-      for (int i = 0; i < kNB; ++i) x[i] = 0.f;
-      if (c < nb) {
-        x[c] = 1.f / a[(jb + c) * LD + jb + c];
-        for (int i = c - 1; i >= 0; --i) {
-          float s = 0.f;
-          for (int p = i + 1; p <= c; ++p) s = fmaf(a[(jb + i) * LD + jb + p], x[p], s);
-          x[i] = -s / a[(jb + i) * LD + jb + i];
-        }
+    for (int i = 0; i < kNB; ++i) x[i] = (i == lane) ? 1.f : 0.f;
+#pragma unroll
+    for (int i = kNB - 1; i >= 0; --i) {
+      if (i < nb) {
+        x[i] = (i <= lane) ? x[i] / a[(jb + i) * LD + jb + i] : 0.f;
+#pragma unroll
+        for (int q = 0; q < i; ++q) x[q] = fmaf(-a[(jb + q) * LD + jb + i], x[i], x[q]);
       }
-#pragma unroll
-      for (int i = 0; i < kNB; ++i) Dinv[i * kNB + c] = (c < nb && i <= c) ? x[i] : 0.f;
     }
-    // W = X_tl (jb x jb, upper, already inverted) * R_blk (jb x nb)
+    __syncwarp();
+    if (lane < nb) {
+#pragma unroll
+      for (int i = 0; i < kNB; ++i)
+        if (i < nb && i <= lane) a[(jb + i) * LD + jb + lane] = x[i];
+    }
+  }
+  __syncthreads();
+  // block column j: X[0:jb, j] = -(X[0:jb, 0:jb] R[0:jb, j]) X_jj
+  for (int jb = kNB; jb < n; jb += kNB) {
+    const int nb = min(kNB, n - jb);
     for (int e = tid; e < jb * nb; e += nthreads) {
       const int r = e / nb, c = e % nb;
       float s = 0.f;
@@ -156,16 +166,11 @@ chol_inv_kernel(int n, const float* __restrict__ G, int64_t ldg, float* __restri
       W[r * kNB + c] = s;
     }
     __syncthreads();
-    // X_blk = -W * Dinv ; diagonal block = Dinv
     for (int e = tid; e < jb * nb; e += nthreads) {
       const int r = e / nb, c = e % nb;
       float s = 0.f;
-      for (int p = 0; p <= c; ++p) s = fmaf(W[r * kNB + p], Dinv[p * kNB + c], s);
+      for (int p = 0; p <= c; ++p) s = fmaf(W[r * kNB + p], a[(jb + p) * LD + jb + c], s);
       a[r * LD + jb + c] = -s;
-    }
-    for (int e = tid; e < nb * nb; e += nthreads) {
-      const int r = e / nb, c = e % nb;
-      if (c >= r) a[(jb + r) * LD + jb + c] = Dinv[r * kNB + c];
     }
     __syncthreads();
   }
@@ -187,13 +192,13 @@ extern "C" int rla_chol_inv_f32(int64_t n, const float* G, int64_t ldg, float* R
   RLA_CUDA_TRY(cudaMemsetAsync(info, 0, sizeof(int), st));
   if (n == 0) return RLA_OK;
   if (!G || !Rinv) return RLA_ERR_ARG;
-  const size_t smem = (static_cast<size_t>(n) * (n + 1) + static_cast<size_t>(n) * kNB + kNB * kNB) * sizeof(float);
+  const size_t smem = (static_cast<size_t>(n) * (n + 1) + static_cast<size_t>(n) * kNB + kNB) * sizeof(float);
   static thread_local int attr_dev = -1;
   int dev = 0;
   RLA_CUDA_TRY(cudaGetDevice(&dev));
   if (attr_dev != dev) {  // raise the dynamic smem limit once per device and thread
     const size_t smax =
-        (static_cast<size_t>(kCholInvMax) * (kCholInvMax + 1) + kCholInvMax * kNB + kNB * kNB) * sizeof(float);
+        (static_cast<size_t>(kCholInvMax) * (kCholInvMax + 1) + kCholInvMax * kNB + kNB) * sizeof(float);
     RLA_CUDA_TRY(cudaFuncSetAttribute(chol_inv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       static_cast<int>(smax)));
     attr_dev = dev;

@@ -1,0 +1,427 @@
+// Small dense SVD for the randomized low-rank drivers, without the vendor
+// eigensolver.
+//
+// SVD1/EVD1 need the thin SVD of a wide l x n matrix B (l = k + over, a few
+// hundred).  The path here:
+//   1. G = B B^T accumulated in double-float (existing GEMM),
+//   2. G = R^T R by a double-float Cholesky in ONE CTA with the packed upper
+//      triangle resident in shared memory (rla_potrf_df_small),
+//   3. the SVD of C = R^T (so B = C W^T with W orthonormal) by one-sided
+//      Jacobi in FP32 on ONE thread-block cluster (rla_svd_jacobi).
+// One-sided Jacobi on the triangular factor keeps the small singular values
+// to high relative accuracy (the squaring of the Gram is undone by working
+// on R, whose FP32 image perturbs each singular value relatively by about
+// the FP32 unit roundoff times a modest condition number), which a Gram-matrix
+// eigensolver in FP32 would not.
+//
+// Jacobi layout: the columns of C are paired; a pair lives in the registers
+// of one warp (E elements per lane per column).  The pairs are spread over a
+// cluster of up to 8 CTAs.  Each round every warp rotates its pair, then
+// passes its two columns on along the round-robin ring (column 0 fixed, all
+// others moving one slot) by writing them into the next round's buffer of
+// the owning CTA through distributed shared memory; one cluster barrier per
+// round.  2P - 1 rounds (P pairs) form a sweep in which every pair of columns
+// meets once.  A sweep with no rotation above the threshold ends the
+// iteration; the sweep count is bounded.
+#include <cooperative_groups.h>
+
+#include "common.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace rla {
+namespace {
+
+constexpr int kCholDfMax = 232;     // packed df upper triangle fits in 227 KB
+constexpr int kCholDfThreads = 1024;
+constexpr int kJacMaxN = 448;       // 28 elements per lane (half-warp per column), 8 CTAs
+constexpr int kJacMaxCluster = 8;      // portable cluster size
+
+// ------------------------------------------------ double-float Cholesky
+__device__ __forceinline__ int packed_off(int n, int i) { return i * n - (i * (i - 1)) / 2; }
+
+// a - m * b in double-float with one two_sum (error about 2^-44 (|a| + |m b|),
+// the backward-stable form Cholesky needs); about half the instructions of
+// the exact df_add(a, df_neg(df_mul(m, b))).
+__device__ __forceinline__ df df_fms_sloppy(df a, df m, df b) {
+  const float ph = m.hi * b.hi;
+  float pl = fmaf(m.hi, b.hi, -ph);
+  pl = fmaf(m.hi, b.lo, fmaf(m.lo, b.hi, pl));
+  const float sh = a.hi - ph;
+  const float bb = sh - a.hi;
+  float e = (a.hi - (sh - bb)) + (-ph - bb);
+  e += a.lo - pl;
+  const float hi = sh + e;
+  return df{hi, e - (hi - sh)};
+}
+
+// Symmetric Gaussian elimination on the packed upper triangle:
+//   a_ik -= (a_ji / a_jj) a_jk   (i, k > j),
+// one barrier per column; row j of R is a_j. / sqrt(a_jj) at the end.
+__global__ void __launch_bounds__(kCholDfThreads, 1)
+potrf_df_small_kernel(int n, const double* __restrict__ G, int64_t ldg, float* __restrict__ R32, int64_t ldr,
+                      double* __restrict__ R64, int64_t ldr64, int* __restrict__ info) {
+  extern __shared__ __align__(16) float2 pk[];  // row i: columns i..n-1 as (hi, lo)
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+  for (int i = warp; i < n; i += nw) {
+    const int o = packed_off(n, i) - i;
+    for (int j = i + lane; j < n; j += 32) {
+      const df v = df_from_double(G[static_cast<int64_t>(i) * ldg + j]);
+      pk[o + j] = make_float2(v.hi, v.lo);
+    }
+  }
+  __syncthreads();
+  for (int j = 0; j < n; ++j) {
+    const int oj = packed_off(n, j) - j;
+    const float2 d2 = pk[oj + j];
+    if (!(d2.x > 0.f) || !isfinite(d2.x)) {  // uniform: every thread read the same pivot
+      if (tid == 0) *info = j + 1;
+      return;
+    }
+    const df inv = df_div(df{1.f, 0.f}, df{d2.x, d2.y});
+    for (int i = j + 1 + warp; i < n; i += nw) {
+      const float2 aji = pk[oj + i];
+      const df m = df_mul(df{aji.x, aji.y}, inv);
+      const int oi = packed_off(n, i) - i;
+      for (int k = i + lane; k < n; k += 32) {
+        const float2 x = pk[oi + k], y = pk[oj + k];
+        const df r = df_fms_sloppy(df{x.x, x.y}, m, df{y.x, y.y});
+        pk[oi + k] = make_float2(r.hi, r.lo);
+      }
+    }
+    __syncthreads();
+  }
+  for (int i = warp; i < n; i += nw) {
+    const int o = packed_off(n, i) - i;
+    const float2 d2 = pk[o + i];
+    const df sq = df_sqrt(df{d2.x, d2.y});
+    const df isq = df_div(df{1.f, 0.f}, sq);
+    for (int k = lane; k < n; k += 32) {
+      df v{0.f, 0.f};
+      if (k == i) v = sq;
+      else if (k > i) {
+        const float2 x = pk[o + k];
+        v = df_mul(df{x.x, x.y}, isq);
+      }
+      if (R32) R32[static_cast<int64_t>(i) * ldr + k] = v.hi + v.lo;
+      if (R64) R64[static_cast<int64_t>(i) * ldr64 + k] = static_cast<double>(v.hi) + static_cast<double>(v.lo);
+    }
+  }
+}
+
+// ------------------------------------------------ one-sided Jacobi (FP32)
+struct JacArgs {
+  int n;           // order of C
+  int P;           // column pairs (n rounded up to even, halved)
+  int ppc;         // pairs per CTA
+  const float* Ct; // row c = column c of C
+  int64_t ldc;
+  float* U;        // n x n row-major, column r = r-th left singular vector
+  int64_t ldu;
+  float* s;        // n singular values, descending
+  int* info;       // [0]: 1 if the sweep limit was reached; [1]: sweeps run
+  int max_sweeps;
+  float tol;
+};
+
+// A half-warp (16 lanes) owns one column pair; column slots are padded to
+// 16 E + 8 floats so that the two half-warps of a warp hit different banks.
+template <int E>
+struct JacLayout {
+  static constexpr int kSlot = 16 * E + 8;
+};
+
+template <int E>
+__global__ void __launch_bounds__(512, 1) svd_jacobi_f32_kernel(JacArgs a) {
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = static_cast<int>(cluster.block_rank());
+  const int lane = threadIdx.x & 31, hl = lane & 15, half = lane >> 4, warp = threadIdx.x >> 5;
+  constexpr int CS = JacLayout<E>::kSlot;
+  extern __shared__ __align__(16) float sm[];
+  float* cols = sm;                                                  // [2][ppc][2][CS]
+  int* ids = reinterpret_cast<int*>(cols + 4 * a.ppc * CS);          // [2][ppc][2]
+  unsigned* total = reinterpret_cast<unsigned*>(ids + 4 * a.ppc);    // [1]   (rank 0)
+  float* sig = reinterpret_cast<float*>(total + 4);                  // [2P]  (rank 0)
+  const int bufstride = 2 * a.ppc * CS, idstride = 2 * a.ppc;
+  auto slot = [&](int buf, int j, int tb) { return cols + buf * bufstride + (j * 2 + tb) * CS; };
+  auto slot_id = [&](int buf, int j, int tb) { return ids + buf * idstride + j * 2 + tb; };
+
+  const int j = 2 * warp + half;  // local pair of this half-warp
+  const int k = rank * a.ppc + j;  // global pair
+  const bool act = j < a.ppc && k < a.P;
+
+  // initial columns: pair k holds columns 2k and 2k + 1 (ids >= n are zero padding)
+  if (act) {
+    for (int tb = 0; tb < 2; ++tb) {
+      const int c = 2 * k + tb;
+      float* dst = slot(0, j, tb);
+#pragma unroll
+      for (int e = 0; e < E; ++e) {
+        const int i = hl + 16 * e;
+        dst[i] = (c < a.n && i < a.n) ? a.Ct[static_cast<int64_t>(c) * a.ldc + i] : 0.f;
+      }
+      if (hl == 0) *slot_id(0, j, tb) = c;
+    }
+  }
+  if (rank == 0 && threadIdx.x == 0) *total = 0u;
+
+  // static ring destinations: top[0] stays; top[k] -> top[k+1]; top[P-1] -> bot[P-1];
+  // bot[k] -> bot[k-1]; bot[0] -> top[1]
+  float *dx = nullptr, *dy = nullptr;
+  int *dix = nullptr, *diy = nullptr;
+  if (act) {
+    int tk, ttb, bk, btb;
+    if (k == 0) { tk = 0; ttb = 0; }
+    else if (k < a.P - 1) { tk = k + 1; ttb = 0; }
+    else { tk = k; ttb = 1; }
+    if (k == 0) { bk = a.P > 1 ? 1 : 0; btb = a.P > 1 ? 0 : 1; }
+    else { bk = k - 1; btb = 1; }
+    dx = cluster.map_shared_rank(slot(0, tk % a.ppc, ttb), tk / a.ppc);
+    dy = cluster.map_shared_rank(slot(0, bk % a.ppc, btb), bk / a.ppc);
+    dix = cluster.map_shared_rank(slot_id(0, tk % a.ppc, ttb), tk / a.ppc);
+    diy = cluster.map_shared_rank(slot_id(0, bk % a.ppc, btb), bk / a.ppc);
+  }
+  cluster.sync();
+
+  unsigned* total0 = cluster.map_shared_rank(total, 0);
+  const int rounds = 2 * a.P - 1;
+  const float tol2 = a.tol * a.tol;
+  unsigned seen = 0;
+  int cur = 0, sweeps = 0;
+  bool converged = false;
+  while (!converged && sweeps < a.max_sweeps) {
+    unsigned rotated = 0;
+    for (int r = 0; r < rounds; ++r) {
+      const int nxt = cur ^ 1;
+      float x[E], y[E];
+      int idx = 0, idy = 0;
+      if (act) {
+        const float* sx = slot(cur, j, 0);
+        const float* sy = slot(cur, j, 1);
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+          x[e] = sx[hl + 16 * e];
+          y[e] = sy[hl + 16 * e];
+        }
+        idx = *slot_id(cur, j, 0);
+        idy = *slot_id(cur, j, 1);
+      } else {
+#pragma unroll
+        for (int e = 0; e < E; ++e) x[e] = y[e] = 0.f;
+      }
+      float app0 = 0.f, aqq0 = 0.f, apq0 = 0.f, app1 = 0.f, aqq1 = 0.f, apq1 = 0.f;
+#pragma unroll
+      for (int e = 0; e < E; e += 2) {
+        app0 = fmaf(x[e], x[e], app0);
+        aqq0 = fmaf(y[e], y[e], aqq0);
+        apq0 = fmaf(x[e], y[e], apq0);
+        if (e + 1 < E) {
+          app1 = fmaf(x[e + 1], x[e + 1], app1);
+          aqq1 = fmaf(y[e + 1], y[e + 1], aqq1);
+          apq1 = fmaf(x[e + 1], y[e + 1], apq1);
+        }
+      }
+      float app = app0 + app1, aqq = aqq0 + aqq1, apq = apq0 + apq1;
+#pragma unroll
+      for (int o = 8; o > 0; o >>= 1) {
+        app += __shfl_xor_sync(0xffffffffu, app, o);
+        aqq += __shfl_xor_sync(0xffffffffu, aqq, o);
+        apq += __shfl_xor_sync(0xffffffffu, apq, o);
+      }
+      // the half-warp's lane 0 sums for all its lanes: one rotation per column
+      app = __shfl_sync(0xffffffffu, app, half * 16);
+      aqq = __shfl_sync(0xffffffffu, aqq, half * 16);
+      apq = __shfl_sync(0xffffffffu, apq, half * 16);
+      if (apq * apq > tol2 * app * aqq) {
+        // t = tan(theta) of the rotation diagonalising [[app, apq], [apq, aqq]]
+        const float d = aqq - app;
+        const float den = fabsf(d) + sqrtf(fmaf(d, d, 4.f * apq * apq));
+        const float t = copysignf(1.f, d) * (2.f * apq) / den;
+        const float x1 = fmaf(t, t, 1.f);
+        float c = rsqrtf(x1);
+        c = c * fmaf(-0.5f * x1, c * c, 1.5f);
+        const float sn = t * c;
+        const float tau = sn * __frcp_rn(1.f + c);
+        // x' = x - s (y + tau x), y' = y + s (x - tau y), tau = tan(theta/2):
+        // c = 1 - s tau is never rounded on its own, so rotations by tiny
+        // angles (where 1 + t^2 rounds to 1) do not stretch the columns.
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+          const float xe = x[e], ye = y[e];
+          x[e] = fmaf(-sn, fmaf(tau, xe, ye), xe);
+          y[e] = fmaf(sn, fmaf(-tau, ye, xe), ye);
+        }
+        ++rotated;
+      }
+      if (act) {
+        float* tx = dx + nxt * bufstride;
+        float* ty = dy + nxt * bufstride;
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+          tx[hl + 16 * e] = x[e];
+          ty[hl + 16 * e] = y[e];
+        }
+        if (hl == 0) {
+          dix[nxt * idstride] = idx;
+          diy[nxt * idstride] = idy;
+        }
+      }
+      cluster.sync();
+      cur = nxt;
+    }
+    ++sweeps;
+    if (act && hl == 0 && rotated) atomicAdd(total0, rotated);
+    cluster.sync();
+    const unsigned now = *total0;  // same value in every thread of the cluster
+    converged = (now == seen);
+    seen = now;
+    cluster.sync();  // all reads done before the next sweep adds again
+  }
+
+  // singular values: norms of the final columns; rank them (descending)
+  float nrm[2] = {0.f, 0.f};
+  int id[2] = {a.n, a.n};
+  for (int tb = 0; tb < 2; ++tb) {
+    float nn = 0.f;
+    if (act) {
+      const float* sx = slot(cur, j, tb);
+#pragma unroll
+      for (int e = 0; e < E; ++e) nn = fmaf(sx[hl + 16 * e], sx[hl + 16 * e], nn);
+      id[tb] = *slot_id(cur, j, tb);
+    }
+#pragma unroll
+    for (int o = 8; o > 0; o >>= 1) nn += __shfl_xor_sync(0xffffffffu, nn, o);
+    nrm[tb] = sqrtf(__shfl_sync(0xffffffffu, nn, half * 16));
+    if (act && hl == 0) cluster.map_shared_rank(sig, 0)[id[tb]] = id[tb] < a.n ? nrm[tb] : -1.f;
+  }
+  cluster.sync();
+  const float* sig0 = cluster.map_shared_rank(sig, 0);
+  for (int tb = 0; tb < 2; ++tb) {
+    const float sv = nrm[tb];
+    int cnt = 0;
+    if (act) {
+      for (int i = hl; i < 2 * a.P; i += 16) {
+        const float o = sig0[i];
+        cnt += (o > sv || (o == sv && i < id[tb])) ? 1 : 0;
+      }
+    }
+#pragma unroll
+    for (int o = 8; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    if (act && id[tb] < a.n) {
+      const float* sx = slot(cur, j, tb);
+      const float inv = sv > 0.f ? 1.f / sv : 0.f;
+#pragma unroll
+      for (int e = 0; e < E; ++e) {
+        const int i = hl + 16 * e;
+        if (i < a.n) a.U[static_cast<int64_t>(i) * a.ldu + cnt] = sx[i] * inv;
+      }
+      if (hl == 0) a.s[cnt] = sv;
+    }
+  }
+  if (rank == 0 && threadIdx.x == 0) {
+    a.info[0] = converged ? 0 : 1;
+    a.info[1] = sweeps;
+  }
+  cluster.sync();  // peers read rank 0's shared memory above
+}
+
+template <int E>
+int launch_jacobi(JacArgs a, int cs, int threads, cudaStream_t st) {
+  const size_t smem = (static_cast<size_t>(4) * a.ppc * JacLayout<E>::kSlot) * sizeof(float) +
+                      4 * a.ppc * sizeof(int) + 4 * sizeof(unsigned) + static_cast<size_t>(2 * a.P) * sizeof(float);
+  if (smem > 227 * 1024) return RLA_ERR_UNSUPPORTED;
+  static thread_local int attr_dev = -1;
+  int dev = 0;
+  RLA_CUDA_TRY(cudaGetDevice(&dev));
+  if (attr_dev != dev) {
+    RLA_CUDA_TRY(cudaFuncSetAttribute(svd_jacobi_f32_kernel<E>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      227 * 1024));
+    RLA_CUDA_TRY(cudaFuncSetAttribute(svd_jacobi_f32_kernel<E>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    attr_dev = dev;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(cs, 1, 1);
+  cfg.blockDim = dim3(threads, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = cs;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  RLA_CUDA_TRY(cudaLaunchKernelEx(&cfg, svd_jacobi_f32_kernel<E>, a));
+  return RLA_OK;
+}
+
+}  // namespace
+}  // namespace rla
+
+extern "C" int rla_potrf_df_small(int64_t n, const double* G, int64_t ldg, float* R32, int64_t ldr,
+                                  double* R64, int64_t ldr64, int* info, rla_stream_t stream) {
+  using namespace rla;
+  if (n < 0 || ldg < n || !info || (R32 && ldr < n) || (R64 && ldr64 < n)) return RLA_ERR_ARG;
+  if (n > kCholDfMax) return RLA_ERR_UNSUPPORTED;
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  RLA_CUDA_TRY(cudaMemsetAsync(info, 0, sizeof(int), st));
+  if (n == 0) return RLA_OK;
+  if (!G || (!R32 && !R64)) return RLA_ERR_ARG;
+  static thread_local int attr_dev = -1;
+  int dev = 0;
+  RLA_CUDA_TRY(cudaGetDevice(&dev));
+  if (attr_dev != dev) {
+    RLA_CUDA_TRY(cudaFuncSetAttribute(potrf_df_small_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      static_cast<int>(kCholDfMax * (kCholDfMax + 1) / 2 * sizeof(float2))));
+    attr_dev = dev;
+  }
+  const size_t smem = static_cast<size_t>(n) * (n + 1) / 2 * sizeof(float2);
+  potrf_df_small_kernel<<<1, kCholDfThreads, smem, st>>>(static_cast<int>(n), G, ldg, R32, ldr, R64, ldr64, info);
+  RLA_CUDA_TRY(cudaGetLastError());
+  return RLA_OK;
+}
+
+extern "C" int rla_svd_jacobi(int dtype, int64_t n, const void* Ct, int64_t ldc, void* U, int64_t ldu, void* s,
+                              int* info, int max_sweeps, int cluster, rla_stream_t stream) {
+  using namespace rla;
+  if (n < 0 || ldc < n || ldu < n || !info || max_sweeps <= 0 || cluster < 0 || cluster > kJacMaxCluster)
+    return RLA_ERR_ARG;
+  if (dtype != RLA_F32) return RLA_ERR_UNSUPPORTED;
+  if (n > kJacMaxN) return RLA_ERR_UNSUPPORTED;
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  RLA_CUDA_TRY(cudaMemsetAsync(info, 0, 2 * sizeof(int), st));
+  if (n == 0) return RLA_OK;
+  if (!Ct || !U || !s) return RLA_ERR_ARG;
+  JacArgs a;
+  a.n = static_cast<int>(n);
+  a.P = static_cast<int>((n + 1) / 2);
+  // default: about 14 pairs (7 warps) per CTA, at most 8 CTAs (portable cluster size)
+  int cs = cluster > 0 ? cluster : (a.P + 13) / 14;
+  cs = cs < 1 ? 1 : (cs > kJacMaxCluster ? kJacMaxCluster : cs);
+  a.ppc = (a.P + cs - 1) / cs;
+  cs = (a.P + a.ppc - 1) / a.ppc;
+  const int warps = (a.ppc + 1) / 2;
+  if (warps > 16) return RLA_ERR_UNSUPPORTED;
+  a.Ct = static_cast<const float*>(Ct);
+  a.ldc = ldc;
+  a.U = static_cast<float*>(U);
+  a.ldu = ldu;
+  a.s = static_cast<float*>(s);
+  a.info = info;
+  a.max_sweeps = max_sweeps;
+  a.tol = 2.0f * 5.96e-8f * sqrtf(static_cast<float>(n));
+  const int ept = (a.n + 15) / 16;  // elements per lane: a half-warp holds a column
+  const int th = 32 * warps;
+  if (ept <= 1) return launch_jacobi<1>(a, cs, th, st);
+  if (ept <= 2) return launch_jacobi<2>(a, cs, th, st);
+  if (ept <= 4) return launch_jacobi<4>(a, cs, th, st);
+  if (ept <= 6) return launch_jacobi<6>(a, cs, th, st);
+  if (ept <= 8) return launch_jacobi<8>(a, cs, th, st);
+  if (ept <= 10) return launch_jacobi<10>(a, cs, th, st);
+  if (ept <= 12) return launch_jacobi<12>(a, cs, th, st);
+  if (ept <= 14) return launch_jacobi<14>(a, cs, th, st);
+  if (ept <= 16) return launch_jacobi<16>(a, cs, th, st);
+  if (ept <= 20) return launch_jacobi<20>(a, cs, th, st);
+  if (ept <= 24) return launch_jacobi<24>(a, cs, th, st);
+  return launch_jacobi<28>(a, cs, th, st);
+}

@@ -57,14 +57,52 @@ def sym_eig(G):
     return torch.linalg.eigh(Gs)
 
 
+JACOBI_MAX = 232
+
+
+def _svd_from_gram(G):
+    """U, s of a square-root factor of the SPD Gram G (binary64, k x k).
+
+    G = R^T R by the double-float single-CTA Cholesky, then one-sided Jacobi
+    (FP32, one CTA cluster) on C = R^T, whose left singular vectors and
+    singular values are those of any B with B B^T = G.  Returns None when
+    the Cholesky fails or Jacobi does not converge (the caller then uses the
+    dense eigensolver).  Inside a deferred-check scope nothing synchronises.
+    """
+    from .operand import current_checks
+    chk = current_checks()
+    if chk is not None:
+        R = K.potrf_df_small(G, info=chk.new_flag())
+        U, s, inf = K.svd_jacobi(R)
+        chk.add_flag(inf[:1])
+        return U, s
+    try:
+        R = K.potrf_df_small(G)
+    except RlaError:
+        return None
+    U, s, inf = K.svd_jacobi(R)
+    if int(inf[0].item()):
+        return None
+    return U, s
+
+
 def small_svd_wide(B):
     """Thin SVD of a wide k x n device matrix B (k << n) through its Gram.
 
-    G = B B^T is accumulated in double-float, G = U diag(lam) U^T, then
-    s = sqrt(lam) and Vh = diag(1/s) U^T B.  Returned in descending order.
+    G = B B^T is accumulated in double-float.  For binary32 B (k <= 232)
+    U and s come from the Cholesky + one-sided Jacobi kernels; otherwise
+    G = U diag(lam) U^T and s = sqrt(lam).  Vh = diag(1/s) U^T B.
+    Returned in descending order.
     """
     B64 = B if B.dtype == torch.float64 else B.to(torch.float64)
     G = K.gemm(B64, B64, transb=True, mode="df")
+    if B.dtype == torch.float32 and B.shape[0] <= JACOBI_MAX:
+        res = _svd_from_gram(G)
+        if res is not None:
+            U, s = res
+            inv = torch.where(s > 0, 1.0 / s, torch.zeros_like(s))
+            Vh = K.gemm(U, B, transa=True, mode="f32") * inv[:, None]
+            return U, s, Vh
     lam, U = sym_eig(G)
     lam, U = lam.flip(0), U.flip(1).contiguous()
     s = torch.sqrt(torch.clamp(lam, min=0.0))
@@ -77,6 +115,13 @@ def small_svd_tall(B):
     """Thin SVD of a tall n x k device matrix B (k << n) through B^T B."""
     B64 = B if B.dtype == torch.float64 else B.to(torch.float64)
     G = K.gemm(B64, B64, transa=True, mode="df")
+    if B.dtype == torch.float32 and B.shape[1] <= JACOBI_MAX:
+        res = _svd_from_gram(G)
+        if res is not None:
+            V, s = res
+            inv = torch.where(s > 0, 1.0 / s, torch.zeros_like(s))
+            U = K.gemm(B, V, mode="f32") * inv[None, :]
+            return U, s, V.t().contiguous()
     lam, V = sym_eig(G)
     lam, V = lam.flip(0), V.flip(1).contiguous()
     s = torch.sqrt(torch.clamp(lam, min=0.0))

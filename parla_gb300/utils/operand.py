@@ -35,6 +35,10 @@ class DeferredChecks:
         self.flags.append(f)
         return f
 
+    def add_flag(self, f):
+        """Register an existing int32 device flag (non-zero = failed)."""
+        self.flags.append(f.reshape(-1))
+
     def failed(self):
         if not self.flags:
             return False

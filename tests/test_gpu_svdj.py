@@ -1,0 +1,104 @@
+"""Small-SVD kernels: double-float Cholesky and cluster one-sided Jacobi.
+
+Gated against LAPACK (NumPy, binary64) on the same inputs:
+  Cholesky     backward error ||R^T R - G|| <= 1e-13 ||G||; R within
+               1e-9 of LAPACK's (condition number 1e6)
+  Jacobi       singular values within 4e-6 * s_max * max(1, sqrt(n)/8)
+               (FP32 arithmetic);
+               graded inputs: each s_i within 1e-4 relative;
+               U orthonormal to 1e-5 and equal to LAPACK's up to sign
+               for well-separated singular values.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module")
+def K():
+    import __graft_entry__
+    __graft_entry__.build()
+    from parla_gb300 import _kernels
+    return _kernels
+
+
+def spd(n, rng, cond=1e6):
+    Q, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    lam = np.logspace(0, -np.log10(cond), n)
+    return (Q * lam) @ Q.T
+
+
+@pytest.mark.parametrize("n", [1, 5, 64, 210, 232])
+def test_potrf_df_small_matches_lapack(K, n):
+    rng = np.random.default_rng(n)
+    G = spd(n, rng)
+    Rl = np.linalg.cholesky(G).T
+    R32, R64 = K.potrf_df_small(torch.from_numpy(G).cuda(), want64=True)
+    R64 = R64.cpu().numpy()
+    assert np.linalg.norm(R64.T @ R64 - G) <= 1e-13 * np.linalg.norm(G)
+    assert np.max(np.abs(R64 - Rl)) <= 1e-9 * np.max(np.abs(Rl))
+    assert np.allclose(R32.cpu().numpy(), Rl.astype(np.float32), rtol=1e-6, atol=1e-7 * np.abs(Rl).max())
+
+
+def test_potrf_df_small_reports_pivot(K):
+    G = np.eye(6)
+    G[3, 3] = -1.0
+    flag = torch.zeros(1, dtype=torch.int32, device="cuda")
+    K.potrf_df_small(torch.from_numpy(G).cuda(), info=flag)
+    assert int(flag.item()) == 4
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 31, 33, 100, 210, 300, 448])
+def test_svd_jacobi_random(K, n):
+    rng = np.random.default_rng(100 + n)
+    C = rng.standard_normal((n, n)).astype(np.float32)
+    U, s, info = K.svd_jacobi(torch.from_numpy(C.T.copy()).cuda())
+    U, s, info = U.cpu().numpy().astype(float), s.cpu().numpy().astype(float), info.cpu().numpy()
+    sl = np.linalg.svd(C.astype(float), compute_uv=False)
+    assert info[0] == 0 and 1 <= info[1] <= 20
+    assert np.all(np.diff(s) <= 0)
+    assert np.max(np.abs(s - sl)) <= 4e-6 * sl[0] * max(1.0, np.sqrt(n) / 8)
+    assert np.max(np.abs(U.T @ U - np.eye(n))) <= 1e-5 * max(1.0, np.sqrt(n) / 8)
+    # C = U diag(s) W^T  =>  ||U^T C||_row = s
+    assert np.allclose(np.linalg.norm(U.T @ C.astype(float), axis=1), s, rtol=1e-4, atol=1e-5 * sl[0])
+
+
+def test_svd_jacobi_graded_from_gram(K):
+    """The RSVD use: B (l x n) with singular values from 1 down to 1e-4."""
+    rng = np.random.default_rng(7)
+    l, n = 210, 4096
+    Ul, _ = np.linalg.qr(rng.standard_normal((l, l)))
+    V, _ = np.linalg.qr(rng.standard_normal((n, l)))
+    sv = np.arange(1, l + 1, dtype=float) ** -1.5 + 1e-4
+    B = ((Ul * sv) @ V.T).astype(np.float32)
+    Bd = torch.from_numpy(B).cuda()
+    from parla_gb300 import _kernels as Kk
+    G = Kk.gemm(Bd.double(), Bd.double(), transb=True, mode="df")
+    R = K.potrf_df_small(G)
+    U, s, info = K.svd_jacobi(R)
+    s = s.cpu().numpy().astype(float)
+    sl = np.linalg.svd(B.astype(float), compute_uv=False)
+    assert int(info[0].item()) == 0
+    assert np.max(np.abs(s - sl) / sl) <= 1e-4
+    U = U.cpu().numpy().astype(float)
+    # left singular vectors: U^T B has orthogonal rows of norms s
+    P = U.T @ B.astype(float)
+    assert np.allclose(np.linalg.norm(P, axis=1), sl, rtol=1e-4)
+
+
+def test_small_svd_wide_uses_jacobi(K, monkeypatch):
+    from parla_gb300.utils import linalg_wrappers as law
+    rng = np.random.default_rng(9)
+    B = rng.standard_normal((150, 3000)).astype(np.float32)
+    Bd = torch.from_numpy(B).cuda()
+    calls = []
+    real = K.svd_jacobi
+    monkeypatch.setattr(K, "svd_jacobi", lambda *a, **k: calls.append(1) or real(*a, **k))
+    U, s, Vh = law.small_svd_wide(Bd)
+    assert calls == [1]
+    Bh = (U.double() * s.double()) @ Vh.double()
+    assert float((Bh - Bd.double()).abs().max()) <= 1e-4 * float(Bd.abs().max())
+    sl = np.linalg.svd(B.astype(float), compute_uv=False)
+    assert np.allclose(s.cpu().numpy(), sl, rtol=1e-5)
