@@ -1,14 +1,16 @@
-// R^-1 from G = R^T R (upper Cholesky, then in-place triangular inverse) for
-// small symmetric positive definite FP32 matrices, in ONE CTA with the matrix
+// R^-1 from G = R^T R (upper Cholesky, then triangular inverse) for small
+// symmetric positive definite FP32 matrices, in ONE CTA with the matrix
 // resident in shared memory (n <= kCholInvMax).
 //
-// Blocked in 32-column panels so that most of the arithmetic is register-tiled:
-//   Cholesky (right-looking): warp-level factor of the 32 x 32 diagonal block,
-//     per-column forward substitution for the panel row, 4 x 4 register tiles
-//     for the symmetric trailing update;
-//   inverse (left-looking, in place): all diagonal blocks inverted at once,
-//     one warp per block; then per block column W = X_tl R_blk with the
-//     already inverted leading block, and X_blk = -W D^-1.
+// Blocked in 32-column panels.  The sequential parts (factor and inverse of
+// a 32 x 32 diagonal block, the panel row solve) are short loops over shared
+// memory, not unrolled: straight-line code that a warp runs once is fetched
+// from L2 instruction by instruction, which costs more than the arithmetic.
+//   Cholesky (right-looking): warp-level factor of the diagonal block (lane c
+//     holds column c), per-column forward substitution for the panel row,
+//     4 x 4 register tiles (float4 loads) for the symmetric trailing update;
+//   inverse: all diagonal blocks inverted at once (one warp per block), then
+//     per block column W = X_tl R_blk and X_blk = -W X_bb.
 // Replaces the pair potrf + trtri of the CholeskyQR stabilizer: one launch
 // instead of two grid-wide factorizations.
 #include "common.cuh"
@@ -17,26 +19,26 @@ namespace rla {
 namespace {
 
 constexpr int kCholInvMax = 216;
-constexpr int kCiThreads = 384;
+constexpr int kCiThreads = 512;
 constexpr int kNB = 32;
+
+__host__ __device__ __forceinline__ int ci_ld(int n) { return (n + 3) & ~3; }
 
 __global__ void __launch_bounds__(kCiThreads, 1)
 chol_inv_kernel(int n, const float* __restrict__ G, int64_t ldg, float* __restrict__ Rinv, int64_t ldr,
                 float* __restrict__ Rout, int64_t ldro, int* __restrict__ info) {
   extern __shared__ __align__(16) float smem[];
-  const int LD = n + 1;
+  const int LD = ci_ld(n);
   float* a = smem;                        // n x LD
   float* W = a + n * LD;                  // n x kNB scratch
-  float* dinv = W + n * kNB;              // kNB reciprocal pivots of the current block
+  float* dinv = W + n * kNB;              // reciprocal pivots of the current block
   __shared__ int s_bad;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
   const int nthreads = blockDim.x;
   const int nblk = (n + kNB - 1) / kNB;
 
-  for (int e = tid; e < n * n; e += nthreads) {
-    int r = e / n, c = e % n;
-    a[r * LD + c] = c >= r ? G[static_cast<int64_t>(r) * ldg + c] : 0.f;
-  }
+  for (int r = warp; r < n; r += nw)
+    for (int c = lane; c < n; c += 32) a[r * LD + c] = c >= r ? G[static_cast<int64_t>(r) * ldg + c] : 0.f;
   if (tid == 0) s_bad = 0;
   __syncthreads();
 
@@ -44,52 +46,41 @@ chol_inv_kernel(int n, const float* __restrict__ G, int64_t ldg, float* __restri
   for (int jb = 0; jb < n; jb += kNB) {
     const int nb = min(kNB, n - jb);
     if (warp == 0) {
-      // lane c holds column c of the diagonal block (rows 0..nb-1)
-      float col[kNB];
-#pragma unroll
-      for (int r = 0; r < kNB; ++r) col[r] = (r < nb && lane < nb) ? a[(jb + r) * LD + jb + lane] : 0.f;
+      // lane c owns column c of the diagonal block; row i is the pivot row
+      float* blk = a + jb * LD + jb;
       int bad = 0;
-#pragma unroll
-      for (int i = 0; i < kNB; ++i) {
-        if (i < nb) {
-          float d = __shfl_sync(0xffffffffu, col[i], i);
-          if (!(d > 0.f) || !isfinite(d)) { bad = jb + i + 1; d = 1.f; }
-          const float piv = sqrtf(d);
-          if (lane == i) col[i] = piv;
-          else if (lane > i) col[i] = col[i] / piv;
-#pragma unroll
-          for (int r = i + 1; r < kNB; ++r) {
-            const float rir = __shfl_sync(0xffffffffu, col[i], r);  // R[i][r]
-            if (r < nb && lane >= r) col[r] = fmaf(-rir, col[i], col[r]);
-          }
+#pragma unroll 1
+      for (int i = 0; i < nb; ++i) {
+        float d = blk[i * LD + i];
+        if (!(d > 0.f) || !isfinite(d)) { bad = bad ? bad : i + 1; d = 1.f; }
+        const float piv = sqrtf(d);
+        __syncwarp();
+        if (lane == i) blk[i * LD + i] = piv;
+        else if (lane > i && lane < nb) blk[i * LD + lane] *= 1.f / piv;
+        if (lane == 0) dinv[i] = 1.f / piv;
+        __syncwarp();
+        if (lane > i && lane < nb) {
+          const float ric = blk[i * LD + lane];
+#pragma unroll 1
+          for (int r = i + 1; r <= lane; ++r) blk[r * LD + lane] = fmaf(-blk[i * LD + r], ric, blk[r * LD + lane]);
         }
+        __syncwarp();
       }
-#pragma unroll
-      for (int r = 0; r < kNB; ++r)
-        if (r < nb && lane < nb && lane >= r) a[(jb + r) * LD + jb + lane] = col[r];
-      if (lane < nb) dinv[lane] = 1.f / col[lane];
-      if (lane == 0 && bad) { s_bad = bad; *info = bad; }
+      if (lane == 0 && bad) { s_bad = jb + bad; *info = jb + bad; }
     }
     __syncthreads();
     if (s_bad) return;
-    // panel row: rows jb..jb+nb, columns c >= jb+nb: solve R_d^T X = G_panel,
-    // column-oriented so each step is one multiply plus independent FMAs
+    // panel row: rows jb..jb+nb, columns c >= jb+nb: solve R_d^T X = G_panel
     for (int c = jb + nb + tid; c < n; c += nthreads) {
-      float v[kNB];
-#pragma unroll
-      for (int i = 0; i < kNB; ++i) v[i] = i < nb ? a[(jb + i) * LD + c] : 0.f;
-#pragma unroll
-      for (int p = 0; p < kNB; ++p) {
-        if (p < nb) {
-          v[p] *= dinv[p];
-#pragma unroll
-          for (int i = p + 1; i < kNB; ++i)
-            if (i < nb) v[i] = fmaf(-a[(jb + p) * LD + jb + i], v[p], v[i]);
-        }
+      float* colc = a + jb * LD + c;
+#pragma unroll 1
+      for (int p = 0; p < nb; ++p) {
+        const float xp = colc[p * LD] * dinv[p];
+        colc[p * LD] = xp;
+        const float* rp = a + (jb + p) * LD + jb;
+#pragma unroll 4
+        for (int i = p + 1; i < nb; ++i) colc[i * LD] = fmaf(-rp[i], xp, colc[i * LD]);
       }
-#pragma unroll
-      for (int i = 0; i < kNB; ++i)
-        if (i < nb) a[(jb + i) * LD + c] = v[i];
     }
     __syncthreads();
     // trailing update on 4 x 4 register tiles of the upper triangle
@@ -103,16 +94,13 @@ chol_inv_kernel(int n, const float* __restrict__ G, int64_t ldg, float* __restri
         float acc[4][4] = {};
         for (int p = 0; p < nb; ++p) {
           const float* prow = a + (jb + p) * LD;
-          float u[4], w[4];
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            u[q] = (r0 + q < n) ? prow[r0 + q] : 0.f;
-            w[q] = (c0 + q < n) ? prow[c0 + q] : 0.f;
-          }
+          const float4 u = *reinterpret_cast<const float4*>(prow + r0);
+          const float4 w = *reinterpret_cast<const float4*>(prow + c0);
+          const float uu[4] = {u.x, u.y, u.z, u.w}, ww[4] = {w.x, w.y, w.z, w.w};
 #pragma unroll
           for (int q = 0; q < 4; ++q)
 #pragma unroll
-            for (int z = 0; z < 4; ++z) acc[q][z] = fmaf(u[q], w[z], acc[q][z]);
+            for (int z = 0; z < 4; ++z) acc[q][z] = fmaf(uu[q], ww[z], acc[q][z]);
         }
 #pragma unroll
         for (int q = 0; q < 4; ++q)
@@ -126,44 +114,55 @@ chol_inv_kernel(int n, const float* __restrict__ G, int64_t ldg, float* __restri
     __syncthreads();
   }
   if (Rout) {
-    for (int e = tid; e < n * n; e += nthreads) {
-      int r = e / n, c = e % n;
-      Rout[static_cast<int64_t>(r) * ldro + c] = c >= r ? a[r * LD + c] : 0.f;
-    }
+    for (int r = warp; r < n; r += nw)
+      for (int c = lane; c < n; c += 32) Rout[static_cast<int64_t>(r) * ldro + c] = c >= r ? a[r * LD + c] : 0.f;
   }
 
   // ------------------------------------------- in-place inverse (upper)
-  // All diagonal blocks are inverted at once (warp b inverts block b, lane c
-  // solves R_bb x = e_c column-oriented from the bottom), written over R_bb.
+  // All diagonal blocks at once: warp b, lane c solves R_bb x = e_c from the
+  // bottom (identity padding beyond nb) and writes column c of R_bb^-1.
   if (warp < nblk) {
     const int jb = warp * kNB, nb = min(kNB, n - jb);
-    float x[kNB];
-#pragma unroll
-    for (int i = 0; i < kNB; ++i) x[i] = (i == lane) ? 1.f : 0.f;
-#pragma unroll
-    for (int i = kNB - 1; i >= 0; --i) {
-      if (i < nb) {
-        x[i] = (i <= lane) ? x[i] / a[(jb + i) * LD + jb + i] : 0.f;
-#pragma unroll
-        for (int q = 0; q < i; ++q) x[q] = fmaf(-a[(jb + q) * LD + jb + i], x[i], x[q]);
-      }
+    const float* blk = a + jb * LD + jb;
+    float* x = W + jb * kNB;  // x[i * kNB + c]: row i of column c of the block inverse
+#pragma unroll 1
+    for (int i = 0; i < nb; ++i) x[i * kNB + lane] = i == lane ? 1.f : 0.f;
+    __syncwarp();
+#pragma unroll 1
+    for (int i = nb - 1; i >= 0; --i) {
+      const float xi = i <= lane ? x[i * kNB + lane] / blk[i * LD + i] : 0.f;
+      x[i * kNB + lane] = xi;
+#pragma unroll 4
+      for (int q = 0; q < i; ++q) x[q * kNB + lane] = fmaf(-blk[q * LD + i], xi, x[q * kNB + lane]);
     }
     __syncwarp();
     if (lane < nb) {
-#pragma unroll
-      for (int i = 0; i < kNB; ++i)
-        if (i < nb && i <= lane) a[(jb + i) * LD + jb + lane] = x[i];
+#pragma unroll 1
+      for (int i = 0; i <= lane; ++i) a[(jb + i) * LD + jb + lane] = x[i * kNB + lane];
     }
   }
   __syncthreads();
-  // block column j: X[0:jb, j] = -(X[0:jb, 0:jb] R[0:jb, j]) X_jj
+  // block column j: X[0:jb, j] = -(X[0:jb, 0:jb] R[0:jb, j]) X_jj; one thread
+  // per (row, 4 columns) so the X row entries are reused four times
   for (int jb = kNB; jb < n; jb += kNB) {
     const int nb = min(kNB, n - jb);
-    for (int e = tid; e < jb * nb; e += nthreads) {
-      const int r = e / nb, c = e % nb;
-      float s = 0.f;
-      for (int p = r; p < jb; ++p) s = fmaf(a[r * LD + p], a[p * LD + jb + c], s);
-      W[r * kNB + c] = s;
+    const int cq = (nb + 3) / 4;
+    for (int e = tid; e < jb * cq; e += nthreads) {
+      const int r = e / cq, c = (e % cq) * 4;
+      float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+      for (int p = r; p < jb; ++p) {
+        const float xr = a[r * LD + p];
+        const float* rp = a + p * LD + jb + c;
+        s0 = fmaf(xr, rp[0], s0);
+        s1 = fmaf(xr, c + 1 < nb ? rp[1] : 0.f, s1);
+        s2 = fmaf(xr, c + 2 < nb ? rp[2] : 0.f, s2);
+        s3 = fmaf(xr, c + 3 < nb ? rp[3] : 0.f, s3);
+      }
+      float* wr = W + r * kNB + c;
+      wr[0] = s0;
+      if (c + 1 < nb) wr[1] = s1;
+      if (c + 2 < nb) wr[2] = s2;
+      if (c + 3 < nb) wr[3] = s3;
     }
     __syncthreads();
     for (int e = tid; e < jb * nb; e += nthreads) {
@@ -174,10 +173,8 @@ chol_inv_kernel(int n, const float* __restrict__ G, int64_t ldg, float* __restri
     }
     __syncthreads();
   }
-  for (int e = tid; e < n * n; e += nthreads) {
-    int r = e / n, c = e % n;
-    Rinv[static_cast<int64_t>(r) * ldr + c] = c >= r ? a[r * LD + c] : 0.f;
-  }
+  for (int r = warp; r < n; r += nw)
+    for (int c = lane; c < n; c += 32) Rinv[static_cast<int64_t>(r) * ldr + c] = c >= r ? a[r * LD + c] : 0.f;
 }
 
 }  // namespace
@@ -192,13 +189,12 @@ extern "C" int rla_chol_inv_f32(int64_t n, const float* G, int64_t ldg, float* R
   RLA_CUDA_TRY(cudaMemsetAsync(info, 0, sizeof(int), st));
   if (n == 0) return RLA_OK;
   if (!G || !Rinv) return RLA_ERR_ARG;
-  const size_t smem = (static_cast<size_t>(n) * (n + 1) + static_cast<size_t>(n) * kNB + kNB) * sizeof(float);
+  const size_t smem = (static_cast<size_t>(n) * (ci_ld(static_cast<int>(n)) + kNB) + kNB) * sizeof(float);
   static thread_local int attr_dev = -1;
   int dev = 0;
   RLA_CUDA_TRY(cudaGetDevice(&dev));
   if (attr_dev != dev) {  // raise the dynamic smem limit once per device and thread
-    const size_t smax =
-        (static_cast<size_t>(kCholInvMax) * (kCholInvMax + 1) + kCholInvMax * kNB + kNB) * sizeof(float);
+    const size_t smax = (static_cast<size_t>(kCholInvMax) * (ci_ld(kCholInvMax) + kNB) + kNB) * sizeof(float);
     RLA_CUDA_TRY(cudaFuncSetAttribute(chol_inv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       static_cast<int>(smax)));
     attr_dev = dev;
