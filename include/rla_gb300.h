@@ -335,6 +335,57 @@ int rla_convert_bf16_pair(int src_dtype, int64_t rows, int64_t cols,
 int rla_split_f64(int64_t rows, int64_t cols, const double* x, int64_t ldx,
                   float* hi, float* lo, int64_t ldh, rla_stream_t stream);
 
+
+/* ------------------------------------------------------------------------
+ * Learned sparse sketch (no counterpart in the reference; plugs in where
+ * the reference takes a SketchOpGen, parla/comps/sketchers/oblivious.py:25-28,
+ * and a QBDecomposer, parla/comps/qb.py:241-283).  Network: 4 -> 64 (tanh)
+ * -> 8, 840 binary32 parameters laid out W1[64][4], b1[64], W2[8][64], b2[8].
+ * ---------------------------------------------------------------------- */
+
+/* out[j] = sum_i A[i][j]^2 (binary32, row-major A). */
+int rla_col_sumsq(int64_t m, int64_t n, const float* A, int64_t lda, float* out, rla_stream_t stream);
+
+/* Per-column features of nmat matrices from squared column norms cn2 and
+ * pre-sketch leverage scores lev (both nmat x n): F is nmat x n x 4. */
+int rla_lsk_features(int64_t nmat, int64_t n, int k_pre, const float* cn2, const float* lev, float* F,
+                     rla_stream_t stream);
+
+/* Network forward for N = nmat * n columns: vals (N x 8) = sign exp(o) / sqrt(8)
+ * with the signs of the fixed pattern (n x 8); hidden (N x 64) kept for the
+ * backward pass when not NULL. */
+int rla_mlp_fwd(int64_t N, int64_t n, const float* F, const float* params, const int8_t* signs, float* vals,
+                float* hidden, rla_stream_t stream);
+
+/* Network backward: grad (840) = scale * sum over columns of the parameter
+ * gradients given dO = dL/do (N x 8).  Workspace query with ws == NULL. */
+int rla_mlp_bwd(int64_t N, const float* F, const float* hidden, const float* dO, const float* params, float scale,
+                float* grad, void* ws, size_t* ws_bytes, rla_stream_t stream);
+
+/* One Adam step on n parameters (step counts from 1). */
+int rla_adam_step(int64_t n, float* p, const float* g, float* m, float* v, float lr, float beta1, float beta2,
+                  float eps, int64_t step, rla_stream_t stream);
+
+/* Y (m x d) = A S^T for the value-carrying pattern given by sketch rows
+ * (rowptr[d + 1]; entries: column cidx, value vals[vidx]); n <= 7000. */
+int rla_lsk_sketch_right(int64_t m, int64_t n, int d, const int* rowptr, const int* cidx, const int* vidx,
+                         const float* vals, const float* A, int64_t lda, float* Y, int64_t ldy,
+                         rla_stream_t stream);
+
+/* W[b] (d x K) = S_b X[b] for nmat matrices (vals nmat x n x 8, X nmat x n x K). */
+int rla_lsk_sketch_left(int64_t nmat, int d, int K, int64_t n, int nnz, const int* rowptr, const int* cidx,
+                        const int* vidx, const float* vals, const float* X, float* W, rla_stream_t stream);
+
+/* dO[b][j][t] = vals[b][j][t] * <dW[b][rows[j][t]], X[b][j]>. */
+int rla_lsk_value_grad(int64_t nmat, int d, int K, int64_t n, const int* rows, const float* vals, const float* X,
+                       const float* dW, float* dO, rla_stream_t stream);
+
+/* Training loss per matrix (binary64): with Wt = W diag(sigma), G = Wt Wt^T,
+ * H = Wt diag(sigma^2) Wt^T, loss = (sum sigma^2 - tr(G^-1 H)) / sum_{i>=k} sigma_i^2,
+ * and dW = dloss/dW.  W: nmat x d x K, sigma: nmat x K.  Workspace query with ws == NULL. */
+int rla_lsk_loss(int64_t nmat, int d, int K, int k, const float* W, const float* sigma, double* loss, float* dW,
+                 void* ws, size_t* ws_bytes, rla_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

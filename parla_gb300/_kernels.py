@@ -314,6 +314,94 @@ def svd_jacobi(Ct, max_sweeps=40, info=None, cluster=0):
     return U, s, inf
 
 
+# ----------------------------------------------------------- learned sketch
+
+def col_sumsq(A):
+    """Squared column norms of a binary32 row-major matrix."""
+    m, n = A.shape
+    out = torch.empty((n,), dtype=torch.float32, device=A.device)
+    _timed("col_sumsq", 1, call, "rla_col_sumsq", m, n, ptr(A), A.stride(0), ptr(out), stream())
+    return out
+
+
+def lsk_features(cn2, lev, k_pre):
+    """Features (nmat x n x 4) from squared column norms and leverage (nmat x n)."""
+    cn2 = cn2.reshape(-1, cn2.shape[-1]).contiguous()
+    lev = lev.reshape(cn2.shape).contiguous()
+    nmat, n = cn2.shape
+    F = torch.empty((nmat, n, 4), dtype=torch.float32, device=cn2.device)
+    _timed("lsk_features", 1, call, "rla_lsk_features", nmat, n, k_pre, ptr(cn2), ptr(lev), ptr(F), stream())
+    return F
+
+
+def mlp_fwd(F, params, signs, n, want_hidden=False):
+    """Sketch values (N x 8) from features (N x 4); hidden (N x 64) if asked."""
+    F = F.reshape(-1, 4).contiguous()
+    N = F.shape[0]
+    vals = torch.empty((N, 8), dtype=torch.float32, device=F.device)
+    H = torch.empty((N, 64), dtype=torch.float32, device=F.device) if want_hidden else None
+    _timed("mlp_fwd", 1, call, "rla_mlp_fwd", N, n, ptr(F), ptr(params), ptr(signs), ptr(vals), ptr(H), stream())
+    return vals, H
+
+
+def mlp_bwd(F, H, dO, params, scale=1.0):
+    """Parameter gradient (840) of scale * sum_g <dO[g], o[g]>."""
+    F = F.reshape(-1, 4).contiguous()
+    N = F.shape[0]
+    sz = C.c_size_t(0)
+    call("rla_mlp_bwd", N, None, None, None, None, C.c_float(scale), None, None, C.byref(sz), stream())
+    ws = workspace(sz.value)
+    grad = torch.empty((840,), dtype=torch.float32, device=F.device)
+    _timed("mlp_bwd", 2, call, "rla_mlp_bwd", N, ptr(F), ptr(H), ptr(dO), ptr(params), C.c_float(scale), ptr(grad),
+           ptr(ws), C.byref(sz), stream())
+    return grad
+
+
+def adam_step(p, g, m, v, lr, step, beta1=0.9, beta2=0.999, eps=1e-8):
+    _timed("adam", 1, call, "rla_adam_step", p.numel(), ptr(p), ptr(g), ptr(m), ptr(v), C.c_float(lr),
+           C.c_float(beta1), C.c_float(beta2), C.c_float(eps), step, stream())
+
+
+def lsk_sketch_right(A, rowptr, cidx, vidx, vals, d):
+    """Y (m x d) = A S^T for the value-carrying pattern."""
+    m, n = A.shape
+    Y = torch.empty((m, d), dtype=torch.float32, device=A.device)
+    _timed("lsk_sketch_right", 1, call, "rla_lsk_sketch_right", m, n, d, ptr(rowptr), ptr(cidx), ptr(vidx),
+           ptr(vals), ptr(A), A.stride(0), ptr(Y), d, stream())
+    return Y
+
+
+def lsk_sketch_left(rowptr, cidx, vidx, vals, X, d):
+    """W (nmat x d x K) = S_b X[b] with X (nmat x n x K)."""
+    nmat, n, Kc = X.shape
+    W = torch.empty((nmat, d, Kc), dtype=torch.float32, device=X.device)
+    _timed("lsk_sketch_left", 1, call, "rla_lsk_sketch_left", nmat, d, Kc, n, 8, ptr(rowptr), ptr(cidx), ptr(vidx),
+           ptr(vals), ptr(X), ptr(W), stream())
+    return W
+
+
+def lsk_value_grad(rows, vals, X, dW):
+    nmat, n, Kc = X.shape
+    d = dW.shape[1]
+    dO = torch.empty((nmat * n, 8), dtype=torch.float32, device=X.device)
+    _timed("lsk_value_grad", 1, call, "rla_lsk_value_grad", nmat, d, Kc, n, ptr(rows), ptr(vals), ptr(X), ptr(dW),
+           ptr(dO), stream())
+    return dO
+
+
+def lsk_loss(W, sigma, k):
+    """Per-matrix loss (binary64) and dloss/dW for W (nmat x d x K), sigma (nmat x K)."""
+    nmat, d, Kc = W.shape
+    sz = C.c_size_t(0)
+    call("rla_lsk_loss", nmat, d, Kc, k, None, None, None, None, None, C.byref(sz), stream())
+    ws = workspace(sz.value)
+    loss = torch.empty((nmat,), dtype=torch.float64, device=W.device)
+    dW = torch.empty_like(W)
+    _timed("lsk_loss", 1, call, "rla_lsk_loss", nmat, d, Kc, k, ptr(W), ptr(sigma), ptr(loss), ptr(dW), ptr(ws),
+           C.byref(sz), stream())
+    return loss, dW
+
+
 def trtri_upper(R, mode=None):
     if mode is None:
         mode = "f32" if R.dtype == torch.float32 else "f64"

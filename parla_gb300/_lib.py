@@ -63,6 +63,15 @@ SIGNATURES = {
     "rla_potrf_upper": [_i32, _i64, _p, _i64, _p, _p, _psz, _p],
     "rla_chol_inv_f32": [_i64, _p, _i64, _p, _i64, _p, _i64, _p, _p],
     "rla_potrf_df_small": [_i64, _p, _i64, _p, _i64, _p, _i64, _p, _p],
+    "rla_col_sumsq": [_i64, _i64, _p, _i64, _p, _p],
+    "rla_lsk_features": [_i64, _i64, _i32, _p, _p, _p, _p],
+    "rla_mlp_fwd": [_i64, _i64, _p, _p, _p, _p, _p, _p],
+    "rla_mlp_bwd": [_i64, _p, _p, _p, _p, C.c_float, _p, _p, _psz, _p],
+    "rla_adam_step": [_i64, _p, _p, _p, _p, C.c_float, C.c_float, C.c_float, C.c_float, _i64, _p],
+    "rla_lsk_sketch_right": [_i64, _i64, _i32, _p, _p, _p, _p, _p, _i64, _p, _i64, _p],
+    "rla_lsk_sketch_left": [_i64, _i32, _i32, _i64, _i32, _p, _p, _p, _p, _p, _p, _p],
+    "rla_lsk_value_grad": [_i64, _i32, _i32, _i64, _p, _p, _p, _p, _p, _p],
+    "rla_lsk_loss": [_i64, _i32, _i32, _i32, _p, _p, _p, _p, _p, _psz, _p],
     "rla_svd_jacobi": [_i32, _i64, _p, _i64, _p, _i64, _p, _p, _i32, _i32, _p],
     "rla_trtri_upper": [_i32, _i64, _p, _i64, _p, _i64, _p],
     "rla_lsqr_run": [_i32, _i64, _i64, _i64, _p, _p, _p, _i64, _p, _i64, _f64, _p, _p, _i32, _f64, _f64,
