@@ -222,10 +222,83 @@ def run_ours(args):
         line["cpu_baseline"] = cpu_baseline(A.cpu().numpy(), budget_s=args.cpu_budget)
     del A, Ad_, A_host
     torch.cuda.empty_cache()
+    line["sketch_apply"] = bench_sketch_apply(torch)
+    if args.learned:
+        line["learned_sketch"] = bench_learned(torch, args.learned_eval)
     if args.ls:
         line["ls_single"] = bench_ls_single(torch, pg)
         line["ls_batched"] = bench_ls_batched(torch, pg, args.ls_problems)
     print(json.dumps(line))
+
+
+def _event_ms(torch, fn, reps=10):
+    fn()
+    torch.cuda.synchronize()
+    s_, e_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s_.record()
+    for _ in range(reps):
+        fn()
+    e_.record()
+    torch.cuda.synchronize()
+    return s_.elapsed_time(e_) / reps
+
+
+def bench_sketch_apply(torch):
+    """HBM roofline of the sketch-apply kernels on inputs larger than L2.
+
+    Algorithmic bytes: A read once, the sketch written once, the pattern read
+    once (SJLT: 4-byte row + 1-byte sign per nonzero; learned: CSR 8 bytes +
+    4-byte value per nonzero)."""
+    from parla_gb300 import _kernels as K
+    from parla_gb300.learned.sketch import SJLTPattern
+    hbm, _, src = peaks()
+    out = {"peak_gbs": hbm, "peak_source": src}
+    m, n, d = 65536, 512, 2048
+    rows, signs = K.sjlt_pattern(d, m, 8, 1)
+    for dt, tag in ((torch.float64, "sjlt_f64"), (torch.float32, "sjlt_f32")):
+        A = torch.randn((m, n), device="cuda", dtype=dt)
+        es = A.element_size()
+        ms = _event_ms(torch, lambda: K.sjlt_apply(rows, signs, 8, d, A, 8 ** -0.5))
+        byts = m * n * es + d * n * es + m * 8 * 5
+        out[tag] = {"shape": f"S (2048 x 65536, 8 nnz/col) @ A (65536 x 512 {tag[-3:]})", "ms": ms,
+                    "gbs": byts / ms / 1e6, "frac": byts / ms / 1e6 / hbm}
+        del A
+    m2, n2, d2 = 16384, 4096, 74
+    A = torch.randn((m2, n2), device="cuda", dtype=torch.float32)
+    pat = SJLTPattern(d2, n2, 1234)
+    vals = torch.randn((n2, 8), device="cuda", dtype=torch.float32)
+    ms = _event_ms(torch, lambda: pat.right(A, vals))
+    byts = m2 * n2 * 4 + m2 * d2 * 4 + n2 * 8 * 12
+    out["learned_right"] = {"shape": "A (16384 x 4096 f32) @ S^T (learned values, 74 rows)", "ms": ms,
+                            "gbs": byts / ms / 1e6, "frac": byts / ms / 1e6 / hbm}
+    return out
+
+
+def bench_learned(torch, n_eval):
+    """Learned sparse sketch on the 4096 x 4096 family (k = 64, d = 74) with the
+    shipped network: held-out range-finder errors against the plain Gaussian
+    and plain SJLT sketches of the same size, the guard's fallback rate, and
+    the time of one guarded QB against a plain Gaussian QB (binary32)."""
+    import numpy as np
+    from parla_gb300 import learned as L
+    from parla_gb300.learned import train as T
+    from parla_gb300 import QB1, RF1, RS1, SkOpGA
+    out = {"workload": "family A = G1 diag(exp(-i/40)) G2^T + 1e-3 N, 4096 x 4096, rank 64..256; k=64, d=74, "
+                       "8 nnz/col; network trained on 16384 matrices (seeds 0..16383)",
+           "held_out_seeds": f"{T.HELD_OUT_SEED0}..{T.HELD_OUT_SEED0 + n_eval - 1}"}
+    net = L.SketchNet.load()
+    out["cfg5"] = T.summary(T.evaluate(net, list(range(T.HELD_OUT_SEED0, T.HELD_OUT_SEED0 + n_eval)), 74, 64))
+    kw = {"coherent": True, "noise": 0.05, "decay": 24.0, "rank_range": (32, 128)}
+    netc = L.SketchNet.load(os.path.join(ROOT, "parla_gb300", "learned", "sketchnet_k64_d74_coherent.npz"))
+    out["coherent"] = T.summary(T.evaluate(netc, list(range(T.HELD_OUT_SEED0, T.HELD_OUT_SEED0 + min(256, n_eval))),
+                                           74, 64, **kw))
+    out["coherent"]["family"] = "columns of G2 scaled by exp(1.5 N(0,1)); noise 0.05, decay 24, rank 32..128"
+    A, _ = L.family_matrix(T.HELD_OUT_SEED0)
+    guard = L.LearnedQB(net)
+    plain = QB1(RF1(RS1(SkOpGA(), 0), precision="f32"), precision="f32")
+    out["qb_ms"] = {"learned_guarded": _event_ms(torch, lambda: guard(A, 74, np.nan, 1), reps=5),
+                    "plain_gaussian": _event_ms(torch, lambda: plain(A, 74, np.nan, 1), reps=5)}
+    return out
 
 
 def bench_ls_single(torch, pg):
@@ -407,6 +480,9 @@ def main():
     ap.add_argument("--no-ls", dest="ls", action="store_false", default=True,
                     help="skip the least-squares measurements (configs[0] and configs[2])")
     ap.add_argument("--ls-problems", type=int, default=1024)
+    ap.add_argument("--no-learned", dest="learned", action="store_false", default=True,
+                    help="skip the learned-sketch evaluation (configs[4])")
+    ap.add_argument("--learned-eval", type=int, default=1024)
     args = ap.parse_args()
     if args.case:
         run_case(args)

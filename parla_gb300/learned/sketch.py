@@ -59,12 +59,14 @@ def pattern_for(d, n, seed):
     return _PATTERNS[key]
 
 
-def column_features(A, seed, k_pre=K_PRE):
+def column_features(A, seed, k_pre=K_PRE, want_presketch_error=False):
     """Features (n x 4) of a binary32 device matrix A (m x n).
 
     Squared column norms, and leverage scores of the columns in the row space
     of P = Gamma A with a k_pre x m Gaussian Gamma: lev_j = ||R^-T p_j||^2 where
-    P P^T = R^T R.  Returns (F, cn2, lev).
+    P P^T = R^T R.  Returns (F, cn2, lev), plus, when asked, the a-posteriori
+    error of that plain Gaussian sketch, ||A - A Z^T Z||_F with Z = R^-T P
+    (orthonormal rows): the plain sketch's error the learned one is held to.
     """
     m, n = A.shape
     cn2 = K.col_sumsq(A)
@@ -75,7 +77,12 @@ def column_features(A, seed, k_pre=K_PRE):
     Z = K.gemm(Rinv, P, transa=True, mode="f32")
     lev = K.col_sumsq(Z)
     F = K.lsk_features(cn2.view(1, -1), lev.view(1, -1), k_pre).view(n, 4)
-    return F, cn2, lev
+    if not want_presketch_error:
+        return F, cn2, lev
+    AZ = K.gemm(A, Z, transb=True, mode="f32")
+    a2 = float(torch.sum(cn2.double()))
+    c2 = float(torch.sum(K.col_sumsq(AZ).double()))
+    return F, cn2, lev, float(np.sqrt(max(a2 - c2, 0.0)))
 
 
 class LearnedSketchOperator(DeviceOperator):
@@ -103,11 +110,13 @@ class RSLearned(RowSketcher):
 
     ``pattern_seed`` fixes the sparsity pattern (the network was trained on one
     pattern per (k, n)); the features use a Gaussian pre-sketch drawn from rng.
+    ``last_presketch_error`` keeps the a-posteriori error of that pre-sketch.
     """
 
     def __init__(self, net, pattern_seed=1234):
         self.net = net
         self.pattern_seed = pattern_seed
+        self.last_presketch_error = None
 
     def __call__(self, A, k, rng):
         Am = opd.wrap(A)
@@ -115,41 +124,42 @@ class RSLearned(RowSketcher):
         m, n = Ad.shape
         rng = np.random.default_rng(rng)
         pat = pattern_for(k, n, self.pattern_seed)
-        F, _, _ = column_features(Ad.contiguous(), int(rng.integers(1, 2 ** 62)))
+        F, _, _, e_pre = column_features(Ad.contiguous(), int(rng.integers(1, 2 ** 62)), want_presketch_error=True)
+        self.last_presketch_error = e_pre
         vals, _ = self.net.forward(F, pat.signs, n)
         return LearnedSketchOperator(pat, vals)
 
 
 class LearnedQB(QBDecomposer):
-    """QB with the learned sketch, guarded by the plain sketch's error bound.
+    """QB with the learned sketch, guarded by a plain sketch's error.
 
-    After Q from the learned sketch and B = Q^T A, the error is known exactly
-    a posteriori: e^2 = ||A||_F^2 - ||B||_F^2.  With k_t = k - oversampling the
-    plain Gaussian sketch satisfies E||A - Q Q^T A||_F <= sqrt(1 + k_t/(p-1)) *
-    (sum_{i>k_t} s_i^2)^(1/2) (Halko, Martinsson, Tropp 2011, Thm 10.5), and
-    sum_{k_t<i<=k} sb_i^2 (sb: singular values of B, which interlace those of A)
-    is a lower bound of that tail.  When e exceeds the bound evaluated on that
-    lower bound, the call is repeated with the plain Gaussian sketch.
+    After Q from the learned d-column sketch and B = Q^T A the error is known
+    a posteriori: e^2 = ||A||_F^2 - ||B||_F^2.  The features were computed from
+    a plain Gaussian sketch with 32 rows, whose a-posteriori error e_32 comes
+    at the cost of one 32-column product; a healthy d-column sketch (d > 32)
+    does better than it (for Gaussian sketches the expected error falls with
+    the sketch size, Halko, Martinsson, Tropp 2011, Thm 10.5).  When e > e_32
+    the call is repeated with the plain Gaussian sketch of the same size.
     """
 
     TOL_CONTROL = "none"
 
-    def __init__(self, net, oversampling=10, fallback=True, pattern_seed=1234):
+    def __init__(self, net, fallback=True, pattern_seed=1234):
         self.net = net
-        self.oversampling = oversampling
         self.fallback = fallback
         self.pattern_seed = pattern_seed
         self.last = {}
 
     def __call__(self, A, k, tol, rng):
-        assert k > self.oversampling
+        assert k > K_PRE
         rng = np.random.default_rng(rng)
         Ad = K.to_dev(A, torch.float32) if not isinstance(A, torch.Tensor) else A
         Ad = Ad if Ad.dtype == torch.float32 else Ad.to(torch.float32)
         Ad = Ad.contiguous()
-        qb = QB1(RF1(RSLearned(self.net, self.pattern_seed), precision="f32"), precision="f32")
-        Q, B = qb(Ad, k, np.nan, rng)
-        est, bound = self.estimate(Ad, B, k)
+        rs = RSLearned(self.net, self.pattern_seed)
+        Q, B = QB1(RF1(rs, precision="f32"), precision="f32")(Ad, k, np.nan, rng)
+        est = self.error(Ad, B)
+        bound = rs.last_presketch_error
         used = False
         if self.fallback and not est <= bound:
             Q, B = QB1(RF1(RS1(SkOpGA(), 0), precision="f32"), precision="f32")(Ad, k, np.nan, rng)
@@ -157,12 +167,9 @@ class LearnedQB(QBDecomposer):
         self.last = {"estimate": est, "bound": bound, "fallback": used}
         return Q, B
 
-    def estimate(self, A, B, k):
+    @staticmethod
+    def error(A, B):
+        """||A - Q B||_F = (||A||^2 - ||B||^2)^(1/2) for B = Q^T A, Q orthonormal."""
         a2 = float(torch.sum(K.col_sumsq(A).double()))
         b2 = float(torch.sum(K.col_sumsq(B.contiguous()).double()))
-        est = float(np.sqrt(max(a2 - b2, 0.0)))
-        _, sb, _ = law.small_svd_wide(B.contiguous())
-        kt = k - self.oversampling
-        tail = float(torch.sum(sb[kt:k].double() ** 2))
-        bound = float(np.sqrt(1.0 + kt / (self.oversampling - 1.0)) * np.sqrt(tail))
-        return est, bound
+        return float(np.sqrt(max(a2 - b2, 0.0)))

@@ -19,7 +19,7 @@ from .. import _kernels as K
 from ..utils import linalg_wrappers as law
 from .family import family_matrix, plain_targets
 from .network import Adam, SketchNet
-from .sketch import column_features, pattern_for
+from .sketch import K_PRE, column_features, pattern_for
 
 HELD_OUT_SEED0 = 10 ** 6
 
@@ -89,7 +89,7 @@ def evaluate(net, seeds, d, k, pattern_seed=1234, **family_kw):
     pat = pattern_for(d, n, pattern_seed)
     zero = torch.zeros_like(net.params)
     out = []
-    guard = LearnedQB(net, oversampling=d - k, pattern_seed=pattern_seed)
+    guard = LearnedQB(net, pattern_seed=pattern_seed)
     for s in seeds:
         A, r = family_matrix(s, **family_kw)
         F, _, _ = column_features(A, s + 7)
@@ -99,9 +99,11 @@ def evaluate(net, seeds, d, k, pattern_seed=1234, **family_kw):
         e_p = range_error(A, pat.right(A, v0))
         Om = K.gaussian_fill(n, d, s + 11, 1.0, torch.float32)
         e_g = range_error(A, K.gemm(A, Om, mode="f32"))
-        guard(A, d, np.nan, s + 13)
-        out.append({"seed": s, "rank": r, "learned": e_l, "plain_sjlt": e_p, "gaussian": e_g,
-                    "fallback": guard.last["fallback"]})
+        fb = None
+        if d > K_PRE:  # the guard compares with the 32-row pre-sketch
+            guard(A, d, np.nan, s + 13)
+            fb = guard.last["fallback"]
+        out.append({"seed": s, "rank": r, "learned": e_l, "plain_sjlt": e_p, "gaussian": e_g, "fallback": fb})
     return out
 
 
@@ -111,7 +113,8 @@ def summary(rows):
     g = np.array([r["gaussian"] for r in rows])
     return {"matrices": len(rows), "ratio_vs_gaussian": float(np.mean(l / g)),
             "ratio_vs_plain_sjlt": float(np.mean(l / p)), "plain_sjlt_vs_gaussian": float(np.mean(p / g)),
-            "fallback_rate": float(np.mean([r["fallback"] for r in rows]))}
+            "fallback_rate": (float(np.mean([r["fallback"] for r in rows]))
+                              if all(r["fallback"] is not None for r in rows) else None)}
 
 
 def main():
@@ -126,9 +129,13 @@ def main():
     ap.add_argument("--targets", type=int, default=128)
     ap.add_argument("--size", type=int, default=4096)
     ap.add_argument("--coherent", action="store_true")
+    ap.add_argument("--noise", type=float, default=1e-3)
+    ap.add_argument("--decay", type=float, default=40.0)
+    ap.add_argument("--rank", type=int, nargs=2, default=(64, 256))
     ap.add_argument("--out", default=None)
     args = ap.parse_args()
-    kw = {"m": args.size, "n": args.size, "coherent": args.coherent}
+    kw = {"m": args.size, "n": args.size, "coherent": args.coherent, "noise": args.noise, "decay": args.decay,
+          "rank_range": tuple(args.rank)}
     net = SketchNet(seed=0)
     t0 = time.time()
     hist = train(net, list(range(args.n_train)), args.d, args.k, args.targets, batch=args.batch, lr=args.lr,

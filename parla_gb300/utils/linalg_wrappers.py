@@ -12,6 +12,9 @@ import torch
 from .. import _kernels as K
 from .._lib import RlaError
 
+# largest order of the single-CTA double-float Cholesky (and of the Jacobi SVD path)
+JACOBI_MAX = 232
+
 
 def householder_orth(S):
     """Thin Q of a binary64 m x k matrix by device Householder QR."""
@@ -29,12 +32,14 @@ def cholqr(Y, passes=2):
     for p in range(passes):
         Q64 = Q if Q.dtype == torch.float64 else Q.to(torch.float64)
         G = K.gemm(Q64, Q64, transa=True, mode="df")
+        k = G.shape[0]
+        chol = (lambda X: K.potrf_df_small(X, want64=True)[1]) if k <= JACOBI_MAX else \
+            (lambda X: K.potrf_upper(X.clone(), mode="df"))
         try:
-            R = K.potrf_upper(G.clone(), mode="df")
+            R = chol(G)
         except RlaError:
-            k = G.shape[0]
             shift = 1e-7 * float(torch.trace(G)) / k + 1e-30
-            R = K.potrf_upper(G + shift * torch.eye(k, dtype=G.dtype, device=G.device), mode="df")
+            R = chol(G + shift * torch.eye(k, dtype=G.dtype, device=G.device))
         Rinv = K.trtri_upper(R, mode="df")
         Q = K.gemm(Q, Rinv if Q.dtype == torch.float64 else Rinv.to(Q.dtype))
     return Q
@@ -55,9 +60,6 @@ def sym_eig(G):
     """
     Gs = 0.5 * (G + G.t())
     return torch.linalg.eigh(Gs)
-
-
-JACOBI_MAX = 232
 
 
 def _svd_from_gram(G):

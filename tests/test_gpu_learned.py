@@ -167,22 +167,28 @@ def test_training_gains_over_plain_sjlt(env):
 
 
 def test_fallback_guard(env):
-    """A network that suppresses the heavy columns trips the guard, which
-    reruns with the plain Gaussian sketch; the plain-SJLT network does not."""
+    """A network that keeps only the few heaviest columns (a rank-deficient
+    sketch) does worse than the 32-row plain pre-sketch, which trips the
+    guard; the guard then reruns with the plain Gaussian sketch.  The
+    plain-SJLT network passes."""
     K, L = env
+    from parla_gb300.learned import train as T
     kw = {"m": 512, "n": 512, "coherent": True, "noise": 0.05, "rank_range": (32, 64), "decay": 12.0}
     A, _ = L.family_matrix(77, **kw)
-    d = 26
-    ok = L.LearnedQB(L.SketchNet(np.zeros(OL.N_PARAMS, dtype=np.float32)), oversampling=10)
+    d = 48
+    ok = L.LearnedQB(L.SketchNet(np.zeros(OL.N_PARAMS, dtype=np.float32)))
     Q, B = ok(A, d, np.nan, 1)
     assert not ok.last["fallback"] and ok.last["estimate"] <= ok.last["bound"]
+    err = float(torch.linalg.matrix_norm(A.double() - Q.double() @ B.double()))
+    # ||A||^2 - ||B||^2 from binary32 column sums: exact up to the cancellation
+    assert abs(err - ok.last["estimate"]) <= 1e-2 * err
     p = np.zeros(OL.N_PARAMS, dtype=np.float32)
-    p[0] = 20.0                         # W1[0][0]: hidden unit 0 follows the log norm ratio
-    p[OL.OFF_W2:OL.OFF_B2].reshape(8, 64)[:, 0] = -12.0
-    bad = L.LearnedQB(L.SketchNet(p), oversampling=10)
+    p[2] = 20.0                         # W1[0][2]: hidden unit 0 = +1 iff norm ratio > 5
+    p[OL.OFF_B1] = -80.0
+    p[OL.OFF_W2:OL.OFF_B2].reshape(8, 64)[:, 0] = 12.0   # those columns weigh e^24 more
+    bad = L.LearnedQB(L.SketchNet(p))
     Q, B = bad(A, d, np.nan, 1)
-    assert bad.last["fallback"]
-    from parla_gb300.learned import train as T
+    assert bad.last["fallback"] and bad.last["estimate"] > bad.last["bound"]
     err = float(torch.linalg.matrix_norm(A.double() - Q.double() @ B.double()))
     Om = K.gaussian_fill(512, d, 3, 1.0, torch.float32)
     assert err <= 1.5 * T.range_error(A, K.gemm(A, Om, mode="f32"))
