@@ -457,9 +457,10 @@ def run_case(args):
         for _ in range(3):
             h = K.lsqr_launch(None, M, b, None, 0.0, 0.0, 0.0, 0.0, 8, "df", (hi, lo), 0, 0.0)
         torch.cuda.synchronize()
-    elif args.case == "sjlt":
+    elif args.case in ("sjlt", "sjlt32"):
         m, n, d = 65536, 512, 2048
-        A = torch.randn((m, n), generator=g, device="cuda", dtype=torch.float64)
+        dt = torch.float64 if args.case == "sjlt" else torch.float32
+        A = torch.randn((m, n), generator=g, device="cuda", dtype=dt)
         rows, signs = K.sjlt_pattern(d, m, 8, 1)
         for _ in range(3):
             K.sjlt_apply(rows, signs, 8, d, A, 8 ** -0.5)
@@ -468,7 +469,7 @@ def run_case(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--case", default=None, choices=["tc_pass", "sjlt", "lsqr"],
+    ap.add_argument("--case", default=None, choices=["tc_pass", "sjlt", "sjlt32", "lsqr"],
                     help="run one small kernel case for a profiler capture and exit")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)

@@ -12,6 +12,7 @@
 //                     through distributed shared memory, and one partial per
 //                     cluster goes to the workspace for a fixed-order sum.
 // rla_sjlt_apply_right - Y = A S for a tall S (RS1 / learned-sketch use).
+// Binary32 inputs with d <= 2048 take the chunked path of sjlt_chunked.cu.
 #include <climits>
 #include <cooperative_groups.h>
 #include "common.cuh"
@@ -19,6 +20,10 @@
 namespace cg = cooperative_groups;
 
 namespace rla {
+size_t sjlt_chunked_ws(int64_t d, int64_t m, int nnz);
+int sjlt_apply_chunked_f32(int64_t d, int64_t m, int64_t n, int nnz, const int32_t* rows, const int8_t* signs,
+                           double scale, const float* A, int64_t lda, float* Y, int64_t ldy, void* ws,
+                           cudaStream_t st);
 namespace {
 
 constexpr int kClusterChunks = 8;    // CTAs per cluster along the row-chunk axis
@@ -298,7 +303,20 @@ int rla_sjlt_apply(int dtype, int64_t d, int64_t m, int64_t n, int nnz, const in
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   switch (dtype) {
     case RLA_F64: return rla::sjlt_apply_impl<double>(d, m, n, nnz, rows, signs, scale, A, lda, Y, ldy, ws, ws_bytes, st);
-    case RLA_F32: return rla::sjlt_apply_impl<float>(d, m, n, nnz, rows, signs, scale, A, lda, Y, ldy, ws, ws_bytes, st);
+    case RLA_F32: {
+      // binary32 with d <= 2048: the chunked bandwidth path (its own workspace)
+      const size_t cws = rla::sjlt_chunked_ws(d, m, nnz);
+      if (cws > 0 && n > 0) {
+        if (ws == nullptr && ws_bytes != nullptr) {
+          *ws_bytes = cws;
+          return RLA_OK;
+        }
+        if (!ws_bytes || *ws_bytes < cws) return RLA_ERR_WORKSPACE;
+        return rla::sjlt_apply_chunked_f32(d, m, n, nnz, rows, signs, scale, static_cast<const float*>(A), lda,
+                                           static_cast<float*>(Y), ldy, ws, st);
+      }
+      return rla::sjlt_apply_impl<float>(d, m, n, nnz, rows, signs, scale, A, lda, Y, ldy, ws, ws_bytes, st);
+    }
     default: return RLA_ERR_ARG;
   }
 }

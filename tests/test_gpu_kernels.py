@@ -91,8 +91,30 @@ def test_sjlt_apply_matches_reference_operator(K, dtype, d, m, n):
     signs = np.sign(Sc.data).astype(np.int8)
     tdt = torch.float64 if dtype == np.float64 else torch.float32
     Y = K.sjlt_apply(dev(rows), dev(signs), 8, d, dev(A, tdt), 1 / np.sqrt(8)).cpu().numpy()
-    tol = 1e-14 if dtype == np.float64 else 1e-6
+    tol = 1e-14 if dtype == np.float64 else 1e-5  # binary32: exact fixed point / binary32 sums
     assert rel(Y, ref) <= tol
+
+
+@pytest.mark.parametrize("d,m,n,nnz,pad", [(2048, 50000, 40, 8, 0), (1000, 3000, 33, 16, 3), (64, 1024, 16, 8, 0),
+                                           (3000, 5000, 70, 8, 4),
+                                           (512, 7777, 100, 4, 4)])
+def test_sjlt_apply_f32_chunked_path(K, d, m, n, nnz, pad):
+    """Binary32 inputs with d <= 2048 take the chunked kernel: ragged slabs and
+    chunks, padded leading dimensions, and bitwise repeatable results."""
+    rng = np.random.default_rng(d + m)
+    rows, signs = K.sjlt_pattern(d, m, nnz, 17)
+    A = rng.standard_normal((m, n + pad)).astype(np.float32)
+    Ad = dev(A, torch.float32)[:, :n]
+    Y = K.sjlt_apply(rows, signs, nnz, d, Ad, nnz ** -0.5)
+    Y2 = K.sjlt_apply(rows, signs, nnz, d, Ad, nnz ** -0.5)
+    assert torch.equal(Y, Y2)
+    r = rows.cpu().numpy().reshape(m, nnz)
+    sg = signs.cpu().numpy().reshape(m, nnz).astype(np.float64)
+    ref = np.zeros((d, n))
+    for t in range(nnz):
+        np.add.at(ref, r[:, t], sg[:, t, None] * A[:, :n].astype(np.float64))
+    ref *= nnz ** -0.5
+    assert rel(Y.cpu().numpy(), ref) <= 1e-5
 
 
 def test_sjlt_apply_with_replacement_duplicates(K):
