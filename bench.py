@@ -223,6 +223,8 @@ def run_ours(args):
     del A, Ad_, A_host
     torch.cuda.empty_cache()
     line["sketch_apply"] = bench_sketch_apply(torch)
+    if args.nystrom:
+        line["nystrom_evd2"] = bench_nystrom(torch, pg)
     if args.learned:
         line["learned_sketch"] = bench_learned(torch, args.learned_eval)
     if args.ls:
@@ -271,6 +273,86 @@ def bench_sketch_apply(torch):
     byts = m2 * n2 * 4 + m2 * d2 * 4 + n2 * 8 * 12
     out["learned_right"] = {"shape": "A (16384 x 4096 f32) @ S^T (learned values, 74 rows)", "ms": ms,
                             "gbs": byts / ms / 1e6, "frac": byts / ms / 1e6 / hbm}
+    return out
+
+
+def _rbf_problem(N, dim=16, seed=2024):
+    """Points of the mixture (8 means ~ N(0, 4 I), unit variance) and
+    gamma = 1 / (2 h^2), h the median pairwise distance of a 2048-point subsample."""
+    import numpy as np
+    from scipy.spatial.distance import pdist
+    rng = np.random.default_rng(seed)
+    means = rng.normal(0.0, 2.0, (8, dim))
+    X = means[rng.integers(0, 8, N)] + rng.normal(0.0, 1.0, (N, dim))
+    h = float(np.median(pdist(X[rng.choice(N, 2048, replace=False)])))
+    return X, 1.0 / (2.0 * h * h), h
+
+
+def bench_nystrom(torch, pg):
+    """Nystrom EVD2 (configs[3]) on the 32768 x 32768 Gaussian kernel matrix,
+    k = 512, over = 16: K S on the bf16 tensor cores (split hi + lo pair,
+    fp32 accumulation), shift / S^T Y / Cholesky / SVD of B in double-float.
+    The kernel matrix is built on the device by rla_rbf_kernel_matrix (timed
+    separately).  Accuracy: the same solver on the 8192-point sub-problem
+    (first 8192 points, same bandwidth) against binary64 eigvalsh of its
+    kernel matrix."""
+    import numpy as np
+    from parla_gb300 import _kernels as K
+    from parla_gb300.utils.operand import DeviceMatrix
+    N, k, over = 32768, 512, 16
+    X, gamma, h = _rbf_problem(N)
+    Xd = torch.from_numpy(X.astype(np.float32)).cuda()
+    out = {"workload": f"EVD2(RS1(SkOpGA, 0)) on the {N}x{N} RBF kernel of 8-cluster points in R^16, "
+                       f"k={k}, over={over}, h={h:.4f} (median pairwise distance of 2048 points)"}
+    t_gen = _event_ms(torch, lambda: K.rbf_matrix(Xd, gamma, 2), reps=2)
+    hi, lo = K.rbf_matrix(Xd, gamma, 2)
+    Am = DeviceMatrix.from_bf16(hi, lo)
+    evd = pg.EVD2(pg.RS1(pg.SkOpGA(), 0))
+    import warnings
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        t_evd = _event_ms(torch, lambda: evd(Am, k, np.nan, over, 1), reps=3)
+        V, lam = evd(Am, k, np.nan, over, 1)
+    out["bf16_split"] = {"ms": t_evd, "kernel_matrix_ms": t_gen, "retained": int(lam.numel()),
+                         "lambda_1": float(lam[0])}
+    del hi, lo, Am
+    torch.cuda.empty_cache()
+    K32 = K.rbf_matrix(Xd, gamma, 0)
+    evd32 = pg.EVD2(pg.RS1(pg.SkOpGA(), 0), precision="f32")
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        t32 = _event_ms(torch, lambda: evd32(K32, k, np.nan, over, 1), reps=2)
+    out["plain_fp32_gpu"] = {"ms": t32, "speedup": t32 / t_evd}
+    del K32
+    torch.cuda.empty_cache()
+    # accuracy on the 8192-point sub-problem
+    n2 = 8192
+    X2 = Xd[:n2].contiguous()
+    K64 = torch.exp(-gamma * torch.cdist(X2.double(), X2.double()) ** 2)
+    ref = np.sort(torch.linalg.eigvalsh(K64).cpu().numpy())[::-1]
+    del K64
+    hi, lo = K.rbf_matrix(X2, gamma, 2)
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        _, lam2 = evd(DeviceMatrix.from_bf16(hi, lo), k, np.nan, over, 2)
+        K64 = torch.exp(-gamma * torch.cdist(X2.double(), X2.double()) ** 2)
+        _, lam64 = evd(K64, k, np.nan, over, 2)          # binary64 path, same sketch
+        del K64
+    lam2 = lam2.double().cpu().numpy()
+    lam64 = lam64.cpu().numpy()
+    r = min(lam2.size, lam64.size)
+    rel = np.abs(lam2[:r] - ref[:r]) / ref[:r]
+    rel64 = np.abs(lam64[:r] - ref[:r]) / ref[:r]
+    prec = np.abs(lam2[:r] - lam64[:r]) / lam64[:r]
+    out["subproblem_8192"] = {
+        "retained": r,
+        "vs_exact_eigh": {"rel_err_median": float(np.median(rel)), "rel_err_top10_max": float(np.max(rel[:10])),
+                          "rel_err_max": float(np.max(rel))},
+        "fp64_nystrom_vs_exact_eigh": {"rel_err_median": float(np.median(rel64)),
+                                       "rel_err_top10_max": float(np.max(rel64[:10]))},
+        "bf16_vs_fp64_nystrom_same_sketch": {"rel_err_median": float(np.median(prec)),
+                                             "rel_err_max": float(np.max(prec))},
+        "lambda_ratio_last": float(ref[r - 1] / ref[0])}
     return out
 
 
@@ -484,6 +566,8 @@ def main():
     ap.add_argument("--no-learned", dest="learned", action="store_false", default=True,
                     help="skip the learned-sketch evaluation (configs[4])")
     ap.add_argument("--learned-eval", type=int, default=1024)
+    ap.add_argument("--no-nystrom", dest="nystrom", action="store_false", default=True,
+                    help="skip the Nystrom EVD2 measurement (configs[3])")
     args = ap.parse_args()
     if args.case:
         run_case(args)

@@ -386,6 +386,16 @@ int rla_lsk_value_grad(int64_t nmat, int d, int K, int64_t n, const int* rows, c
 int rla_lsk_loss(int64_t nmat, int d, int K, int k, const float* W, const float* sigma, double* loss, float* dW,
                  void* ws, size_t* ws_bytes, rla_stream_t stream);
 
+
+/* Gaussian kernel matrix K_ij = exp(-gamma ||x_i - x_j||^2) of N points
+ * (X: N x dim row-major binary32, dim <= 64), the input of the Nystrom
+ * eigensolver (parla/drivers/evd.py:299-384) on kernel matrices.
+ * mode 0: binary32 K32; mode 1: bf16 hi; mode 2: bf16 pair hi + lo with
+ * lo = bf16(K - hi).  No counterpart in the reference (its tests build A on
+ * the host). */
+int rla_rbf_kernel_matrix(int64_t N, int dim, const float* X, int64_t ldx, float gamma, int mode, float* K32,
+                          int64_t ld32, void* hi, void* lo, int64_t ldb, rla_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

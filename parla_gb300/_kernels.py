@@ -314,6 +314,25 @@ def svd_jacobi(Ct, max_sweeps=40, info=None, cluster=0):
     return U, s, inf
 
 
+def rbf_matrix(X, gamma, mode=0):
+    """K = exp(-gamma ||x_i - x_j||^2) for points X (N x dim, binary32).
+
+    mode 0: binary32 K; 1: bf16 K; 2: (hi, lo) bf16 pair.
+    """
+    X = X.contiguous()
+    N, dim = X.shape
+    if mode == 0:
+        K32 = torch.empty((N, N), dtype=torch.float32, device=X.device)
+        _timed("rbf_matrix", 1, call, "rla_rbf_kernel_matrix", N, dim, ptr(X), dim, C.c_float(gamma), 0, ptr(K32), N,
+               None, None, N, stream())
+        return K32
+    hi = empty_bf16(N, N, X.device)
+    lo = empty_bf16(N, N, X.device) if mode == 2 else None
+    _timed("rbf_matrix", 1, call, "rla_rbf_kernel_matrix", N, dim, ptr(X), dim, C.c_float(gamma), mode, None, N,
+           ptr(hi), ptr(lo), hi.stride(0), stream())
+    return (hi, lo) if mode == 2 else hi
+
+
 # ----------------------------------------------------------- learned sketch
 
 def col_sumsq(A):

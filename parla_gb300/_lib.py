@@ -64,6 +64,7 @@ SIGNATURES = {
     "rla_chol_inv_f32": [_i64, _p, _i64, _p, _i64, _p, _i64, _p, _p],
     "rla_potrf_df_small": [_i64, _p, _i64, _p, _i64, _p, _i64, _p, _p],
     "rla_col_sumsq": [_i64, _i64, _p, _i64, _p, _p],
+    "rla_rbf_kernel_matrix": [_i64, _i32, _p, _i64, C.c_float, _i32, _p, _i64, _p, _p, _i64, _p],
     "rla_lsk_features": [_i64, _i64, _i32, _p, _p, _p, _p],
     "rla_mlp_fwd": [_i64, _i64, _p, _p, _p, _p, _p, _p],
     "rla_mlp_bwd": [_i64, _p, _p, _p, _p, C.c_float, _p, _p, _psz, _p],

@@ -8,7 +8,8 @@ import numpy as np
 import torch
 
 from .. import _kernels as K
-from ..comps.sketchers.aware import _times
+from .._lib import RlaError
+from ..comps.sketchers.aware import _as_panel, _times
 from ..utils import linalg_wrappers as law
 from ..utils import operand as opd
 
@@ -58,12 +59,22 @@ class EVD2(EVDecomposer):
     SVD of B through its l x l Gram, truncation rule and lambda = sigma^2 - nu
     exactly as the reference (only the leading r columns of the reference's
     full-matrices SVD are used, so the thin factorisation is equivalent).
+
+    ``precision`` ('f64', 'f32', 'bf16') selects the arithmetic of Y = A S;
+    A may also be a bf16 ``DeviceMatrix`` (``from_bf16``, optionally a split
+    hi + lo pair).  Everything after Y (shift, S^T Y, Cholesky, B and its
+    SVD) runs in double-float/binary64.  With reduced-precision products the
+    regularisation starts at the reference's nu = sqrt(n) eps ||Y||_F and is
+    raised tenfold (up to u ||Y||_F, u the unit roundoff of the product) only
+    while S^T (Y + nu S) is not numerically positive definite; components with
+    sigma^2 <= nu are dropped by the reference's own rule.
     """
 
     TOL_CONTROL = "none"
 
-    def __init__(self, sk_op):
+    def __init__(self, sk_op, precision=None):
         self.sk_op = sk_op
+        self.precision = precision
 
     def __call__(self, A, k, tol, over, rng):
         assert k > 0
@@ -75,17 +86,42 @@ class EVD2(EVDecomposer):
             approximation error. Parameter "tol" is being ignored.
             """)
         rng = np.random.default_rng(rng)
-        Ad = A if isinstance(A, torch.Tensor) and A.is_cuda else K.to_dev(A, torch.float64)
+        if isinstance(A, opd.DeviceMatrix) or self.precision is not None:
+            Am = opd.wrap(A, self.precision)
+            Ad = Am
+            u = Am.unit_roundoff
+        else:
+            Ad = A if isinstance(A, torch.Tensor) and A.is_cuda else K.to_dev(A, torch.float64)
+            Am = None
+            u = 0.0
         S = self.sk_op(Ad, k + over, rng)
-        S = S.to(Ad.dtype) if S.dtype != Ad.dtype else S
-        Y = _times(Ad, S)
+        if Am is not None and Am.tc:
+            S = S if isinstance(S, torch.Tensor) else _as_panel(S, torch.float32)
+            Y = opd.tc_times(Am, S).contiguous()
+        else:
+            Ab = Am.A if Am is not None else Ad
+            S = S.to(Ab.dtype) if isinstance(S, torch.Tensor) and S.dtype != Ab.dtype else S
+            Y = _times(Ab, S)
+        S = S if isinstance(S, torch.Tensor) else _as_panel(S, torch.float64)
         Y64 = Y.to(torch.float64) if Y.dtype != torch.float64 else Y
         S64 = S.to(torch.float64) if S.dtype != torch.float64 else S
-        nu = float(np.sqrt(n) * EPS * float(torch.linalg.vector_norm(Y64)))
+        ynorm = float(torch.linalg.vector_norm(Y64))
+        nu = float(np.sqrt(n) * EPS * ynorm)
+        SY = K.gemm(S64, Y64, transa=True, mode="df")
+        StS = K.gemm(S64, S64, transa=True, mode="df") if u > 0 else None
+        while True:
+            G = SY + nu * StS if StS is not None else K.gemm(S64, Y64 + nu * S64, transa=True, mode="df")
+            G = 0.5 * (G + G.t())
+            try:
+                R = K.potrf_upper(G.contiguous(), mode="df")
+                break
+            except RlaError:
+                # reduced-precision Y: the smallest shift (x10 steps, up to
+                # the product's unit roundoff) that keeps S^T (Y + nu S) definite
+                if u <= 0 or nu >= u * ynorm:
+                    raise
+                nu = min(10.0 * nu, u * ynorm)
         Y64 = Y64 + nu * S64
-        G = K.gemm(S64, Y64, transa=True, mode="df")
-        G = 0.5 * (G + G.t())
-        R = K.potrf_upper(G.contiguous(), mode="df")
         Rinv = K.trtri_upper(R, mode="df")
         B = K.gemm(Y64, Rinv, mode="df")
         V, sigma, _ = law.small_svd_tall(B)
@@ -94,4 +130,8 @@ class EVD2(EVDecomposer):
         r = min(cuts)
         lamb = (sigma ** 2)[:r] - nu
         V = V[:, :r].contiguous()
-        return K.like_input(V.to(Ad.dtype), A), K.like_input(lamb.to(Ad.dtype), A)
+        out_dtype = torch.float32 if Am is not None and Am.dtype == torch.float32 else (
+            Ad.dtype if isinstance(Ad, torch.Tensor) else torch.float64)
+        if isinstance(A, (torch.Tensor, opd.DeviceMatrix)):
+            return V.to(out_dtype), lamb.to(out_dtype)
+        return K.like_input(V.to(out_dtype), A), K.like_input(lamb.to(out_dtype), A)

@@ -77,9 +77,31 @@ class DeviceMatrix:
         self.dtype = A.dtype if precision != "bf16" else torch.float32
         self._pair = None
 
+    @classmethod
+    def from_bf16(cls, hi, lo=None, symmetric=True):
+        """A bf16 operand already on the device (A ~ hi, or hi + lo for a split
+        pair).  ``symmetric``: A^T = A, so one copy serves both products."""
+        if not symmetric:
+            raise NotImplementedError("only symmetric bf16 operands")
+        dm = cls.__new__(cls)
+        dm.A = hi
+        dm.precision = "bf16"
+        dm.shape = tuple(hi.shape)
+        dm.dtype = torch.float32
+        dm._pair = (hi, hi)
+        dm.lo = lo
+        return dm
+
     @property
     def tc(self):
         return self.precision == "bf16"
+
+    @property
+    def unit_roundoff(self):
+        """Unit roundoff of the products with this operand."""
+        if self.precision == "bf16":
+            return 2.0 ** -16 if getattr(self, "lo", None) is not None else 2.0 ** -8
+        return 2.0 ** -24 if self.precision == "f32" else 2.0 ** -53
 
     def bf16_pair(self):
         if self._pair is None:
@@ -110,10 +132,23 @@ def panel_t(S):
 
 
 def tc_times(Am, S):
-    """A @ S on the tensor cores; returns an (m x l) view of l x m storage."""
+    """A @ S on the tensor cores; returns an (m x l) view of l x m storage.
+
+    For a split operand (A = hi + lo, both bf16) the sketch is split the same
+    way and hi S_hi + hi S_lo + lo S_hi are accumulated in fp32 (about 16
+    significant bits)."""
     Ab, _ = Am.bf16_pair()
-    Wt = K.convert(panel_t(S), torch.bfloat16)
-    return K.gemm_tc(Ab, Wt, out_trans=True).t()
+    St = panel_t(S)
+    Wt = K.convert(St, torch.bfloat16)
+    lo = getattr(Am, "lo", None)
+    if lo is None:
+        return K.gemm_tc(Ab, Wt, out_trans=True).t()
+    St32 = St if St.dtype == torch.float32 else St.to(torch.float32)
+    Wl = K.convert((St32 - Wt.float()).contiguous(), torch.bfloat16)
+    out = K.gemm_tc(Ab, Wt, out_trans=True)
+    K.gemm_tc(Ab, Wl, out=out, out_trans=True, beta=1.0)
+    K.gemm_tc(lo, Wt, out=out, out_trans=True, beta=1.0)
+    return out.t()
 
 
 def tc_times_t(Am, S):

@@ -190,3 +190,52 @@ def test_qb1_bf16_orthonormal_basis(pg):
     Qd = Q.double()
     assert float((Qd.t() @ Qd - torch.eye(150, dtype=torch.float64, device="cuda")).abs().max()) <= 1e-4
     assert B.shape == (150, 1500)
+
+
+def _rbf_points(N, dim, seed):
+    rng = np.random.default_rng(seed)
+    means = rng.normal(0.0, 2.0, (8, dim))
+    X = means[rng.integers(0, 8, N)] + rng.normal(0.0, 1.0, (N, dim))
+    sub = X[rng.choice(N, min(N, 512), replace=False)]
+    d2 = np.sum((sub[:, None, :] - sub[None, :, :]) ** 2, axis=-1)
+    h = np.median(np.sqrt(d2[np.triu_indices(len(sub), 1)]))
+    return X, 1.0 / (2.0 * h * h)
+
+
+def test_rbf_kernel_matrix(pg):
+    from parla_gb300 import _kernels as K
+    X, gamma = _rbf_points(300, 16, 0)
+    Kr = np.exp(-gamma * np.sum((X[:, None, :] - X[None, :, :]) ** 2, axis=-1))
+    Xd = torch.from_numpy(X.astype(np.float32)).cuda()
+    K32 = K.rbf_matrix(Xd, gamma, 0).cpu().numpy()
+    assert np.max(np.abs(K32 - Kr)) <= 1e-5
+    hi, lo = K.rbf_matrix(Xd, gamma, 2)
+    Kp = hi.float().cpu().numpy()[:, :300] + lo.float().cpu().numpy()[:, :300]
+    assert np.max(np.abs(Kp - K32)) <= 2.0 ** -16
+
+
+@pytest.mark.filterwarnings("ignore::UserWarning")
+def test_evd2_bf16_rbf_eigenvalues(pg):
+    """Nystrom EVD2 on an RBF kernel matrix with the bf16 tensor-core product
+    (split hi + lo pair) against the binary64 path of the same algorithm with
+    the same sketch (the precision effect alone); and both against binary64
+    eigvalsh (the Nystrom approximation error, the same for both)."""
+    from parla_gb300 import _kernels as K
+    from parla_gb300.utils.operand import DeviceMatrix
+    N, k, over = 2048, 64, 16
+    X, gamma = _rbf_points(N, 16, 1)
+    Xd = torch.from_numpy(X.astype(np.float32)).cuda()
+    K64 = torch.exp(-gamma * torch.cdist(Xd.double(), Xd.double()) ** 2)
+    lam_ref = np.sort(torch.linalg.eigvalsh(K64).cpu().numpy())[::-1]
+    hi, lo = K.rbf_matrix(Xd, gamma, 2)
+    V, lam = pg.EVD2(pg.RS1(pg.SkOpGA(), 0))(DeviceMatrix.from_bf16(hi, lo), k, np.nan, over, 3)
+    V64, lam64 = pg.EVD2(pg.RS1(pg.SkOpGA(), 0))(K64, k, np.nan, over, 3)
+    lam, lam64 = lam.double().cpu().numpy(), lam64.cpu().numpy()
+    r = min(lam.size, lam64.size)
+    assert r >= 32
+    top = slice(0, 32)
+    assert np.max(np.abs(lam[top] - lam64[top]) / lam64[top]) <= 1e-3
+    # Nystrom underestimates: both lie below the exact eigenvalues
+    assert np.all(lam64[top] <= lam_ref[top] * (1 + 1e-9))
+    Vd = V.double()
+    assert float((Vd.t() @ Vd - torch.eye(lam.size, dtype=torch.float64, device="cuda")).abs().max()) <= 1e-4
