@@ -2,7 +2,7 @@
 
 TEST INFRASTRUCTURE ONLY.  This package is a NumPy/SciPy restatement of the
 reference algorithms (sketching operators, LSQR, sketch-and-precondition least
-squares, the RS1 -> RF1 -> QB1 -> SVD1 chain and the EVD1/EVD2 eigensolvers).
+squares, the RS1 -> RF1 -> QB1/QB2/QB3 -> SVD1 chain and the EVD1/EVD2 eigensolvers).
 Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
 ``bench.py`` may import it, and only as the checker or as the timed CPU
 baseline.  The GPU product in ``parla_gb300`` never imports it.
@@ -20,11 +20,11 @@ from oracle.sketching import (gaussian_operator, sjlt_operator, generate_srct,
 from oracle.lsqr import lsqr
 from oracle.least_squares import (dim_checks, spo, sso1, pcss2,
                                   svd_right_precond, SketchAndPrecondLog)
-from oracle.lowrank import orth, rs1, rf1, qb1, svd1, evd1, evd2
+from oracle.lowrank import orth, rs1, rf1, qb1, qb2, qb3, svd1, evd1, evd2
 
 __all__ = [
     "gaussian_operator", "sjlt_operator", "generate_srct", "apply_srct",
     "srct_apply_dense", "orthonormal_operator", "lsqr", "dim_checks", "spo",
     "sso1", "pcss2", "svd_right_precond", "SketchAndPrecondLog", "orth", "rs1",
-    "rf1", "qb1", "svd1", "evd1", "evd2",
+    "rf1", "qb1", "qb2", "qb3", "svd1", "evd1", "evd2",
 ]

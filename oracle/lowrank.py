@@ -67,6 +67,83 @@ def qb1(A, k, tol, rng, rangefinder):
     return Q, Q.T @ A
 
 
+def project_out(Qi, Q):
+    """Qi - Q Q' Qi (``parla/comps/qb.py:603-613``)."""
+    return Qi - Q @ (Q.T @ Qi)
+
+
+def qb2(A, k, tol, rng, rangefinder, blk):
+    """Blocked QB with deflation and a Frobenius tolerance (``parla/comps/qb.py:373-482``).
+
+    Each block: Qi from the rangefinder on the deflated A, projected against
+    the current Q and re-orthonormalised, Bi = Qi' A, A -= Qi Bi; stop when k
+    columns are reached or ||A - Q B||_F^2 (tracked as ||A||^2 - sum ||Bi||^2)
+    falls below tol^2 ||A||_F^2.
+    """
+    A = np.array(A, dtype=float, copy=True)
+    k = min(k, min(A.shape))
+    use_tol = not np.isnan(tol) and tol > 0
+    if use_tol:
+        sq = la.norm(A, 'fro') ** 2
+        abs_sq_tol = sq * tol ** 2
+    gen = np.random.default_rng(rng)
+    Q = np.empty((A.shape[0], 0))
+    B = np.empty((0, A.shape[1]))
+    b = blk
+    while True:
+        if B.shape[0] + b > k:
+            b = k - B.shape[0]
+        Qi = rangefinder(A, b, np.nan, gen)
+        Qi = project_out(Qi, Q)
+        Qi = la.qr(Qi, mode='economic')[0]
+        Bi = Qi.T @ A
+        Q = np.column_stack((Q, Qi))
+        B = np.vstack((B, Bi))
+        A -= Qi @ Bi
+        if use_tol:
+            sq = sq - la.norm(Bi, 'fro') ** 2
+            if sq <= abs_sq_tol:
+                break
+        if B.shape[0] >= k:
+            break
+    return Q, B
+
+
+def qb3(A, k, tol, rng, row_sketcher, blk):
+    """Single-sketch blocked QB (``parla/comps/qb.py:485-595``): G = A S, H = A' G,
+    then per block Yi = G_i - Q (B S_i), two QR steps, Bi from H_i by a
+    triangular solve."""
+    assert 0 < k < min(A.shape)
+    use_tol = not np.isnan(tol) and tol > 0
+    if use_tol:
+        sq = la.norm(A, 'fro') ** 2
+        abs_sq_tol = sq * tol ** 2
+    gen = np.random.default_rng(rng)
+    Q = np.empty((A.shape[0], 0))
+    B = np.empty((0, A.shape[1]))
+    S = row_sketcher(A, k, gen)
+    G = A @ S
+    H = A.T @ G
+    for i in range(int(np.ceil(k / blk))):
+        s0, s1 = i * blk, min((i + 1) * blk, k)
+        Si = S[:, s0:s1]
+        BSi = B @ Si
+        Yi = G[:, s0:s1] - Q @ BSi
+        Qi, Ri = la.qr(Yi, mode='economic')
+        Qi = project_out(Qi, Q)
+        Qi, Rh = la.qr(Qi, mode='economic')
+        Ri = Rh @ Ri
+        Bi = H[:, s0:s1].T - (Yi.T @ Q) @ B - BSi.T @ B
+        Bi = la.solve_triangular(Ri, Bi, trans='T')
+        Q = np.column_stack((Q, Qi))
+        B = np.vstack((B, Bi))
+        if use_tol:
+            sq = sq - la.norm(Bi, 'fro') ** 2
+            if sq <= abs_sq_tol:
+                break
+    return Q, B
+
+
 def svd1(A, k, tol, over, rng, qb):
     """Randomized SVD driver (``parla/drivers/svd.py:161-176``).
 

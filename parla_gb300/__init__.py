@@ -1,7 +1,7 @@
 """parla_gb300: the randomized-linear-algebra hot path of PARLA on NVIDIA GB300.
 
 Same names and call signatures as the reference package (``parla/__init__.py``):
-sketch generators (SkOpGA, SkOpSJ, SkOpTC), RS1, RF1, QB1, SVD1, EVD1,
+sketch generators (SkOpGA, SkOpSJ, SkOpTC), RS1, RF1, QB1, QB2, QB3, SVD1, EVD1,
 EVD2, SPO and SSO1.  Products, factorizations and LSQR run in the CUDA
 kernels of ``librla_gb300.so`` (C ABI in ``include/rla_gb300.h``).
 """
@@ -13,7 +13,7 @@ from .utils.sketching import (gaussian_operator, sjlt_operator, srct_operator, g
 from .comps.sketchers.oblivious import SketchOpGen, SkOpGA, SkOpSJ, SkOpTC
 from .comps.sketchers.aware import RowSketcher, RS1
 from .comps.rangefinders import RangeFinder, RF1
-from .comps.qb import QBDecomposer, QB1
+from .comps.qb import QBDecomposer, QB1, QB2, QB3
 from .comps.determiter.logging import SketchAndPrecondLog
 from .comps.determiter.saddle import PrecondSaddleSolver, PcSS2
 from .comps.determiter.lsqr import lsqr, PrecondOperator

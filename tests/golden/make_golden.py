@@ -128,7 +128,7 @@ def lowrank_cases(parla):
     import parla.comps.sketchers.oblivious as sko
     from parla.comps.sketchers.aware import RS1
     from parla.comps.rangefinders import RF1
-    from parla.comps.qb import QB1
+    from parla.comps.qb import QB1, QB2, QB3
     from parla.drivers.svd import SVD1
     from parla.drivers.evd import EVD1, EVD2
     import parla.utils.linalg_wrappers as law
@@ -152,6 +152,13 @@ def lowrank_cases(parla):
     out['qb1_Q'], out['qb1_B'] = qb(A, 12, np.nan, np.random.default_rng(71))
     with warnings.catch_warnings():
         warnings.simplefilter('ignore')
+        rf0 = RF1(RS1(sko.SkOpGA(), 2, law.orth, 1))
+        out['qb2_Q'], out['qb2_B'] = QB2(rf0, 5, False)(A, 17, 0.0, np.random.default_rng(76))
+        out['qb2t_Q'], out['qb2t_B'] = QB2(rf0, 4, False)(A, 40, 0.05, np.random.default_rng(77))
+        out['qb3_Q'], out['qb3_B'] = QB3(RS1(sko.SkOpGA(), 2, law.orth, 1), 5)(A, 17, 0.0,
+                                                                            np.random.default_rng(78))
+        out['qb3t_Q'], out['qb3t_B'] = QB3(RS1(sko.SkOpGA(), 2, law.orth, 1), 4)(A, 40, 0.05,
+                                                                             np.random.default_rng(79))
         U1, s1, Vh1 = SVD1(qb)(A, 10, np.nan, 5, np.random.default_rng(72))
     out['svd1_U'], out['svd1_s'], out['svd1_Vh'] = U1, s1, Vh1
     # symmetric and PSD inputs for the eigensolvers

@@ -134,6 +134,31 @@ def test_qb1_svd1_match_oracle(pg, golden):
 
 
 @pytest.mark.filterwarnings("ignore::UserWarning")
+def test_qb2_qb3_match_reference(pg, golden):
+    """Blocked QB with and without a tolerance, operators drawn as the reference draws them."""
+    g = golden("lowrank")
+    A = g["A"]
+    gen = pg.SkOpGA(seed_compat=True)
+    for tag, k, tol, blk, seed in (("qb2", 17, 0.0, 5, 76), ("qb2t", 40, 0.05, 4, 77)):
+        Q, B = pg.QB2(pg.RF1(pg.RS1(gen, 2)), blk)(A, k, tol, seed)
+        Qr, Br = g[f"{tag}_Q"], g[f"{tag}_B"]
+        assert Q.shape == Qr.shape
+        assert np.allclose(np.abs(Q.T @ Qr), np.eye(Q.shape[1]), atol=1e-7)
+        assert np.linalg.norm(Q @ B - Qr @ Br) <= 1e-9 * np.linalg.norm(A)
+    for tag, k, tol, blk, seed in (("qb3", 17, 0.0, 5, 78), ("qb3t", 40, 0.05, 4, 79)):
+        Q, B = pg.QB3(pg.RS1(gen, 2), blk)(A, k, tol, seed)
+        Qr, Br = g[f"{tag}_Q"], g[f"{tag}_B"]
+        assert Q.shape == Qr.shape
+        assert np.allclose(np.abs(Q.T @ Qr), np.eye(Q.shape[1]), atol=1e-6)
+        assert np.linalg.norm(Q @ B - Qr @ Br) <= 1e-8 * np.linalg.norm(A)
+    # fixed-rank QB2 on a device tensor leaves the input alone
+    Ad = torch.from_numpy(A).cuda()
+    A0 = Ad.clone()
+    pg.QB2(pg.RF1(pg.RS1(pg.SkOpGA(), 2)), 6)(Ad, 12, 0.0, 3)
+    assert torch.equal(Ad, A0)
+
+
+@pytest.mark.filterwarnings("ignore::UserWarning")
 def test_evd1_evd2_match_oracle(pg, golden):
     g = golden("lowrank")
     gen = pg.SkOpGA(seed_compat=True)

@@ -155,6 +155,27 @@ def test_rf1_qb1_svd1(golden):
 
 
 @pytest.mark.filterwarnings("ignore::UserWarning")
+def test_qb2_qb3(golden):
+    """Blocked QB (fixed rank and with a Frobenius tolerance) against the reference."""
+    g = golden("lowrank")
+    A = g["A"]
+    rso, rf, _ = _chain()
+    for tag, k, tol, blk, seed in (("qb2", 17, 0.0, 5, 76), ("qb2t", 40, 0.05, 4, 77)):
+        Q, B = olr.qb2(A, k, tol, np.random.default_rng(seed), rf, blk)
+        assert Q.shape == g[f"{tag}_Q"].shape
+        close(Q, g[f"{tag}_Q"], 1e-9)
+        close(B, g[f"{tag}_B"], 1e-9)
+    for tag, k, tol, blk, seed in (("qb3", 17, 0.0, 5, 78), ("qb3t", 40, 0.05, 4, 79)):
+        Q, B = olr.qb3(A, k, tol, np.random.default_rng(seed), rso, blk)
+        assert Q.shape == g[f"{tag}_Q"].shape
+        close(Q, g[f"{tag}_Q"], 1e-8)
+        close(B, g[f"{tag}_B"], 1e-8)
+    # the tolerance runs stop early with the requested accuracy
+    Q, B = olr.qb2(A, 40, 0.05, np.random.default_rng(77), rf, 4)
+    assert Q.shape[1] < 40 and np.linalg.norm(A - Q @ B) <= 0.05 * np.linalg.norm(A) * (1 + 1e-9)
+
+
+@pytest.mark.filterwarnings("ignore::UserWarning")
 def test_evd1_evd2(golden):
     g = golden("lowrank")
     _, _, qb = _chain()
