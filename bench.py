@@ -103,13 +103,23 @@ def chain(pg, precision="bf16"):
     return pg.SVD1(pg.QB1(pg.RF1(pg.RS1(pg.SkOpGA(), NUM_PASS))), precision=precision)
 
 
+def _dist():
+    """(rank, world, dist module or None) of a torchrun launch."""
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world <= 1:
+        return 0, 1, None
+    import torch.distributed as dist
+    return dist.get_rank(), world, dist
+
+
 def run_ours(args):
     import torch
     import parla_gb300 as pg
     from parla_gb300 import _kernels as K
     import __graft_entry__
     __graft_entry__.build()
-    torch.cuda.set_device(0)
+    rank, world, dist = _dist()
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     A, s = make_problem(torch)
     tail = float(np.sqrt(np.sum(s[K_RANK:] ** 2)))
     svd = chain(pg)
@@ -123,15 +133,24 @@ def run_ours(args):
     K.STATS.reset()
     K.STATS.timing = True
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler() as clk:
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        if dist is not None:
+            dist.barrier()
         torch.cuda.synchronize()
         e0.record(stream)
         for it in range(args.steps):
             U, sv, Vh = svd(A, K_RANK, np.nan, OVER, 2000 + it)
         e1.record(stream)
         torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
     K.STATS.timing = False
     total_ms = e0.elapsed_time(e1)
+    if dist is not None:
+        # replicas: every rank runs the same workload; the job takes the slowest
+        t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
     launches = K.STATS.launches
     per_kernel = {}
     for name, s_ev, e_ev in K.STATS.events:
@@ -160,6 +179,12 @@ def run_ours(args):
     t1.record(stream)
     torch.cuda.synchronize()
     e2e_ms = t0.elapsed_time(t1)
+    if dist is not None:
+        t = torch.tensor([e2e_ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+        if rank != 0:
+            return
 
     hbm, bf16, src = peaks()
     # dominant kernel: the tensor-core passes over A (six per step).  Algorithmic
@@ -190,25 +215,26 @@ def run_ours(args):
 
     line = {
         "metric": METRIC,
-        "value": args.steps / (total_ms * 1e-3),
+        "value": world * args.steps / (total_ms * 1e-3),
         "unit": "rsvd/s",
-        "n_gpus": 1,
+        "n_gpus": world,
         "steps": args.steps,
         "warmup": args.warmup,
         "ms_per_step": total_ms / args.steps,
         "higher_is_better": True,
-        "scaling": "replicas",
+        "scaling": "weak",
         "vs_baseline": None,
         "dtype": "bf16 tensor-core products, fp32 accumulation and factorizations",
         "data": "synthetic (seeded Haar U, V; s_i = i^-1.5 + 1e-4)",
         "config": {"workload": "SVD1(QB1(RF1(RS1(SkOpGA, num_pass=4)))) on A 16384x8192 fp32, k=200, over=10",
-                   "global_batch": 1, "seq_len": 0, "parallelism": "single GPU",
+                   "global_batch": world, "seq_len": 0,
+                   "parallelism": "single GPU" if world == 1 else f"{world} independent replicas (one RSVD per GPU)",
                    "l2": "inputs larger than L2 (A = 537 MB)",
                    "path": "tcgen05 bf16 passes (fp32 accumulate), tensor-core CholeskyQR stabilizer"},
         "error": {"frob_err": err, "optimal_tail": tail, "ratio": err / tail,
                   "plain_fp32_ratio": err_plain / tail},
         "plain_fp32_gpu": {"ms_per_step": plain_ms, "speedup": plain_ms / (total_ms / args.steps)},
-        "e2e": {"value": args.steps / (e2e_ms * 1e-3), "unit": "rsvd/s", "h2d_bytes_per_step": h2d,
+        "e2e": {"value": world * args.steps / (e2e_ms * 1e-3), "unit": "rsvd/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "roofline": {"kernel": "gemm_tc_kernel (RSVD pass)", "bound": "hbm", "achieved": achieved, "peak": hbm,
                      "unit": "GB/s", "frac": achieved / hbm, "peak_source": src, "traffic": None,
@@ -222,6 +248,9 @@ def run_ours(args):
         line["cpu_baseline"] = cpu_baseline(A.cpu().numpy(), budget_s=args.cpu_budget)
     del A, Ad_, A_host
     torch.cuda.empty_cache()
+    if world > 1:  # the side measurements are single-GPU workloads
+        print(json.dumps(line))
+        return
     line["sketch_apply"] = bench_sketch_apply(torch)
     if args.nystrom:
         line["nystrom_evd2"] = bench_nystrom(torch, pg)
@@ -505,7 +534,7 @@ def run_reference(args):
     line = {
         "metric": METRIC, "value": cb["value"], "unit": "rsvd/s", "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 / cb["value"], "higher_is_better": True,
-        "scaling": "replicas", "vs_baseline": None, "dtype": "f64 (reference promotes f32 input)",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64 (reference promotes f32 input)",
         "data": "synthetic (seeded Haar U, V; s_i = i^-1.5 + 1e-4)", "impl": "reference",
         "config": {"workload": "SVD1(QB1(RF1(RS1(SkOpGA, num_pass=4)))) on A 16384x8192 fp32, k=200, over=10",
                    "global_batch": 1, "seq_len": 0, "parallelism": "host cores"},
@@ -546,12 +575,38 @@ def run_case(args):
         rows, signs = K.sjlt_pattern(d, m, 8, 1)
         for _ in range(3):
             K.sjlt_apply(rows, signs, 8, d, A, 8 ** -0.5)
+    elif args.case == "small":
+        # the small dense kernels of one RSVD step at l = 210
+        C = torch.randn((210, 210), generator=g, device="cuda")
+        G = (C.double() @ C.double().t()).contiguous()
+        G32 = G.float().contiguous()
+        for _ in range(3):
+            K.chol_inv_f32(G32)
+            R = K.potrf_df_small(G)
+            K.svd_jacobi(R)
+    elif args.case == "learned":
+        # one training step and one sketch of the learned SJLT, 8 matrices of 4096 columns
+        from parla_gb300.learned.sketch import SJLTPattern
+        n, d, Kt, B = 4096, 74, 128, 8
+        pat = SJLTPattern(d, n, 1234)
+        F = torch.randn((B * n, 4), generator=g, device="cuda")
+        X = torch.randn((B, n, Kt), generator=g, device="cuda")
+        sig = torch.exp(-torch.arange(Kt, device="cuda", dtype=torch.float32) / 40.0).repeat(B, 1).contiguous()
+        P = torch.zeros(840, device="cuda")
+        A = torch.randn((16384, n), generator=g, device="cuda")
+        for _ in range(3):
+            vals, H = K.mlp_fwd(F, P, pat.signs, n, want_hidden=True)
+            W = pat.left(vals.view(B, n, 8), X)
+            loss, dW = K.lsk_loss(W, sig, 64)
+            dO = K.lsk_value_grad(pat.rows, vals, X, dW)
+            K.mlp_bwd(F, H, dO, P, 1.0 / B)
+            pat.right(A, vals[:n])
     torch.cuda.synchronize()
 
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--case", default=None, choices=["tc_pass", "sjlt", "sjlt32", "lsqr"],
+    ap.add_argument("--case", default=None, choices=["tc_pass", "sjlt", "sjlt32", "lsqr", "small", "learned"],
                     help="run one small kernel case for a profiler capture and exit")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
@@ -580,11 +635,14 @@ def main():
     if world > 1:
         import torch
         import torch.distributed as dist
-        dist.init_process_group("nccl")
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl")
         if rank != 0:
             args.cpu_baseline = False
     run_ours(args)
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
 
 
 if __name__ == "__main__":

@@ -405,3 +405,14 @@ def batch_shapes(count, seed, m_lo=2048, m_hi=65536, n_lo=16, n_hi=512, ratio=16
         kappa = float(math.exp(rng.uniform(math.log(kappa_lo), math.log(kappa_hi))))
         out.append((m, n, kappa))
     return out
+
+
+def shard_indices(count, rank, world):
+    """Problems of this rank when a batch is split over ``world`` GPUs.
+
+    Independent problems need no collective: rank r takes every world-th
+    problem starting at r (interleaved, so sizes balance across ranks).
+    """
+    if world < 1 or not 0 <= rank < world:
+        raise ValueError("rank must lie in [0, world)")
+    return list(range(rank, count, world))

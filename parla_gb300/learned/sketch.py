@@ -153,6 +153,8 @@ class LearnedQB(QBDecomposer):
     def __call__(self, A, k, tol, rng):
         assert k > K_PRE
         rng = np.random.default_rng(rng)
+        if isinstance(A, opd.DeviceMatrix):
+            A = A.A
         Ad = K.to_dev(A, torch.float32) if not isinstance(A, torch.Tensor) else A
         Ad = Ad if Ad.dtype == torch.float32 else Ad.to(torch.float32)
         Ad = Ad.contiguous()

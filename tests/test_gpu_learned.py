@@ -192,3 +192,17 @@ def test_fallback_guard(env):
     err = float(torch.linalg.matrix_norm(A.double() - Q.double() @ B.double()))
     Om = K.gaussian_fill(512, d, 3, 1.0, torch.float32)
     assert err <= 1.5 * T.range_error(A, K.gemm(A, Om, mode="f32"))
+
+
+def test_svd1_over_learned_qb(env):
+    """The guarded learned QB plugs into SVD1 like any QBDecomposer."""
+    K, L = env
+    import parla_gb300 as pg
+    A, _ = L.family_matrix(4242, m=1024, n=1024, rank_range=(64, 96))
+    net = L.SketchNet(np.zeros(OL.N_PARAMS, dtype=np.float32))
+    U, s, Vh = pg.SVD1(L.LearnedQB(net))(A, 40, np.nan, 10, 5)
+    assert U.shape == (1024, 40) and Vh.shape == (40, 1024)
+    err = float(torch.linalg.matrix_norm(A.double() - (U.double() * s.double()) @ Vh.double()))
+    Up, sp, Vhp = pg.SVD1(pg.QB1(pg.RF1(pg.RS1(pg.SkOpGA(), 0))), precision="f32")(A, 40, np.nan, 10, 5)
+    errp = float(torch.linalg.matrix_norm(A.double() - (Up.double() * sp.double()) @ Vhp.double()))
+    assert err <= 1.2 * errp
