@@ -218,28 +218,51 @@ __device__ __forceinline__ void lsqr_body(const LsqrArgs& a, const int G, const 
     V part = R::zero();
     const V vca = R::from_d(ca), vcu = R::from_d(cu);
     int cnt = 0;
-    for (int64_t i = r0 + warp; i < r1; i += nw) {
-      V av[NPL > 0 ? NPL : 1];
+    // software pipelined over the warp's rows (n <= 256): the next row's
+    // elements are loaded while the current one is reduced, so two rows per
+    // warp are in flight (one row at a time left the pass latency-bound);
+    // wider rows keep one row in flight to stay within the register budget
+    constexpr int NP = NPL > 0 ? NPL : 1;
+    constexpr bool kPrefetch = NPL <= 8;
+    auto load_row = [&](int64_t i, V (&dst)[NP]) {
+#pragma unroll
+      for (int q = 0; q < NP; ++q) {
+        const int64_t j = lane + 32 * q;
+        dst[q] = j < a.n ? Elem<V>::ld(a, i, j) : R::zero();
+      }
+    };
+    V cur[NP], nxt[NP];
+    int64_t i = r0 + warp;
+    if (i < r1) load_row(i, cur);
+    for (; i < r1; i += nw) {
+      const int64_t inext = i + nw;
+      if (kPrefetch && inext < r1) load_row(inext, nxt);
+      const V uold = with_b ? R::ld(a.b + i) : R::ldcg(a.u + i);
       V dot = R::zero();
 #pragma unroll
-      for (int q = 0; q < (NPL > 0 ? NPL : 1); ++q) {
+      for (int q = 0; q < NP; ++q) {
         const int64_t j = lane + 32 * q;
-        av[q] = j < a.n ? Elem<V>::ld(a, i, j) : R::zero();
-        if (j < a.n) Elem<V>::mac(dot, av[q], xs[j]);
+        if (j < a.n) Elem<V>::mac(dot, cur[q], xs[j]);
       }
       Elem<V>::renorm(dot);
       dot = R::wsum(dot);
-      V ui = with_b ? R::ld(a.b + i) : R::mul(vcu, R::ldcg(a.u + i));
+      V ui = with_b ? uold : R::mul(vcu, uold);
       ui = R::add(ui, R::mul(vca, dot));
       if (lane == 0) {
         R::st(a.u + i, ui);
         part = R::fma(part, ui, ui);
       }
 #pragma unroll
-      for (int q = 0; q < (NPL > 0 ? NPL : 1); ++q) Elem<V>::mac(acc[q], av[q], ui);
+      for (int q = 0; q < NP; ++q) Elem<V>::mac(acc[q], cur[q], ui);
       if ((++cnt & 15) == 0) {
 #pragma unroll
-        for (int q = 0; q < (NPL > 0 ? NPL : 1); ++q) Elem<V>::renorm(acc[q]);
+        for (int q = 0; q < NP; ++q) Elem<V>::renorm(acc[q]);
+      }
+      if (kPrefetch) {
+#pragma unroll
+        for (int q = 0; q < NP; ++q) cur[q] = nxt[q];
+      } else if (inext < r1) {
+        load_row(inext, cur);
       }
     }
     if (ext && blk == 0) {
@@ -479,26 +502,23 @@ __device__ __forceinline__ void lsqr_dispatch(const LsqrArgs& a, int G, int blk,
 }
 
 // NPL = columns per lane of the fused one-pass products (n <= 32 NPL);
-// 0 selects the two-pass form for wide problems.
-template <class P>
-__device__ __forceinline__ void lsqr_run_any(const LsqrArgs& a, int G, int blk, unsigned char* smem, bool coop) {
-  if (a.n <= 64) lsqr_dispatch<P, 2>(a, G, blk, smem, coop);
-  else if (a.n <= 128) lsqr_dispatch<P, 4>(a, G, blk, smem, coop);
-  else if (a.n <= 256) lsqr_dispatch<P, 8>(a, G, blk, smem, coop);
-  else if (a.n <= 512) lsqr_dispatch<P, 16>(a, G, blk, smem, coop);
-  else lsqr_dispatch<P, 0>(a, G, blk, smem, coop);
+// 0 selects the two-pass form for wide problems.  Each width class is its
+// own kernel instantiation (its own register allocation), chosen on the host.
+__host__ __device__ inline int lsqr_npl(int64_t n) {
+  return n <= 64 ? 2 : n <= 128 ? 4 : n <= 256 ? 8 : n <= 512 ? 16 : 0;
 }
 
-template <class P>
-__global__ void __launch_bounds__(kLsqrThreads) lsqr_kernel(LsqrArgs a) {
+template <class P, int NPL>
+__global__ void __launch_bounds__(kLsqrThreads, 2) lsqr_kernel(LsqrArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  lsqr_run_any<P>(a, static_cast<int>(gridDim.x), static_cast<int>(blockIdx.x), smem_raw, true);
+  lsqr_dispatch<P, NPL>(a, static_cast<int>(gridDim.x), static_cast<int>(blockIdx.x), smem_raw, true);
 }
 
 // Persistent batched form: each CTA takes the next problem (largest first,
-// `order`) from an atomic queue and solves it alone.
-template <class P>
-__global__ void __launch_bounds__(kLsqrThreads) lsqr_batched_kernel(const LsqrArgs* __restrict__ probs,
+// `order`) from an atomic queue and solves it alone.  All problems of one
+// launch must satisfy lsqr_npl(n) <= NPL (the launcher picks NPL from nmax).
+template <class P, int NPL>
+__global__ void __launch_bounds__(kLsqrThreads, 2) lsqr_batched_kernel(const LsqrArgs* __restrict__ probs,
                                                                      const int* __restrict__ order, int nprob,
                                                                      int* __restrict__ next) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -510,8 +530,29 @@ __global__ void __launch_bounds__(kLsqrThreads) lsqr_batched_kernel(const LsqrAr
     __syncthreads();
     if (i >= nprob) return;
     const LsqrArgs a = probs[order[i]];
-    lsqr_run_any<P>(a, 1, 0, smem_raw, false);
+    lsqr_dispatch<P, NPL>(a, 1, 0, smem_raw, false);
     __syncthreads();
+  }
+}
+
+template <class P>
+const void* lsqr_kernel_fn(int npl) {
+  switch (npl) {
+    case 2: return reinterpret_cast<const void*>(lsqr_kernel<P, 2>);
+    case 4: return reinterpret_cast<const void*>(lsqr_kernel<P, 4>);
+    case 8: return reinterpret_cast<const void*>(lsqr_kernel<P, 8>);
+    case 16: return reinterpret_cast<const void*>(lsqr_kernel<P, 16>);
+    default: return reinterpret_cast<const void*>(lsqr_kernel<P, 0>);
+  }
+}
+template <class P>
+const void* lsqr_batched_fn(int npl) {
+  switch (npl) {
+    case 2: return reinterpret_cast<const void*>(lsqr_batched_kernel<P, 2>);
+    case 4: return reinterpret_cast<const void*>(lsqr_batched_kernel<P, 4>);
+    case 8: return reinterpret_cast<const void*>(lsqr_batched_kernel<P, 8>);
+    case 16: return reinterpret_cast<const void*>(lsqr_batched_kernel<P, 16>);
+    default: return reinterpret_cast<const void*>(lsqr_batched_kernel<P, 0>);
   }
 }
 
@@ -552,9 +593,9 @@ int lsqr_grid(int64_t n, size_t* smem_out) {
   size_t smem = lsqr_smem_bytes(n, sizeof(typename P::V));
   *smem_out = smem;
   int per_sm = 0;
-  if (smem > 48 * 1024)
-    cudaFuncSetAttribute(lsqr_kernel<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lsqr_kernel<P>, kLsqrThreads, smem);
+  const void* fn = lsqr_kernel_fn<P>(lsqr_npl(n));
+  if (smem > 48 * 1024) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kLsqrThreads, smem);
   return max(1, min(per_sm, 2)) * sm_count();
 }
 
@@ -605,10 +646,10 @@ int lsqr_enqueue(int dtype, int64_t m, int64_t n, int64_t p, const double* A, co
   unsigned* barw = reinterpret_cast<unsigned*>(base + L.bar);
   a.bar = GridBar{barw, barw + 1, out + 2};
   void* args[] = {&a};
-  void* fn = nullptr;
-  if (dtype == RLA_DF) fn = reinterpret_cast<void*>(lsqr_kernel<Ar<df>>);
-  else if (dtype == RLA_F64) fn = reinterpret_cast<void*>(lsqr_kernel<Ar<double>>);
-  else if (dtype == RLA_F32) fn = reinterpret_cast<void*>(lsqr_kernel<ArF32D>);
+  const void* fn = nullptr;
+  if (dtype == RLA_DF) fn = lsqr_kernel_fn<Ar<df>>(lsqr_npl(n));
+  else if (dtype == RLA_F64) fn = lsqr_kernel_fn<Ar<double>>(lsqr_npl(n));
+  else if (dtype == RLA_F32) fn = lsqr_kernel_fn<ArF32D>(lsqr_npl(n));
   else return RLA_ERR_ARG;
   RLA_CUDA_TRY(cudaLaunchCooperativeKernel(fn, dim3(G), dim3(kLsqrThreads), args, smem, st));
   return RLA_OK;
@@ -710,14 +751,15 @@ int lsqr_batched_launch(const LsqrArgs* d_args, const int* d_order, int nprob, i
                         cudaStream_t st) {
   size_t smem = lsqr_smem_bytes(nmax, sizeof(typename P::V));
   if (smem > 200 * 1024) return RLA_ERR_UNSUPPORTED;
+  const void* fn = lsqr_batched_fn<P>(lsqr_npl(nmax));
   if (smem > 48 * 1024)
-    RLA_CUDA_TRY(cudaFuncSetAttribute(lsqr_batched_kernel<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      static_cast<int>(smem)));
+    RLA_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
   int per_sm = 0;
-  RLA_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lsqr_batched_kernel<P>, kLsqrThreads, smem));
+  RLA_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kLsqrThreads, smem));
   int grid = static_cast<int>(imin(nprob, static_cast<int64_t>(imax(per_sm, 1)) * sm_count()));
   RLA_CUDA_TRY(cudaMemsetAsync(d_next, 0, sizeof(int), st));
-  lsqr_batched_kernel<P><<<grid, kLsqrThreads, smem, st>>>(d_args, d_order, nprob, d_next);
+  void* args[] = {const_cast<LsqrArgs**>(&d_args), const_cast<int**>(&d_order), &nprob, &d_next};
+  RLA_CUDA_TRY(cudaLaunchKernel(fn, dim3(grid), dim3(kLsqrThreads), args, smem, st));
   RLA_LAUNCH_CHECK();
   return RLA_OK;
 }

@@ -196,9 +196,16 @@ class BatchedSPO:
                       K.ptr(it["Rinv"]), n, 0.0, K.ptr(b), K.ptr(it["z"]), 1, 0.0, 0.0, 0.0, float(self.ptol),
                       int(self.iter_lim), 0, K.ptr(it["out"]), K.ptr(it["arn"]), K.ptr(it["coop_ws"]),
                       C.byref(C.c_size_t(it["coop_ws"].numel())), K.stream())
-        if plan["n_ls_small"]:
-            _lib.call("rla_lsqr_batched", K.MODES["df"], K.ptr(plan["ls_dev"]), K.ptr(plan["ls_order_dev"]),
-                      plan["n_ls_small"], plan["nmax"], K.ptr(plan["next2"]), K.stream())
+        # one persistent launch per width class (each class is its own kernel
+        # instantiation and register budget), side by side on the streams
+        for j, (ordt, cnt, nmx, nxt) in enumerate(plan["ls_classes"]):
+            s = streams[j % self.nstreams]
+            s.wait_stream(main)
+            with torch.cuda.stream(s):
+                _lib.call("rla_lsqr_batched", K.MODES["df"], K.ptr(plan["ls_dev"]), K.ptr(ordt), cnt, nmx,
+                          K.ptr(nxt), K.stream())
+        for s in streams:
+            main.wait_stream(s)
         # x = R^-1 z is written by the LSQR kernels themselves; the large
         # problems' cooperative launches compute it here
         for i in plan["ls_big"]:
@@ -257,6 +264,18 @@ class BatchedSPO:
         plan["order_dev"] = torch.tensor(order + [0], dtype=torch.int32, device=dev)
         plan["qr_order_dev"] = torch.tensor(qr_small + [0], dtype=torch.int32, device=dev)
         plan["ls_order_dev"] = torch.tensor(ls_small + [0], dtype=torch.int32, device=dev)
+        # width classes of the LSQR kernels (columns per lane 2 / 4 / 8 / 16 / two-pass)
+        bounds = (64, 128, 256, 512, None)
+        classes = []
+        lo = 0
+        for hi in bounds:
+            members = [i for i in ls_small if items[i]["n"] > lo and (hi is None or items[i]["n"] <= hi)]
+            if members:
+                nmx = max(items[i]["n"] for i in members)
+                classes.append((torch.tensor(members + [0], dtype=torch.int32, device=dev), len(members), nmx,
+                                torch.zeros(1, dtype=torch.int32, device=dev)))
+            lo = hi if hi is not None else lo
+        plan["ls_classes"] = classes
         plan["next"] = torch.zeros(1, dtype=torch.int32, device=dev)
         plan["next2"] = torch.zeros(1, dtype=torch.int32, device=dev)
         return plan
