@@ -162,6 +162,9 @@ class BatchedSPO:
                           K.ptr(it["lo"]), it["n"], K.stream())
                 rows, signs = K.sjlt_pattern(it["d"], it["m"], it["nnz"], it["seed"])
                 scale = 1.0 / math.sqrt(it["nnz"])
+                # exact (fixed-point) sketch of the binary64 A: with condition
+                # numbers beyond 1/eps_fp32 a binary32 sketch would spoil the
+                # preconditioner's smallest directions
                 Ask = K.sjlt_apply(rows, signs, it["nnz"], it["d"], A, scale)
                 bsk = K.sjlt_apply(rows, signs, it["nnz"], it["d"], b, scale)
                 it["T"][: it["n"]].copy_(Ask.t())
