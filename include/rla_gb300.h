@@ -303,8 +303,12 @@ int rla_lsqr_record(void* rec, int64_t m, int64_t n, int64_t p,
                     double atol, double btol, double conlim, double ptol,
                     int iter_lim, int* out, double* arnorms, double* x,
                     void* ws);
+/* One thread-block cluster of `cluster` CTAs (1..8) per problem, largest
+ * first by `order`; at most max_ctas CTAs resident (0: all that fit), so that
+ * launches of several width classes can share the device side by side. */
 int rla_lsqr_batched(int dtype, const void* probs, const int* order,
-                     int nprob, int64_t nmax, int* next, rla_stream_t stream);
+                     int nprob, int64_t nmax, int cluster, int max_ctas,
+                     int* next, rla_stream_t stream);
 
 /* r = b - A x (m rows) in double-float from the hi/lo planes of A
  * (rla_split_f64): the FP64-class residual of the refinement loop, replacing

@@ -56,7 +56,7 @@ SIGNATURES = {
     "rla_geqrf_batched": [_i32, _p, _p, _i32, _p, _p],
     "rla_geqrf_hl_batched": [_p, _p, _i32, _i64, _p, _p],
     "rla_trtri_hl_batched": [_p, _i32, _i64, _i64, _p],
-    "rla_lsqr_batched": [_i32, _p, _p, _i32, _i64, _p, _p],
+    "rla_lsqr_batched": [_i32, _p, _p, _i32, _i64, _i32, _i32, _p, _p],
     "rla_lsqr_record": [_p, _i64, _i64, _i64, _p, _p, _p, _i64, _p, _i64, _f64, _p, _p, _i32, _f64, _f64, _f64,
                         _f64, _i32, _p, _p, _p, _p],
     "rla_orgqr": [_i32, _i64, _i64, _p, _i64, _p, _p, _i64, _p, _psz, _p],

@@ -431,15 +431,23 @@ extern "C" int rla_geqrf_batched(int dtype, const void* probs, const int* order,
 }
 
 // ---------------------------------------------------------------------------
-// Batched double-float Householder QR on FP32 hi/lo planes.
+// Batched double-float Householder QR on FP32 hi/lo planes, blocked.
 //
 // The sketch is stored as two float planes (x = hi + lo), so loads and
-// stores never touch GB300's slow FP64 pipe (a binary64-stored matrix would
-// need two FP64 conversions per element access).  One CTA per problem from
-// an atomic queue; per column j: the column is staged in shared memory as
-// double-float, its norm reduced by the block, then each warp updates whole
-// trailing columns (warp-level dot product + axpy, no block barrier per
-// column).  A 1 CTA-per-problem schedule needs no grid barrier at all.
+// stores never touch GB300's slow FP64 pipe.  One CTA per problem from an
+// atomic queue.  Columns are factored in panels of B reflectors:
+//   panel   - the B panel columns (rows k0..m-1) are staged in shared memory
+//             as double-float and factored there (norm by the block, one
+//             warp per remaining panel column for the reflector update and
+//             one per entry of the compact-WY factor T: H_0 ... H_{B-1} =
+//             I - V T V^T, T upper triangular (Schreiber & Van Loan 1989));
+//   update  - every trailing column a (including the right-hand sides) gets
+//             a <- a - V (T^T (V^T a)) in two passes over its rows (V from
+//             shared memory, two columns per warp), so the trailing matrix
+//             is read and written once per panel instead of once per
+//             reflector.
+// Output as LAPACK geqrf: R on and above the diagonal, the reflectors below
+// it (unit diagonal implied), tau per column.
 namespace rla {
 namespace {
 
@@ -452,96 +460,199 @@ struct QrProblemHL {
 
 constexpr int kQrHLThreads = 512;
 
-__global__ void __launch_bounds__(kQrHLThreads)
-geqrf_hl_batched_kernel(const QrProblemHL* __restrict__ probs, const int* __restrict__ order, int nprob,
-                        int* __restrict__ next) {
-  extern __shared__ __align__(16) df xcol[];
+// acc += x * y with an exact leading product and a lazily renormalised tail
+__device__ __forceinline__ void qr_mac(df& acc, df x, df y) {
+  const float p = x.hi * y.hi;
+  float pe = fmaf(x.hi, y.hi, -p);
+  pe = fmaf(x.hi, y.lo, fmaf(x.lo, y.hi, pe));
+  const float s = acc.hi + p, bb = s - acc.hi;
+  const float e = (acc.hi - (s - bb)) + (p - bb);
+  acc.hi = s;
+  acc.lo += e + pe;
+}
+
+template <int B>
+__global__ void __launch_bounds__(kQrHLThreads, 1)
+geqrf_hl_blocked_kernel(const QrProblemHL* __restrict__ probs, const int* __restrict__ order, int nprob,
+                        int* __restrict__ next, int64_t ms) {
+  extern __shared__ __align__(16) df Vs[];  // B panel columns of ms rows (local row r = global row k0 + r)
+  __shared__ df T[B][B];
+  __shared__ df rdiag[B];
+  __shared__ df zb[B];
   __shared__ df red[32];
-  __shared__ df s_tau;
+  __shared__ df s_par[2];
   __shared__ int s_i;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
   for (;;) {
-    if (threadIdx.x == 0) s_i = atomicAdd(next, 1);
+    if (tid == 0) s_i = atomicAdd(next, 1);
     __syncthreads();
     const int pi = s_i;
     __syncthreads();
     if (pi >= nprob) return;
     const QrProblemHL q = probs[order[pi]];
-    const int64_t m = q.m, ncols = q.n + q.nrhs, lda = q.lda;
-    for (int64_t j = 0; j < q.n; ++j) {
-      float* chi = q.hi + j * lda;
-      float* clo = q.lo + j * lda;
-      // stage column j (rows j..m-1), norm of the part below the diagonal
-      df sig{0.f, 0.f};
-      for (int64_t i = j + threadIdx.x; i < m; i += blockDim.x) {
-        df x{chi[i], clo[i]};
-        xcol[i - j] = x;
-        if (i > j) sig = df_add(sig, df_mul(x, x));
+    const int64_t m = q.m, n = q.n, ncols = q.n + q.nrhs, lda = q.lda;
+    for (int64_t k0 = 0; k0 < n; k0 += B) {
+      const int bk = static_cast<int>(n - k0 < B ? n - k0 : B);
+      const int64_t mp = m - k0;
+      // ---- stage the panel (unused columns zero) ----
+      for (int c = 0; c < B; ++c) {
+        const float* chi = q.hi + (k0 + c) * lda + k0;
+        const float* clo = q.lo + (k0 + c) * lda + k0;
+        for (int64_t r = tid; r < mp; r += blockDim.x)
+          Vs[c * ms + r] = c < bk ? df{chi[r], clo[r]} : df{0.f, 0.f};
       }
-      sig = block_sum_df(sig, red);
-      if (threadIdx.x == 0) {
-        df alpha = xcol[0];
-        df beta, t, sc;
-        if (sig.hi == 0.f) {
-          beta = alpha; t = df{0.f, 0.f}; sc = df{0.f, 0.f};
-        } else {
-          df nrm = df_sqrt(df_add(sig, df_mul(alpha, alpha)));
-          beta = alpha.hi > 0.f ? df_neg(nrm) : nrm;   // beta = -sign(alpha) ||x||
-          t = df_div(df_sub(beta, alpha), beta);
-          sc = df_div(df{1.f, 0.f}, df_sub(alpha, beta));
-        }
-        s_tau = t;
-        q.tau[j] = df_to_double(t);
-        xcol[0] = beta;                                  // R(j, j)
-        red[0] = sc;
-      }
+      if (tid < B * B) T[tid / B][tid % B] = df{0.f, 0.f};
       __syncthreads();
-      const df t = s_tau, sc = red[0];
-      // v = [1; sc * x_{j+1:}]: store into the column (below the diagonal) and smem
-      for (int64_t i = j + threadIdx.x; i < m; i += blockDim.x) {
-        df v = (i == j) ? xcol[0] : df_mul(xcol[i - j], sc);
-        chi[i] = v.hi;
-        clo[i] = v.lo;
-        if (i > j) xcol[i - j] = v;
-      }
-      __syncthreads();
-      if (t.hi != 0.f) {
-        if (threadIdx.x == 0) xcol[0] = df{1.f, 0.f};
-        __syncthreads();
-        // each warp applies H_j to two trailing columns at a time (two
-        // independent accumulation chains hide the load latency)
-        for (int64_t c = j + 1 + 2 * warp; c < ncols; c += 2 * nw) {
-          const bool two = c + 1 < ncols;
-          float* ahi0 = q.hi + c * lda;
-          float* alo0 = q.lo + c * lda;
-          float* ahi1 = two ? ahi0 + lda : ahi0;
-          float* alo1 = two ? alo0 + lda : alo0;
-          df d0{0.f, 0.f}, d1{0.f, 0.f};
-          for (int64_t i = j + lane; i < m; i += 32) {
-            const df v = xcol[i - j];
-            const df a0{ahi0[i], alo0[i]}, a1{ahi1[i], alo1[i]};
-            d0 = df_add(d0, df_mul(v, a0));
-            d1 = df_add(d1, df_mul(v, a1));
+      // ---- factor the panel ----
+      for (int jj = 0; jj < bk; ++jj) {
+        df* v = Vs + jj * ms;
+        df sig{0.f, 0.f};
+        for (int64_t r = jj + 1 + tid; r < mp; r += blockDim.x) sig = df_add(sig, df_mul(v[r], v[r]));
+        sig = block_sum_df(sig, red);
+        if (tid == 0) {
+          const df alpha = v[jj];
+          df beta, t, sc;
+          if (sig.hi == 0.f) {
+            beta = alpha; t = df{0.f, 0.f}; sc = df{0.f, 0.f};
+          } else {
+            const df nrm = df_sqrt(df_add(sig, df_mul(alpha, alpha)));
+            beta = alpha.hi > 0.f ? df_neg(nrm) : nrm;  // beta = -sign(alpha) ||x||
+            t = df_div(df_sub(beta, alpha), beta);
+            sc = df_div(df{1.f, 0.f}, df_sub(alpha, beta));
           }
-          d0 = warp_sum_df(d0);
-          d1 = warp_sum_df(d1);
-          const df w0 = df_mul(t, d0), w1 = df_mul(t, d1);
-          for (int64_t i = j + lane; i < m; i += 32) {
-            const df v = xcol[i - j];
-            const df a0 = df_sub(df{ahi0[i], alo0[i]}, df_mul(w0, v));
-            ahi0[i] = a0.hi;
-            alo0[i] = a0.lo;
-            if (two) {
-              const df a1 = df_sub(df{ahi1[i], alo1[i]}, df_mul(w1, v));
-              ahi1[i] = a1.hi;
-              alo1[i] = a1.lo;
-            }
+          s_par[0] = t;
+          s_par[1] = sc;
+          rdiag[jj] = beta;
+          q.tau[k0 + jj] = df_to_double(t);
+        }
+        __syncthreads();
+        const df t = s_par[0], sc = s_par[1];
+        for (int64_t r = jj + 1 + tid; r < mp; r += blockDim.x) v[r] = df_mul(v[r], sc);
+        if (tid == 0) v[jj] = df{1.f, 0.f};
+        __syncthreads();
+        // warps: H_jj on panel columns jj+1..bk-1, and z_i = v_i . v_jj (i < jj)
+        const int nupd = bk - 1 - jj;
+        for (int task = warp; task < nupd + jj; task += nw) {
+          if (task < nupd) {
+            df* ac = Vs + (jj + 1 + task) * ms;
+            df d{0.f, 0.f};
+            for (int64_t r = jj + lane; r < mp; r += 32) d = df_add(d, df_mul(v[r], ac[r]));
+            d = warp_sum_df(d);
+            const df w = df_mul(t, d);
+            for (int64_t r = jj + lane; r < mp; r += 32) ac[r] = df_sub(ac[r], df_mul(w, v[r]));
+          } else {
+            const int i = task - nupd;
+            const df* vi = Vs + i * ms;
+            df d{0.f, 0.f};
+            for (int64_t r = jj + lane; r < mp; r += 32) d = df_add(d, df_mul(vi[r], v[r]));
+            d = warp_sum_df(d);
+            if (lane == 0) zb[i] = d;
+          }
+        }
+        __syncthreads();
+        if (tid == 0) {
+          // T(0:jj, jj) = -t T(0:jj, 0:jj) z,  T(jj, jj) = t
+          for (int i = 0; i < jj; ++i) {
+            df acc{0.f, 0.f};
+            for (int l = i; l < jj; ++l) acc = df_add(acc, df_mul(T[i][l], zb[l]));
+            T[i][jj] = df_neg(df_mul(t, acc));
+          }
+          T[jj][jj] = t;
+        }
+      }
+      __syncthreads();
+      // ---- write the panel back (R above and on the diagonal, v below);
+      // the smem copy keeps only V (zeros above the unit diagonal) ----
+      for (int c = 0; c < bk; ++c) {
+        float* chi = q.hi + (k0 + c) * lda + k0;
+        float* clo = q.lo + (k0 + c) * lda + k0;
+        for (int64_t r = tid; r < mp; r += blockDim.x) {
+          const df x = r == c ? rdiag[c] : Vs[c * ms + r];
+          chi[r] = x.hi;
+          clo[r] = x.lo;
+          if (r < c) Vs[c * ms + r] = df{0.f, 0.f};
+        }
+      }
+      __syncthreads();
+      // ---- trailing update: a <- a - V (T^T (V^T a)), two columns per warp ----
+      for (int64_t c = k0 + bk + 2 * warp; c < ncols; c += 2 * nw) {
+        const bool two = c + 1 < ncols;
+        float* h0 = q.hi + c * lda + k0;
+        float* l0 = q.lo + c * lda + k0;
+        float* h1 = two ? h0 + lda : h0;
+        float* l1 = two ? l0 + lda : l0;
+        df w0[B], w1[B];
+#pragma unroll
+        for (int i = 0; i < B; ++i) { w0[i] = df{0.f, 0.f}; w1[i] = df{0.f, 0.f}; }
+        int cnt = 0;
+#pragma unroll 2
+        for (int64_t r = lane; r < mp; r += 32) {
+          const df a0{h0[r], l0[r]}, a1{h1[r], l1[r]};
+#pragma unroll
+          for (int i = 0; i < B; ++i) {
+            const df vv = Vs[i * ms + r];
+            qr_mac(w0[i], vv, a0);
+            qr_mac(w1[i], vv, a1);
+          }
+          if ((++cnt & 7) == 0) {
+#pragma unroll
+            for (int i = 0; i < B; ++i) { w0[i] = quick_two_sum(w0[i].hi, w0[i].lo); w1[i] = quick_two_sum(w1[i].hi, w1[i].lo); }
+          }
+        }
+#pragma unroll
+        for (int i = 0; i < B; ++i) {
+          w0[i] = warp_sum_df(quick_two_sum(w0[i].hi, w0[i].lo));
+          w1[i] = warp_sum_df(quick_two_sum(w1[i].hi, w1[i].lo));
+        }
+        // w <- T^T w (T upper triangular): from the last entry down
+#pragma unroll
+        for (int i = B - 1; i >= 0; --i) {
+          df s0{0.f, 0.f}, s1{0.f, 0.f};
+#pragma unroll
+          for (int l = 0; l <= i; ++l) {
+            s0 = df_add(s0, df_mul(T[l][i], w0[l]));
+            s1 = df_add(s1, df_mul(T[l][i], w1[l]));
+          }
+          w0[i] = s0;
+          w1[i] = s1;
+        }
+#pragma unroll 2
+        for (int64_t r = lane; r < mp; r += 32) {
+          df s0{0.f, 0.f}, s1{0.f, 0.f};
+#pragma unroll
+          for (int i = 0; i < B; ++i) {
+            const df vv = Vs[i * ms + r];
+            qr_mac(s0, vv, w0[i]);
+            qr_mac(s1, vv, w1[i]);
+          }
+          const df a0 = df_sub(df{h0[r], l0[r]}, quick_two_sum(s0.hi, s0.lo));
+          h0[r] = a0.hi;
+          l0[r] = a0.lo;
+          if (two) {
+            const df a1 = df_sub(df{h1[r], l1[r]}, quick_two_sum(s1.hi, s1.lo));
+            h1[r] = a1.hi;
+            l1[r] = a1.lo;
           }
         }
       }
       __syncthreads();
     }
   }
+}
+
+template <int B>
+int geqrf_hl_blocked_launch(const QrProblemHL* probs, const int* order, int nprob, int64_t mmax, int* next,
+                            cudaStream_t st) {
+  const size_t smem = static_cast<size_t>(B) * mmax * sizeof(df);
+  RLA_CUDA_TRY(cudaFuncSetAttribute(geqrf_hl_blocked_kernel<B>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    static_cast<int>(smem)));
+  int per_sm = 0;
+  RLA_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, geqrf_hl_blocked_kernel<B>, kQrHLThreads, smem));
+  const int grid = static_cast<int>(imin(nprob, static_cast<int64_t>(imax(per_sm, 1)) * sm_count()));
+  RLA_CUDA_TRY(cudaMemsetAsync(next, 0, sizeof(int), st));
+  geqrf_hl_blocked_kernel<B><<<grid, kQrHLThreads, smem, st>>>(probs, order, nprob, next, mmax);
+  RLA_LAUNCH_CHECK();
+  return RLA_OK;
 }
 
 }  // namespace
@@ -551,28 +662,21 @@ extern "C" size_t rla_qr_hl_record_size(void) { return sizeof(rla::QrProblemHL);
 
 // Batched QR on hi/lo planes: records {int64 m, n, nrhs, lda; float* hi;
 // float* lo; double* tau} (rla_qr_hl_record_size bytes), mmax = largest m.
+// Panel width 8 while the panel (8 x mmax double-float) fits 128 KB of
+// shared memory, narrower for taller problems.
 extern "C" int rla_geqrf_hl_batched(const void* probs, const int* order, int nprob, int64_t mmax, int* next,
                                     rla_stream_t stream) {
   using namespace rla;
   if (nprob < 0 || !probs || !order || !next || mmax <= 0) return RLA_ERR_ARG;
   if (nprob == 0) return RLA_OK;
-  const size_t smem = static_cast<size_t>(mmax) * sizeof(df);
-  if (smem > 200 * 1024) return RLA_ERR_UNSUPPORTED;
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-  static thread_local int attr_dev = -1;
-  int dev = 0;
-  RLA_CUDA_TRY(cudaGetDevice(&dev));
-  if (attr_dev != dev) {
-    RLA_CUDA_TRY(cudaFuncSetAttribute(geqrf_hl_batched_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-    attr_dev = dev;
-  }
-  int per_sm = 0;
-  RLA_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, geqrf_hl_batched_kernel, kQrHLThreads, smem));
-  const int grid = static_cast<int>(imin(nprob, static_cast<int64_t>(imax(per_sm, 1)) * sm_count()));
-  RLA_CUDA_TRY(cudaMemsetAsync(next, 0, sizeof(int), st));
-  geqrf_hl_batched_kernel<<<grid, kQrHLThreads, smem, st>>>(static_cast<const QrProblemHL*>(probs), order, nprob, next);
-  RLA_LAUNCH_CHECK();
-  return RLA_OK;
+  const auto* p = static_cast<const QrProblemHL*>(probs);
+  const size_t col = static_cast<size_t>(mmax) * sizeof(df);
+  if (8 * col <= 128 * 1024) return geqrf_hl_blocked_launch<8>(p, order, nprob, mmax, next, st);
+  if (4 * col <= 200 * 1024) return geqrf_hl_blocked_launch<4>(p, order, nprob, mmax, next, st);
+  if (2 * col <= 200 * 1024) return geqrf_hl_blocked_launch<2>(p, order, nprob, mmax, next, st);
+  if (col <= 200 * 1024) return geqrf_hl_blocked_launch<1>(p, order, nprob, mmax, next, st);
+  return RLA_ERR_UNSUPPORTED;
 }
 
 // ---------------------------------------------------------------------------

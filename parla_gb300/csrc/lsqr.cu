@@ -9,7 +9,9 @@
 //   P5  v' = M^T t - beta v, partial ||v'||^2
 //   P6  alfa = ||v'||, Givens recurrences, z/w updates, next y = M v
 // The scalar recurrences run redundantly in every CTA on identical inputs,
-// so no broadcast is needed.  All sums use a fixed order: results do not
+// so no broadcast is needed.  The batched form runs the same iteration on a
+// thread-block cluster per problem (G = cluster size, hardware cluster
+// barrier between phases, partials exchanged through L2) or on one CTA.  All sums use a fixed order: results do not
 // depend on scheduling.
 //
 // Two arithmetic modes:
@@ -17,12 +19,17 @@
 //   DF  - A pre-split into FP32 hi/lo planes (A = hi + lo to ~2^-48),
 //         double-float products and sums on the FP32 pipes: same 8 bytes per
 //         element of traffic, HBM-bound instead of FP64-bound.
+#include <cooperative_groups.h>
+
 #include "arith.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace rla {
 namespace {
 
 constexpr int kLsqrThreads = 256;
+constexpr int kLsqrMaxCluster = 8;  // largest cluster of the batched form (portable size)
 
 struct LsqrArgs {
   int64_t m, n, p;
@@ -115,9 +122,8 @@ template <> struct Elem<df> {
   __device__ static void renorm(df& acc) { acc = quick_two_sum(acc.hi, acc.lo); }
 };
 
-struct Scal {  // LSQR scalar state (binary64, thread 0 of each CTA)
-  double alfa, beta, rhobar, phibar, anorm, acond, ddnorm, res2, xnorm, xxnorm, zz, cs2, sn2, bnorm, arnorm;
-  double t1, t2, rho;  // per-iteration update coefficients
+struct Scal {  // LSQR recurrence state (binary64, shared memory, advanced by thread 0)
+  double rhobar, phibar, anorm, acond, ddnorm, res2, xnorm, xxnorm, zz, cs2, sn2, bnorm, arnorm, rnorm_prev;
 };
 
 // Sum of the G per-CTA partials, identical in every CTA: warp 0 reads them in
@@ -154,15 +160,28 @@ __device__ __forceinline__ void lsqr_body(const LsqrArgs& a, const int G, const 
   const int64_t chunk = ceil_div(a.m, G);
   const int64_t r0 = min(a.m, static_cast<int64_t>(blk) * chunk), r1 = min(a.m, r0 + chunk);
   const bool ext = a.sd > 0.0;
-  Scal s{};
 
   // ---- helpers ------------------------------------------------------
-  // y = M x (x: p-vector in global), rows of M distributed over all warps.
+  // y = M x (x: p-vector in global), one warp per row of M over all CTAs.
+  // Each lane issues kMU independent loads of the row (and of x) before
+  // accumulating, so a row costs one or two memory round trips.
+  constexpr int kMU = 4;
   auto mat_M_to = [&](const double* x, double scale, double* dst) {
     for (int64_t i = static_cast<int64_t>(blk) * nw + warp; i < a.n; i += static_cast<int64_t>(G) * nw) {
       const double* mr = a.M + i * a.ldm;
       V acc = R::zero();
-      for (int64_t c = lane; c < a.p; c += 32) acc = R::fma(acc, R::ld(mr + c), R::ldcg(x + c));
+      for (int64_t c0 = 0; c0 < a.p; c0 += 32 * kMU) {
+        double mv[kMU], xv[kMU];
+#pragma unroll
+        for (int u = 0; u < kMU; ++u) {
+          const int64_t c = c0 + 32 * u + lane;
+          mv[u] = c < a.p ? mr[c] : 0.0;
+          xv[u] = c < a.p ? __ldcg(x + c) : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < kMU; ++u) Elem<V>::mac(acc, R::ld(mv + u), R::ld(xv + u));
+      }
+      Elem<V>::renorm(acc);
       acc = R::wsum(acc);
       if (lane == 0) R::st(dst + i, R::mul(acc, R::from_d(scale)));
     }
@@ -218,12 +237,14 @@ __device__ __forceinline__ void lsqr_body(const LsqrArgs& a, const int G, const 
     V part = R::zero();
     const V vca = R::from_d(ca), vcu = R::from_d(cu);
     int cnt = 0;
-    // software pipelined over the warp's rows (n <= 256): the next row's
-    // elements are loaded while the current one is reduced, so two rows per
-    // warp are in flight (one row at a time left the pass latency-bound);
-    // wider rows keep one row in flight to stay within the register budget
+    // Software pipelined over the warp's rows: kDepth rows beyond the one
+    // being reduced are in flight (more for narrow rows, whose registers are
+    // cheap; none for the widest class, to stay within the register budget),
+    // and the old u (or b) values of the warp's rows are fetched 32 rows at
+    // a time, one group ahead, and passed along by shuffles, so no load
+    // latency sits on a row's dependency chain.
     constexpr int NP = NPL > 0 ? NPL : 1;
-    constexpr bool kPrefetch = NPL <= 8;
+    constexpr int kDepth = NPL <= 2 ? 4 : NPL <= 4 ? 2 : NPL <= 8 ? 1 : 0;
     auto load_row = [&](int64_t i, V (&dst)[NP]) {
 #pragma unroll
       for (int q = 0; q < NP; ++q) {
@@ -231,18 +252,32 @@ __device__ __forceinline__ void lsqr_body(const LsqrArgs& a, const int G, const 
         dst[q] = j < a.n ? Elem<V>::ld(a, i, j) : R::zero();
       }
     };
-    V cur[NP], nxt[NP];
+    const double* usrc = with_b ? a.b : a.u;
+    // old value of the warp's k-th row .. (k+31)-th row, lane l holding k + l
+    auto load_u = [&](int64_t k) -> double {
+      const int64_t row = r0 + warp + (k + lane) * nw;
+      return row < r1 ? __ldcg(usrc + row) : 0.0;
+    };
+    V buf[kDepth + 1][NP];
     int64_t i = r0 + warp;
-    if (i < r1) load_row(i, cur);
-    for (; i < r1; i += nw) {
-      const int64_t inext = i + nw;
-      if (kPrefetch && inext < r1) load_row(inext, nxt);
-      const V uold = with_b ? R::ld(a.b + i) : R::ldcg(a.u + i);
+#pragma unroll
+    for (int d = 0; d < kDepth; ++d)
+      if (i + d * nw < r1) load_row(i + d * nw, buf[d]);
+    double ucur = load_u(0), unext = load_u(32);
+    for (int64_t k = 0; i < r1; i += nw, ++k) {
+      if (kDepth > 0 && i + kDepth * nw < r1) load_row(i + kDepth * nw, buf[kDepth]);
+      if (kDepth == 0) load_row(i, buf[0]);
+      if ((k & 31) == 0 && k > 0) {
+        ucur = unext;
+        unext = load_u(k + 32);
+      }
+      const double uraw = __shfl_sync(0xffffffffu, ucur, static_cast<int>(k & 31));
+      const V uold = R::ld(&uraw);
       V dot = R::zero();
 #pragma unroll
       for (int q = 0; q < NP; ++q) {
         const int64_t j = lane + 32 * q;
-        if (j < a.n) Elem<V>::mac(dot, cur[q], xs[j]);
+        if (j < a.n) Elem<V>::mac(dot, buf[0][q], xs[j]);
       }
       Elem<V>::renorm(dot);
       dot = R::wsum(dot);
@@ -253,17 +288,15 @@ __device__ __forceinline__ void lsqr_body(const LsqrArgs& a, const int G, const 
         part = R::fma(part, ui, ui);
       }
 #pragma unroll
-      for (int q = 0; q < NP; ++q) Elem<V>::mac(acc[q], cur[q], ui);
+      for (int q = 0; q < NP; ++q) Elem<V>::mac(acc[q], buf[0][q], ui);
       if ((++cnt & 15) == 0) {
 #pragma unroll
         for (int q = 0; q < NP; ++q) Elem<V>::renorm(acc[q]);
       }
-      if (kPrefetch) {
 #pragma unroll
-        for (int q = 0; q < NP; ++q) cur[q] = nxt[q];
-      } else if (inext < r1) {
-        load_row(inext, cur);
-      }
+      for (int d = 0; d < kDepth; ++d)
+#pragma unroll
+        for (int q = 0; q < NP; ++q) buf[d][q] = buf[d + 1][q];
     }
     if (ext && blk == 0) {
       for (int64_t j = tid; j < a.n; j += blockDim.x) {
@@ -290,9 +323,20 @@ __device__ __forceinline__ void lsqr_body(const LsqrArgs& a, const int G, const 
     part = R::bsum(part, red);
     return R::to_d(part);
   };
-  // t_j = scale * (sum_g tpart[g][j] + sd * uext_j): one warp per column,
-  // lanes split the G partials (fixed order), xor-tree reduction
+  // t_j = scale * (sum_g tpart[g][j] + sd * uext_j) in a fixed order.  Grid
+  // form: one warp per column, lanes split the G partials, xor-tree
+  // reduction.  Cluster / single-CTA form (G <= 16): one thread per column
+  // sums the partials in rank order.
   auto reduce_t = [&](double scale) {
+    if (!Coop) {
+      for (int64_t j = gtid; j < a.n; j += gthreads) {
+        double acc = 0.0;
+        for (int g = 0; g < G; ++g) acc += __ldcg(a.tpart + static_cast<int64_t>(g) * a.n + j);
+        if (ext) acc += a.sd * __ldcg(a.uext + j);
+        a.t[j] = acc * scale;
+      }
+      return;
+    }
     const int64_t gw = static_cast<int64_t>(blk) * nw + warp, nwarps_all = static_cast<int64_t>(G) * nw;
     for (int64_t j = gw; j < a.n; j += nwarps_all) {
       double acc = 0.0;
@@ -304,14 +348,27 @@ __device__ __forceinline__ void lsqr_body(const LsqrArgs& a, const int G, const 
       }
     }
   };
-  // v'_c = (M^T t)_c + cv * v_c, one warp per column c over all CTAs (lanes
-  // split the n rows, fixed-order xor tree); returns this CTA's ||v'||^2
+  // v'_c = (M^T t)_c + cv * v_c, one warp per column over all CTAs, lanes
+  // split the n rows (kMU independent loads each; the warps of a CTA take
+  // neighbouring columns, so the sectors of a row are shared in L1),
+  // fixed-order xor tree; returns this CTA's ||v'||^2.
   auto apply_Mt = [&](double cv) -> double {
     V part = R::zero();
     const int64_t gw = static_cast<int64_t>(blk) * nw + warp, nwarps_all = static_cast<int64_t>(G) * nw;
     for (int64_t c = gw; c < a.p; c += nwarps_all) {
       V acc = R::zero();
-      for (int64_t j = lane; j < a.n; j += 32) acc = R::fma(acc, R::ld(a.M + j * a.ldm + c), R::ldcg(a.t + j));
+      for (int64_t j0 = 0; j0 < a.n; j0 += 32 * kMU) {
+        double mv[kMU], tv[kMU];
+#pragma unroll
+        for (int u = 0; u < kMU; ++u) {
+          const int64_t j = j0 + 32 * u + lane;
+          mv[u] = j < a.n ? a.M[j * a.ldm + c] : 0.0;
+          tv[u] = j < a.n ? __ldcg(a.t + j) : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < kMU; ++u) Elem<V>::mac(acc, R::ld(mv + u), R::ld(tv + u));
+      }
+      Elem<V>::renorm(acc);
       acc = R::wsum(acc);
       if (lane == 0) {
         V vn = R::add(acc, R::mul(R::from_d(cv), R::ldcg(a.v + c)));
@@ -322,10 +379,22 @@ __device__ __forceinline__ void lsqr_body(const LsqrArgs& a, const int G, const 
     part = R::bsum(part, red);
     return R::to_d(part);
   };
-#define RLA_SYNC() do { if (Coop) { if (!grid_sync(a.bar)) return; } else { __syncthreads(); } } while (0)
+#define RLA_SYNC()                             \
+  do {                                         \
+    if (Coop) {                                \
+      if (!grid_sync(a.bar)) return;           \
+    } else if (G > 1) {                        \
+      cg::this_cluster().sync();               \
+    } else {                                   \
+      __syncthreads();                         \
+    }                                          \
+  } while (0)
 
   // ---- initialisation -----------------------------------------------
   // The v buffer holds v' = alfa * v (unnormalised); readers scale by 1/alfa.
+  // alfa, beta and bnorm come out of fixed-order sums and are held by every
+  // thread; the rest of the recurrence state lives in shared memory and is
+  // advanced by thread 0, which broadcasts the update coefficients.
   double bnorm2 = 0.0;
   for (int64_t i = r0 + tid; i < r1; i += blockDim.x) { double bi = a.b[i]; bnorm2 = fma(bi, bi, bnorm2); }
   bnorm2 = block_sum(bnorm2, redd);
@@ -336,7 +405,7 @@ __device__ __forceinline__ void lsqr_body(const LsqrArgs& a, const int G, const 
     for (int64_t c = gtid; c < a.p; c += gthreads) a.z[c] = 0.0;
   }
   RLA_SYNC();
-  s.bnorm = sqrt(sum_parts<V>(a.part, G));
+  const double bnorm = sqrt(sum_parts<V>(a.part, G));
   RLA_SYNC();
   double pu = 0.0;
   if (NPL > 0) {
@@ -351,14 +420,14 @@ __device__ __forceinline__ void lsqr_body(const LsqrArgs& a, const int G, const 
   }
   if (tid == 0) a.part[blk] = pu;
   RLA_SYNC();
-  s.beta = a.has_x0 ? sqrt(sum_parts<V>(a.part, G)) : s.bnorm;
-  s.alfa = 0.0;
-  double beta_prev = s.beta > 0.0 ? s.beta : 1.0;  // u is stored unnormalised (fused path)
-  if (s.beta > 0.0) {
+  double beta = a.has_x0 ? sqrt(sum_parts<V>(a.part, G)) : bnorm;
+  double alfa = 0.0;
+  double beta_prev = beta > 0.0 ? beta : 1.0;  // u is stored unnormalised (fused path)
+  if (beta > 0.0) {
     if (NPL > 0) {
-      reduce_t(1.0 / s.beta);
+      reduce_t(1.0 / beta);
     } else {
-      apply_At(1.0 / s.beta);
+      apply_At(1.0 / beta);
       RLA_SYNC();
       reduce_t(1.0);
     }
@@ -367,12 +436,9 @@ __device__ __forceinline__ void lsqr_body(const LsqrArgs& a, const int G, const 
     double pv = apply_Mt(0.0);
     if (tid == 0) a.part[blk] = pv;
     RLA_SYNC();
-    s.alfa = sqrt(sum_parts<V>(a.part, G));
+    alfa = sqrt(sum_parts<V>(a.part, G));
   }
-  const double eps = 2.220446049250313e-16;
-  const double ctol = a.conlim > 0.0 ? 1.0 / a.conlim : 0.0;
-  s.arnorm = s.alfa * s.beta;
-  if (s.arnorm == 0.0) {
+  if (alfa * beta == 0.0) {
     if (blk == 0 && tid == 0) { a.out[0] = 0; a.out[1] = 0; }
     if (a.x != nullptr) {
       RLA_SYNC();
@@ -381,108 +447,125 @@ __device__ __forceinline__ void lsqr_body(const LsqrArgs& a, const int G, const 
     return;
   }
   {
-    const double ia = 1.0 / s.alfa;
+    const double ia = 1.0 / alfa;
     for (int64_t c = gtid; c < a.p; c += gthreads) a.w[c] = __ldcg(a.v + c) * ia;
     mat_M(a.v, ia);
   }
+  __shared__ Scal s;
+  __shared__ double s_coef[3];
+  __shared__ int s_istop;
+  if (tid == 0) {
+    s.bnorm = bnorm;
+    s.arnorm = alfa * beta;
+    s.rhobar = alfa; s.phibar = beta;
+    s.anorm = s.acond = s.ddnorm = s.res2 = s.xnorm = s.xxnorm = s.zz = 0.0;
+    s.cs2 = -1.0; s.sn2 = 0.0;
+    s.rnorm_prev = beta;
+  }
   RLA_SYNC();
-  s.rhobar = s.alfa; s.phibar = s.beta;
-  s.anorm = s.acond = s.ddnorm = s.res2 = s.xnorm = s.xxnorm = s.zz = 0.0;
-  s.cs2 = -1.0; s.sn2 = 0.0;
   int itn = 0, istop = 0;
-  double rnorm_prev = s.beta;
 
   // ---- main loop ----------------------------------------------------
   while (itn < a.iter_lim) {
     if (blk == 0 && tid == 0) a.arn[itn] = s.arnorm;
     ++itn;
     // P2: u = A y - alfa u (fused: with A^T u), and ||w||^2 for ddnorm
-    double pu2 = (NPL > 0) ? apply_A_fused(1.0, -s.alfa / beta_prev, false) : apply_A(1.0, -s.alfa, false);
+    double pu2 = (NPL > 0) ? apply_A_fused(1.0, -alfa / beta_prev, false) : apply_A(1.0, -alfa, false);
     double pw = 0.0;
     for (int64_t c = gtid; c < a.p; c += gthreads) { double wc = a.w[c]; pw = fma(wc, wc, pw); }
     pw = block_sum(pw, redd);
     if (tid == 0) { a.part[blk] = pu2; a.part[G + blk] = pw; }
     RLA_SYNC();
     // P3/P4: beta, t = A^T u / beta
-    s.beta = sqrt(sum_parts<V>(a.part, G));
+    beta = sqrt(sum_parts<V>(a.part, G));
     const double wnorm2 = sum_parts<V>(a.part + G, G);
-    const double alfa_old = s.alfa;
-    if (s.beta > 0.0) {
+    const double alfa_old = alfa;
+    if (beta > 0.0) {
       if (NPL > 0) {
-        reduce_t(1.0 / s.beta);
-        beta_prev = s.beta;
+        reduce_t(1.0 / beta);
+        beta_prev = beta;
       } else {
-        apply_At(1.0 / s.beta);
+        apply_At(1.0 / beta);
         RLA_SYNC();
         reduce_t(1.0);
       }
       RLA_SYNC();
       // P5: v' = M^T t - beta v, with v = v'_old / alfa_old
-      double pv = apply_Mt(-s.beta / alfa_old);
+      double pv = apply_Mt(-beta / alfa_old);
       if (tid == 0) a.part[blk] = pv;
       RLA_SYNC();
-      s.anorm = sqrt(s.anorm * s.anorm + s.alfa * s.alfa + s.beta * s.beta);
-      s.alfa = sqrt(sum_parts<V>(a.part, G));
+      alfa = sqrt(sum_parts<V>(a.part, G));
     }
-    // P6: scalar recurrences (identical in every CTA; no damping term,
-    // the regularisation enters through the [A; sd I] operator)
-    double rhobar1 = fabs(s.rhobar);
-    double cs1 = s.rhobar / rhobar1;
-    s.phibar = cs1 * s.phibar;
-    double cs, sn, rho;
-    {
-      double aa = rhobar1, bb = s.beta;
-      if (bb == 0.0) { cs = (aa > 0) - (aa < 0); sn = 0.0; rho = fabs(aa); }
-      else if (aa == 0.0) { cs = 0.0; sn = (bb > 0) - (bb < 0); rho = fabs(bb); }
-      else if (fabs(bb) > fabs(aa)) { double q = aa / bb; sn = ((bb > 0) - (bb < 0)) / sqrt(1.0 + q * q); cs = sn * q; rho = bb / sn; }
-      else { double q = bb / aa; cs = ((aa > 0) - (aa < 0)) / sqrt(1.0 + q * q); sn = cs * q; rho = aa / cs; }
+    // P6: scalar recurrences (thread 0 of every CTA on identical inputs; no
+    // damping term, the regularisation enters through the [A; sd I] operator)
+    if (tid == 0) {
+      if (beta > 0.0) s.anorm = sqrt(s.anorm * s.anorm + alfa_old * alfa_old + beta * beta);
+      double rhobar1 = fabs(s.rhobar);
+      double cs1 = s.rhobar / rhobar1;
+      s.phibar = cs1 * s.phibar;
+      double cs, sn, rho;
+      {
+        double aa = rhobar1, bb = beta;
+        if (bb == 0.0) { cs = (aa > 0) - (aa < 0); sn = 0.0; rho = fabs(aa); }
+        else if (aa == 0.0) { cs = 0.0; sn = (bb > 0) - (bb < 0); rho = fabs(bb); }
+        else if (fabs(bb) > fabs(aa)) { double q = aa / bb; sn = ((bb > 0) - (bb < 0)) / sqrt(1.0 + q * q); cs = sn * q; rho = bb / sn; }
+        else { double q = bb / aa; cs = ((aa > 0) - (aa < 0)) / sqrt(1.0 + q * q); sn = cs * q; rho = aa / cs; }
+      }
+      double theta = sn * alfa;
+      s.rhobar = -cs * alfa;
+      double phi = cs * s.phibar;
+      s.phibar = sn * s.phibar;
+      double tau = sn * phi;
+      const double ia = alfa > 0.0 ? 1.0 / alfa : 0.0;
+      s_coef[0] = phi / rho;
+      s_coef[1] = -theta / rho;
+      s_coef[2] = beta > 0.0 ? ia : (alfa_old > 0.0 ? 1.0 / alfa_old : 0.0);
+      s.ddnorm += wnorm2 / (rho * rho);
+      double delta = s.sn2 * rho;
+      double gambar = -s.cs2 * rho;
+      double rhs = phi - delta * s.zz;
+      double zbar = rhs / gambar;
+      s.xnorm = sqrt(s.xxnorm + zbar * zbar);
+      double gamma = sqrt(gambar * gambar + theta * theta);
+      s.cs2 = gambar / gamma;
+      s.sn2 = theta / gamma;
+      s.zz = rhs / gamma;
+      s.xxnorm += s.zz * s.zz;
+      s.acond = s.anorm * sqrt(s.ddnorm);
+      double rnorm = sqrt(s.phibar * s.phibar + s.res2);
+      // ||r_{k-1}||^2 - ||r_k||^2 = ||Abar (z_k - z_{k-1})||^2: the prediction change
+      const double dpred2 = fmax(s.rnorm_prev * s.rnorm_prev - rnorm * rnorm, 0.0);
+      s.rnorm_prev = rnorm;
+      s.arnorm = alfa * fabs(tau);
+      const double eps = 2.220446049250313e-16;
+      const double ctol = a.conlim > 0.0 ? 1.0 / a.conlim : 0.0;
+      double test1 = rnorm / s.bnorm;
+      double test2 = s.arnorm / (s.anorm * rnorm + eps);
+      double test3 = 1.0 / (s.acond + eps);
+      double tt1 = test1 / (1.0 + s.anorm * s.xnorm / s.bnorm);
+      double rtol = a.btol + a.atol * s.anorm * s.xnorm / s.bnorm;
+      int st = 0;
+      if (itn >= a.iter_lim) st = 7;
+      if (1.0 + test3 <= 1.0) st = 6;
+      if (1.0 + test2 <= 1.0) st = 5;
+      if (1.0 + tt1 <= 1.0) st = 4;
+      if (test3 <= ctol) st = 3;
+      if (test2 <= a.atol) st = 2;
+      if (test1 <= rtol) st = 1;
+      // prediction-error rule: with linear convergence at rate <= 1/2 the
+      // remaining ||Abar (z - z*)|| is at most the last change
+      if (a.ptol > 0.0 && itn >= 2 && sqrt(dpred2) <= a.ptol * s.bnorm) st = 9;
+      if (!isfinite(s.arnorm) || !isfinite(rnorm)) st = 8;
+      s_istop = st;
     }
-    double theta = sn * s.alfa;
-    s.rhobar = -cs * s.alfa;
-    double phi = cs * s.phibar;
-    s.phibar = sn * s.phibar;
-    double tau = sn * phi;
-    const double t1 = phi / rho, t2 = -theta / rho;
-    const double ia = s.alfa > 0.0 ? 1.0 / s.alfa : 0.0;
-    const double vscale = s.beta > 0.0 ? ia : (alfa_old > 0.0 ? 1.0 / alfa_old : 0.0);
+    __syncthreads();
+    const double t1 = s_coef[0], t2 = s_coef[1], vscale = s_coef[2];
+    istop = s_istop;
     for (int64_t c = gtid; c < a.p; c += gthreads) {
       double wc = a.w[c];
       a.z[c] = fma(t1, wc, a.z[c]);
       a.w[c] = fma(t2, wc, __ldcg(a.v + c) * vscale);
     }
-    s.ddnorm += wnorm2 / (rho * rho);
-    double delta = s.sn2 * rho;
-    double gambar = -s.cs2 * rho;
-    double rhs = phi - delta * s.zz;
-    double zbar = rhs / gambar;
-    s.xnorm = sqrt(s.xxnorm + zbar * zbar);
-    double gamma = sqrt(gambar * gambar + theta * theta);
-    s.cs2 = gambar / gamma;
-    s.sn2 = theta / gamma;
-    s.zz = rhs / gamma;
-    s.xxnorm += s.zz * s.zz;
-    s.acond = s.anorm * sqrt(s.ddnorm);
-    double rnorm = sqrt(s.phibar * s.phibar + s.res2);
-    // ||r_{k-1}||^2 - ||r_k||^2 = ||Abar (z_k - z_{k-1})||^2: the prediction change
-    const double dpred2 = fmax(rnorm_prev * rnorm_prev - rnorm * rnorm, 0.0);
-    rnorm_prev = rnorm;
-    s.arnorm = s.alfa * fabs(tau);
-    double test1 = rnorm / s.bnorm;
-    double test2 = s.arnorm / (s.anorm * rnorm + eps);
-    double test3 = 1.0 / (s.acond + eps);
-    double tt1 = test1 / (1.0 + s.anorm * s.xnorm / s.bnorm);
-    double rtol = a.btol + a.atol * s.anorm * s.xnorm / s.bnorm;
-    if (itn >= a.iter_lim) istop = 7;
-    if (1.0 + test3 <= 1.0) istop = 6;
-    if (1.0 + test2 <= 1.0) istop = 5;
-    if (1.0 + tt1 <= 1.0) istop = 4;
-    if (test3 <= ctol) istop = 3;
-    if (test2 <= a.atol) istop = 2;
-    if (test1 <= rtol) istop = 1;
-    // prediction-error rule: with linear convergence at rate <= 1/2 the
-    // remaining ||Abar (z - z*)|| is at most the last change
-    if (a.ptol > 0.0 && itn >= 2 && sqrt(dpred2) <= a.ptol * s.bnorm) istop = 9;
-    if (!isfinite(s.arnorm) || !isfinite(rnorm)) istop = 8;
     if (istop != 0) break;
     mat_M(a.v, vscale);
     RLA_SYNC();
@@ -495,12 +578,6 @@ __device__ __forceinline__ void lsqr_body(const LsqrArgs& a, const int G, const 
 #undef RLA_SYNC
 }
 
-template <class P, int NPL>
-__device__ __forceinline__ void lsqr_dispatch(const LsqrArgs& a, int G, int blk, unsigned char* smem, bool coop) {
-  if (coop) lsqr_body<P, true, NPL>(a, G, blk, smem);
-  else lsqr_body<P, false, NPL>(a, G, blk, smem);
-}
-
 // NPL = columns per lane of the fused one-pass products (n <= 32 NPL);
 // 0 selects the two-pass form for wide problems.  Each width class is its
 // own kernel instantiation (its own register allocation), chosen on the host.
@@ -511,27 +588,51 @@ __host__ __device__ inline int lsqr_npl(int64_t n) {
 template <class P, int NPL>
 __global__ void __launch_bounds__(kLsqrThreads, 2) lsqr_kernel(LsqrArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  lsqr_dispatch<P, NPL>(a, static_cast<int>(gridDim.x), static_cast<int>(blockIdx.x), smem_raw, true);
+  lsqr_body<P, true, NPL>(a, static_cast<int>(gridDim.x), static_cast<int>(blockIdx.x), smem_raw);
 }
 
-// Persistent batched form: each CTA takes the next problem (largest first,
-// `order`) from an atomic queue and solves it alone.  All problems of one
-// launch must satisfy lsqr_npl(n) <= NPL (the launcher picks NPL from nmax).
+// One width variant of the cluster / single-CTA solve as its own function:
+// each variant keeps its own register allocation inside the shared kernel.
 template <class P, int NPL>
+__device__ __noinline__ void lsqr_body_cluster(const LsqrArgs& a, int G, int blk, unsigned char* smem) {
+  lsqr_body<P, false, NPL>(a, G, blk, smem);
+}
+
+// Persistent batched form: each cluster (G CTAs, the launch's cluster size;
+// G = 1 is a plain CTA) takes the next problem (largest first, `order`) from
+// an atomic queue and solves it alone, rows split over its CTAs.  Rank 0
+// draws the index and the others read it from rank 0's shared memory; every
+// CTA of the cluster runs the same control flow on the same scalars.  The
+// row-width variant (NPL) is chosen per problem, so problems of every width
+// share one launch per cluster size.
+template <class P>
 __global__ void __launch_bounds__(kLsqrThreads, 2) lsqr_batched_kernel(const LsqrArgs* __restrict__ probs,
                                                                      const int* __restrict__ order, int nprob,
                                                                      int* __restrict__ next) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_i;
+  __shared__ LsqrArgs s_args;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int G = static_cast<int>(cluster.num_blocks());
+  const int rank = static_cast<int>(cluster.block_rank());
   for (;;) {
-    if (threadIdx.x == 0) s_i = atomicAdd(next, 1);
-    __syncthreads();
-    const int i = s_i;
-    __syncthreads();
+    if (rank == 0 && threadIdx.x == 0) s_i = atomicAdd(next, 1);
+    if (G > 1) cluster.sync(); else __syncthreads();
+    const int i = G > 1 ? *cluster.map_shared_rank(&s_i, 0) : s_i;
+    if (G > 1) cluster.sync(); else __syncthreads();
     if (i >= nprob) return;
-    const LsqrArgs a = probs[order[i]];
-    lsqr_dispatch<P, NPL>(a, 1, 0, smem_raw, false);
+    // the record stays in shared memory (in registers it would take ~60 of
+    // them for the whole solve)
+    if (threadIdx.x == 0) s_args = probs[order[i]];
     __syncthreads();
+    switch (lsqr_npl(s_args.n)) {
+      case 2: lsqr_body_cluster<P, 2>(s_args, G, rank, smem_raw); break;
+      case 4: lsqr_body_cluster<P, 4>(s_args, G, rank, smem_raw); break;
+      case 8: lsqr_body_cluster<P, 8>(s_args, G, rank, smem_raw); break;
+      case 16: lsqr_body_cluster<P, 16>(s_args, G, rank, smem_raw); break;
+      default: lsqr_body_cluster<P, 0>(s_args, G, rank, smem_raw); break;
+    }
+    if (G > 1) cluster.sync(); else __syncthreads();
   }
 }
 
@@ -546,14 +647,8 @@ const void* lsqr_kernel_fn(int npl) {
   }
 }
 template <class P>
-const void* lsqr_batched_fn(int npl) {
-  switch (npl) {
-    case 2: return reinterpret_cast<const void*>(lsqr_batched_kernel<P, 2>);
-    case 4: return reinterpret_cast<const void*>(lsqr_batched_kernel<P, 4>);
-    case 8: return reinterpret_cast<const void*>(lsqr_batched_kernel<P, 8>);
-    case 16: return reinterpret_cast<const void*>(lsqr_batched_kernel<P, 16>);
-    default: return reinterpret_cast<const void*>(lsqr_batched_kernel<P, 0>);
-  }
+const void* lsqr_batched_fn() {
+  return reinterpret_cast<const void*>(lsqr_batched_kernel<P>);
 }
 
 }  // namespace
@@ -747,43 +842,70 @@ extern "C" int rla_residual_df(int64_t m, int64_t n, const float* A_hi, const fl
 namespace rla {
 namespace {
 template <class P>
-int lsqr_batched_launch(const LsqrArgs* d_args, const int* d_order, int nprob, int* d_next, int64_t nmax,
-                        cudaStream_t st) {
+int lsqr_batched_launch(const LsqrArgs* d_args, const int* d_order, int nprob, int* d_next, int64_t nmax, int cluster,
+                        int max_ctas, cudaStream_t st) {
   size_t smem = lsqr_smem_bytes(nmax, sizeof(typename P::V));
   if (smem > 200 * 1024) return RLA_ERR_UNSUPPORTED;
-  const void* fn = lsqr_batched_fn<P>(lsqr_npl(nmax));
+  const void* fn = lsqr_batched_fn<P>();
   if (smem > 48 * 1024)
     RLA_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
   int per_sm = 0;
   RLA_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kLsqrThreads, smem));
-  int grid = static_cast<int>(imin(nprob, static_cast<int64_t>(imax(per_sm, 1)) * sm_count()));
+  int64_t cap = static_cast<int64_t>(imax(per_sm, 1)) * sm_count();
+  if (max_ctas > 0) cap = imin(cap, max_ctas);
+  int64_t grid = imin(static_cast<int64_t>(nprob) * cluster, cap);
+  grid = imax(cluster, grid / cluster * cluster);
   RLA_CUDA_TRY(cudaMemsetAsync(d_next, 0, sizeof(int), st));
   void* args[] = {const_cast<LsqrArgs**>(&d_args), const_cast<int**>(&d_order), &nprob, &d_next};
-  RLA_CUDA_TRY(cudaLaunchKernel(fn, dim3(grid), dim3(kLsqrThreads), args, smem, st));
+  if (cluster == 1) {
+    RLA_CUDA_TRY(cudaLaunchKernel(fn, dim3(static_cast<unsigned>(grid)), dim3(kLsqrThreads), args, smem, st));
+  } else {
+    cudaLaunchConfig_t cfg{};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = static_cast<unsigned>(cluster);
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.blockDim = dim3(kLsqrThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cfg.gridDim = dim3(static_cast<unsigned>(grid));
+    int max_clusters = 0;
+    RLA_CUDA_TRY(cudaOccupancyMaxActiveClusters(&max_clusters, fn, &cfg));
+    if (max_clusters <= 0) return RLA_ERR_UNSUPPORTED;
+    grid = imin(grid, static_cast<int64_t>(max_clusters) * cluster);
+    cfg.gridDim = dim3(static_cast<unsigned>(grid));
+    RLA_CUDA_TRY(cudaLaunchKernelExC(&cfg, fn, args));
+  }
   RLA_LAUNCH_CHECK();
   return RLA_OK;
 }
 }  // namespace
 }  // namespace rla
 
-// Size of the per-problem LSQR workspace of the batched solver (one CTA per
-// problem): vectors u (m), v, w, z (p), y, t (n), partials and barrier words.
+// Size of the per-problem LSQR workspace of the batched solver: vectors u
+// (m), v, w, z (p), y, t (n), the partials of up to kLsqrMaxCluster CTAs.
 extern "C" size_t rla_lsqr_problem_ws(int64_t m, int64_t n, int64_t p, int iter_lim) {
-  return rla::lsqr_ws_layout(m, n, p, 1, iter_lim).total;
+  return rla::lsqr_ws_layout(m, n, p, rla::kLsqrMaxCluster, iter_lim).total;
 }
 
-// Batched LSQR: `probs` is a device array of nprob rla_lsqr_problem records
-// (one CTA per problem, largest first by `order`).
-extern "C" int rla_lsqr_batched(int dtype, const void* probs, const int* order, int nprob, int64_t nmax, int* next,
-                                rla_stream_t stream) {
+// Batched LSQR: `probs` is a device array of nprob rla_lsqr_problem records,
+// solved largest first by `order`, one thread-block cluster of `cluster`
+// CTAs (1..8) per problem; at most max_ctas CTAs (0: as many as fit).
+extern "C" int rla_lsqr_batched(int dtype, const void* probs, const int* order, int nprob, int64_t nmax, int cluster,
+                                int max_ctas, int* next, rla_stream_t stream) {
   using namespace rla;
-  if (nprob < 0 || !probs || !order || !next || nmax <= 0) return RLA_ERR_ARG;
+  if (nprob < 0 || !probs || !order || !next || nmax <= 0 || cluster < 1 || cluster > kLsqrMaxCluster ||
+      max_ctas < 0)
+    return RLA_ERR_ARG;
   if (nprob == 0) return RLA_OK;
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   const auto* a = static_cast<const LsqrArgs*>(probs);
-  if (dtype == RLA_DF) return lsqr_batched_launch<Ar<df>>(a, order, nprob, next, nmax, st);
-  if (dtype == RLA_F64) return lsqr_batched_launch<Ar<double>>(a, order, nprob, next, nmax, st);
-  if (dtype == RLA_F32) return lsqr_batched_launch<ArF32D>(a, order, nprob, next, nmax, st);
+  if (dtype == RLA_DF) return lsqr_batched_launch<Ar<df>>(a, order, nprob, next, nmax, cluster, max_ctas, st);
+  if (dtype == RLA_F64) return lsqr_batched_launch<Ar<double>>(a, order, nprob, next, nmax, cluster, max_ctas, st);
+  if (dtype == RLA_F32) return lsqr_batched_launch<ArF32D>(a, order, nprob, next, nmax, cluster, max_ctas, st);
   return RLA_ERR_ARG;
 }
 
@@ -798,7 +920,7 @@ extern "C" int rla_lsqr_record(void* rec, int64_t m, int64_t n, int64_t p, const
                                double ptol, int iter_lim, int* out, double* arnorms, double* x, void* ws) {
   using namespace rla;
   if (!rec || m < 0 || n <= 0 || p <= 0 || lda < n || ldm < p || !ws || !out || !arnorms) return RLA_ERR_ARG;
-  LsqrWs L = lsqr_ws_layout(m, n, p, 1, iter_lim);
+  LsqrWs L = lsqr_ws_layout(m, n, p, kLsqrMaxCluster, iter_lim);
   char* base = static_cast<char*>(ws);
   LsqrArgs a{};
   a.m = m; a.n = n; a.p = p; a.A = A; a.Ahi = A_hi; a.Alo = A_lo; a.lda = lda; a.M = M; a.ldm = ldm;

@@ -58,6 +58,7 @@ class BatchedSPO:
         self.big_qr_n = big_qr_n
         self.big_lsqr_numel = big_lsqr_numel
         self.last_info = None
+        self.last_layout = None
 
     # ---------------------------------------------------------------- helpers
     def _sketch_qr(self, A, b, seed, mode, ctas):
@@ -94,6 +95,10 @@ class BatchedSPO:
         self._launch(plan)
         torch.cuda.synchronize()
         self.last_info = self.info_from_plan(plan)
+        # launch layout: (problems, widest n, cluster size, CTA budget) per
+        # class, and the number of problems given a cooperative launch
+        self.last_layout = dict(classes=[(c[1], c[2], c[3], c[4]) for c in plan["ls_classes"]],
+                                cooperative=len(plan["ls_big"]))
         return [it["x"] for it in plan["items"]]
 
     # ------------------------------------------------------ batched plan
@@ -199,15 +204,15 @@ class BatchedSPO:
                       K.ptr(it["Rinv"]), n, 0.0, K.ptr(b), K.ptr(it["z"]), 1, 0.0, 0.0, 0.0, float(self.ptol),
                       int(self.iter_lim), 0, K.ptr(it["out"]), K.ptr(it["arn"]), K.ptr(it["coop_ws"]),
                       C.byref(C.c_size_t(it["coop_ws"].numel())), K.stream())
-        # one persistent launch per width class (each class is its own kernel
-        # instantiation and register budget), side by side on the streams
-        for j, (ordt, cnt, nmx, nxt) in enumerate(plan["ls_classes"]):
-            s = streams[j % self.nstreams]
+        # one persistent launch per cluster size, each on its own stream with
+        # its CTA budget, so that the classes run side by side
+        cls_streams = [torch.cuda.Stream() for _ in plan["ls_classes"]]
+        for s, (ordt, cnt, nmx, g, ctas, nxt) in zip(cls_streams, plan["ls_classes"]):
             s.wait_stream(main)
             with torch.cuda.stream(s):
-                _lib.call("rla_lsqr_batched", K.MODES["df"], K.ptr(plan["ls_dev"]), K.ptr(ordt), cnt, nmx,
+                _lib.call("rla_lsqr_batched", K.MODES["df"], K.ptr(plan["ls_dev"]), K.ptr(ordt), cnt, nmx, g, ctas,
                           K.ptr(nxt), K.stream())
-        for s in streams:
+        for s in cls_streams:
             main.wait_stream(s)
         # x = R^-1 z is written by the LSQR kernels themselves; the large
         # problems' cooperative launches compute it here
@@ -233,7 +238,13 @@ class BatchedSPO:
         dev = K.device()
         order = plan["order"]
         qr_big = []
-        ls_big = [i for i in order if items[i]["m"] * items[i]["n"] >= self.big_lsqr_numel]
+        # a problem takes the whole device (cooperative launch) only when an
+        # 8-CTA cluster would leave it far behind the rest of the batch:
+        # its per-CTA share above twice the batch's per-slot share
+        nslot = 2 * torch.cuda.get_device_properties(dev).multi_processor_count
+        wall = sum((it["m"] + 2 * it["n"]) * it["n"] for it in items)
+        ls_big = [i for i in order if items[i]["m"] * items[i]["n"] >= self.big_lsqr_numel
+                  and (items[i]["m"] + 2 * items[i]["n"]) * items[i]["n"] / 8 > 2 * wall / nslot]
         qr_small = [i for i in order if i not in set(qr_big)]
         ls_small = [i for i in order if i not in set(ls_big)]
         coop_need = 0
@@ -267,17 +278,35 @@ class BatchedSPO:
         plan["order_dev"] = torch.tensor(order + [0], dtype=torch.int32, device=dev)
         plan["qr_order_dev"] = torch.tensor(qr_small + [0], dtype=torch.int32, device=dev)
         plan["ls_order_dev"] = torch.tensor(ls_small + [0], dtype=torch.int32, device=dev)
-        # width classes of the LSQR kernels (columns per lane 2 / 4 / 8 / 16 / two-pass)
-        bounds = (64, 128, 256, 512, None)
+        # LSQR launch classes, one per cluster size: each problem gets a
+        # thread-block cluster of G = 1..8 CTAs by its element count (about
+        # 2^21 elements of A per CTA and pass); the row-width variant is
+        # chosen per problem inside the kernel.  Each class is one persistent
+        # launch with a CTA budget in proportion to its share of the work
+        # (a fixed cost per row plus the elements), so that the classes run
+        # side by side and end together.
+        slots = 2 * torch.cuda.get_device_properties(dev).multi_processor_count
+        work = {i: items[i]["m"] * (items[i]["n"] + 64) + 2 * items[i]["n"] ** 2 for i in ls_small}
+        total = max(1, sum(work.values()))
+
+        def cluster_of(i):
+            e = items[i]["m"] * items[i]["n"]
+            g = 1
+            while g < 8 and e > g * (1 << 21):
+                g *= 2
+            return g
+
+        groups = {}
+        for i in ls_small:
+            groups.setdefault(cluster_of(i), []).append(i)
         classes = []
-        lo = 0
-        for hi in bounds:
-            members = [i for i in ls_small if items[i]["n"] > lo and (hi is None or items[i]["n"] <= hi)]
-            if members:
-                nmx = max(items[i]["n"] for i in members)
-                classes.append((torch.tensor(members + [0], dtype=torch.int32, device=dev), len(members), nmx,
-                                torch.zeros(1, dtype=torch.int32, device=dev)))
-            lo = hi if hi is not None else lo
+        for g, members in sorted(groups.items()):
+            wc = sum(work[i] for i in members)
+            ctas = max(g, int(slots * wc / total) // g * g)
+            ctas = min(ctas, g * len(members))
+            nmx = max(items[i]["n"] for i in members)
+            classes.append((torch.tensor(members + [0], dtype=torch.int32, device=dev), len(members), nmx, g, ctas,
+                            torch.zeros(1, dtype=torch.int32, device=dev)))
         plan["ls_classes"] = classes
         plan["next"] = torch.zeros(1, dtype=torch.int32, device=dev)
         plan["next2"] = torch.zeros(1, dtype=torch.int32, device=dev)

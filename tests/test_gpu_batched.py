@@ -51,3 +51,39 @@ def test_tuner_measures_and_caches(pg, tmp_path):
     tuner.save()
     again = pg.Tuner(path=str(tmp_path / "tune.json"))
     assert again.get("lsqr", 4096, 64) == choice
+
+
+def _check(probs, xs, infos):
+    for (A, b), x, info in zip(probs, xs, infos):
+        An, bn = A.cpu().numpy(), b.cpu().numpy()
+        xr = la.lstsq(An, bn)[0]
+        pred = la.norm(An @ (x.cpu().numpy() - xr)) / la.norm(An @ xr)
+        assert pred <= 1e-10, (A.shape, info, pred)
+        assert info["err"] == 0
+
+
+def test_batched_cluster_sizes(pg):
+    """Problems large enough for 2-, 4- and 8-CTA clusters next to one-CTA
+    problems, in every row-width class; same 1e-10 prediction bar."""
+    from parla_gb300.drivers.batched import make_problem
+    shapes = [(70000, 260, 1e8), (40000, 120, 1e6), (20000, 150, 1e9), (30000, 60, 1e10), (9000, 500, 1e7),
+              (3000, 40, 1e4), (5000, 300, 1e10), (2600, 500, 1e5), (4000, 100, 1e9), (1500, 20, 1e3)]
+    probs = [make_problem(m, n, kap, 1e-8, 300 + i)[:2] for i, (m, n, kap) in enumerate(shapes)]
+    # (in a batch this small the largest problem would otherwise take a
+    # cooperative full-device launch)
+    solver = pg.BatchedSPO(precision="mixed", streams=4, big_lsqr_numel=1 << 40)
+    xs = solver(probs, rng=5)
+    sizes = {g for _, _, g, _ in solver.last_layout["classes"]}
+    assert sizes == {1, 2, 4, 8}, solver.last_layout
+    assert solver.last_layout["cooperative"] == 0
+    _check(probs, xs, solver.last_info)
+
+
+def test_batched_single_large_problem_cooperative(pg):
+    """A batch of one large problem goes to the full-device cooperative LSQR."""
+    from parla_gb300.drivers.batched import make_problem
+    probs = [make_problem(60000, 200, 1e9, 1e-8, 77)[:2]]
+    solver = pg.BatchedSPO(precision="mixed", streams=4)
+    xs = solver(probs, rng=6)
+    assert solver.last_layout["cooperative"] == 1
+    _check(probs, xs, solver.last_info)

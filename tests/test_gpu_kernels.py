@@ -279,3 +279,50 @@ def test_chol_inv_reports_not_spd(K):
     with pytest.raises(RlaError) as ei:
         K.chol_inv_f32(dev(G))
     assert ei.value.status == 3 and "37" in str(ei.value)
+
+
+@pytest.mark.parametrize("shapes", [
+    [(37, 5, 1), (200, 23, 1), (513, 100, 1), (64, 64, 1), (9, 1, 1), (300, 17, 2)],
+    [(2048, 512, 1), (1100, 260, 1), (800, 41, 1)],
+])
+def test_geqrf_hl_batched_backward(K, shapes):
+    """Blocked double-float QR of many problems on hi/lo planes: applying the
+    returned reflectors (v, tau) to the original [A | B] in binary64 gives
+    the returned R (zeros below it) and the returned Q^T B, to 1e-13 of the
+    input norm, for widths that are and are not multiples of the panel."""
+    import ctypes as C
+    import struct
+    from parla_gb300 import _lib
+    lib = _lib.load()
+    rec = lib.rla_qr_hl_record_size()
+    rng = np.random.default_rng(11)
+    host = bytearray(rec * len(shapes))
+    mats, keep = [], []
+    for k, (m, n, nrhs) in enumerate(shapes):
+        A = rng.standard_normal((m, n + nrhs)) * np.logspace(0, -6, n + nrhs)
+        Ad = torch.from_numpy(A.T.copy()).cuda()          # column-major m x (n + nrhs)
+        hi = Ad.float()
+        lo = (Ad - hi.double()).float()
+        tau = torch.zeros(n, dtype=torch.float64, device="cuda")
+        struct.pack_into("qqqqQQQ", host, k * rec, m, n, nrhs, m, hi.data_ptr(), lo.data_ptr(), tau.data_ptr())
+        mats.append((A, hi, lo, tau, m, n, nrhs))
+    probs = torch.frombuffer(host, dtype=torch.uint8).cuda()
+    order = sorted(range(len(shapes)), key=lambda i: -shapes[i][0] * shapes[i][1])
+    order_dev = torch.tensor(order + [0], dtype=torch.int32, device="cuda")
+    nxt = torch.zeros(1, dtype=torch.int32, device="cuda")
+    mmax = max(m for m, _, _ in shapes)
+    _lib.call("rla_geqrf_hl_batched", K.ptr(probs), K.ptr(order_dev), len(shapes), mmax, K.ptr(nxt), K.stream())
+    torch.cuda.synchronize()
+    for A, hi, lo, tau, m, n, nrhs in mats:
+        F = (hi.double() + lo.double()).cpu().numpy().T      # m x (n + nrhs)
+        t = tau.cpu().numpy()
+        B = A.copy()
+        for j in range(n):
+            v = np.zeros(m)
+            v[j] = 1.0
+            v[j + 1:] = F[j + 1:, j]
+            B -= t[j] * np.outer(v, v @ B)
+        R = np.triu(F[:, :n])
+        scale = np.linalg.norm(A)
+        assert np.linalg.norm(B[:, :n] - R) / scale <= 1e-13, (m, n)
+        assert np.linalg.norm(B[:, n:] - F[:, n:]) / scale <= 1e-13, (m, n)
