@@ -272,6 +272,23 @@ def test_chol_inv_f32(K, n):
     assert np.allclose(np.tril(Rinv, -1), 0)
 
 
+@pytest.mark.parametrize("n", [64, 150, 216])
+def test_chol_inv_f32_ill_conditioned(K, n):
+    """kappa(G) = 1e6: backward error of R and R^-1 R = I to kappa(R) u."""
+    rng = np.random.default_rng(7 * n)
+    U, _ = np.linalg.qr(rng.standard_normal((2 * n, n)))
+    V, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    X = (U * np.logspace(0, -3, n)) @ V.T
+    G = (X.T @ X).astype(np.float32)
+    Rinv, R = K.chol_inv_f32(dev(G), want_r=True)
+    R = R.cpu().numpy().astype(np.float64)
+    Rinv = Rinv.cpu().numpy().astype(np.float64)
+    Gd = G.astype(np.float64)
+    assert np.linalg.norm(R.T @ R - Gd) / np.linalg.norm(Gd) <= 1e-6
+    assert np.linalg.norm(Rinv @ R - np.eye(n)) <= 1e3 * n * 6e-8
+    assert np.allclose(np.tril(Rinv, -1), 0) and np.allclose(np.tril(R, -1), 0)
+
+
 def test_chol_inv_reports_not_spd(K):
     from parla_gb300._lib import RlaError
     G = np.eye(40, dtype=np.float32)
