@@ -320,7 +320,7 @@ def _rbf_problem(N, dim=16, seed=2024):
 
 
 def bench_nystrom(torch, pg):
-    """Nystrom EVD2 (configs[3]) on the 32768 x 32768 Gaussian kernel matrix,
+    """Nystrom EVD2 on the 32768 x 32768 Gaussian kernel matrix,
     k = 512, over = 16: K S on the bf16 tensor cores (split hi + lo pair,
     fp32 accumulation), shift / S^T Y / Cholesky / SVD of B in double-float.
     The kernel matrix is built on the device by rla_rbf_kernel_matrix (timed
@@ -415,7 +415,7 @@ def bench_learned(torch, n_eval):
 
 
 def bench_ls_single(torch, pg):
-    """Sketch-and-precondition LS as the reference runs it (configs[0]):
+    """Sketch-and-precondition LS as the reference runs it (20000 x 200, kappa 1e8):
     A 20000 x 200, kappa 1e8, Gaussian sketch d = 4n, QR preconditioner,
     tolerance 1e-12; plain FP64 GPU path vs the double-float path.
     Gated error: ||A (x - x_lapack)|| / ||A x_lapack|| (x_lapack: FP64 LAPACK on the host)."""
@@ -444,7 +444,7 @@ def bench_ls_single(torch, pg):
 
 
 def bench_ls_batched(torch, pg, count):
-    """Batched LS (configs[2]): `count` problems, m log-uniform [2048, 65536],
+    """Batched LS: `count` problems, m log-uniform [2048, 65536],
     n uniform [16, 512], m >= 16 n, kappa log-uniform [1e4, 1e10], noise 1e-8;
     SJLT d = 4n, 8 nonzeros; stop at prediction error ~3e-11.  The batched
     solver replays one CUDA graph; the plain FP64 GPU path solves the problems
@@ -618,13 +618,13 @@ def main():
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--no-ls", dest="ls", action="store_false", default=True,
-                    help="skip the least-squares measurements (configs[0] and configs[2])")
+                    help="skip the least-squares measurements (single SPO and the batched solver)")
     ap.add_argument("--ls-problems", type=int, default=1024)
     ap.add_argument("--no-learned", dest="learned", action="store_false", default=True,
-                    help="skip the learned-sketch evaluation (configs[4])")
+                    help="skip the learned-sketch evaluation")
     ap.add_argument("--learned-eval", type=int, default=1024)
     ap.add_argument("--no-nystrom", dest="nystrom", action="store_false", default=True,
-                    help="skip the Nystrom EVD2 measurement (configs[3])")
+                    help="skip the Nystrom EVD2 measurement")
     args = ap.parse_args()
     if args.case:
         run_case(args)

@@ -11,7 +11,8 @@
 // of the accumulator is row i of D, so a warp's 32 lanes write 32 consecutive
 // floats of a row of D^T (coalesced).
 //
-// One CTA per 128 x N_tile output tile (N_tile <= 256, multiple of 16), six
+// One CTA per bm x N_tile output tile (N_tile <= 256, multiple of 16; bm = 128,
+// or fewer rows when that fills more SMs: the MMA runs 128 rows regardless), six
 // warps: warp 0 issues TMA loads, warp 1 owns TMEM and issues the MMAs from
 // one thread, warps 2-5 (one per TMEM lane quadrant) run the epilogue.
 // Split-K over gridDim.z writes fp32 partials that a second kernel sums in a
@@ -124,6 +125,7 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
 
 struct TcParams {
   int64_t M, N, K;
+  int bm;            // rows of X per CTA (<= kBM; the MMA always runs 128 rows)
   int n_tile;        // columns of W per CTA (multiple of 16, <= 256)
   int stages;
   int kblocks_per_split;
@@ -151,8 +153,10 @@ gemm_tc_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_constant
   const int a_bytes = kBM * kBK * 2;
   const int b_bytes = p.n_tile * kBK * 2;
   const int stage_bytes = a_bytes + b_bytes;
+  // bytes the two TMA boxes deliver per stage (X box: bm rows)
+  const int tx_bytes = p.bm * kBK * 2 + b_bytes;
 
-  const int64_t m0 = static_cast<int64_t>(blockIdx.x) * kBM;
+  const int64_t m0 = static_cast<int64_t>(blockIdx.x) * p.bm;
   const int64_t n0 = static_cast<int64_t>(blockIdx.y) * p.n_tile;
   const int64_t total_kb = ceil_div(p.K, kBK);
   const int64_t kb0 = static_cast<int64_t>(blockIdx.z) * p.kblocks_per_split;
@@ -186,7 +190,7 @@ gemm_tc_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_constant
       ++issued;
       uint8_t* sa = smem + s * stage_bytes;
       uint8_t* sb = sa + a_bytes;
-      mbar_expect_tx(&full_bar[s], static_cast<uint32_t>(stage_bytes));
+      mbar_expect_tx(&full_bar[s], static_cast<uint32_t>(tx_bytes));
       const int kc = static_cast<int>((kb0 + i) * kBK);
       tma_load_2d(sa, &tmap_x, &full_bar[s], kc, static_cast<int>(m0));
       tma_load_2d(sb, &tmap_w, &full_bar[s], kc, static_cast<int>(n0));
@@ -224,6 +228,7 @@ gemm_tc_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_constant
     // ---------------- epilogue: TMEM -> registers -> global
     const int q = warp & 3;  // TMEM lane quadrant this warp may access
     const int64_t row = m0 + q * 32 + lane;
+    const bool own = q * 32 + lane < p.bm;  // accumulator rows past bm belong to no output
     bool ok = nkb > 0 ? mbar_wait(&acc_bar, 0, p.err) : true;
     tc_fence_after();
     if (ok) {
@@ -235,7 +240,7 @@ gemm_tc_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_constant
 #pragma unroll
           for (int t = 0; t < 16; ++t) v[t] = 0.f;
         }
-        if (row < p.M) {
+        if (own && row < p.M) {
 #pragma unroll
           for (int t = 0; t < 16; ++t) {
             const int64_t col = n0 + c + t;
@@ -306,7 +311,7 @@ int make_map(CUtensorMap* map, const void* base, int64_t rows, int64_t cols, int
 }
 
 struct TcPlan {
-  int n_tile, stages, splits, kbps;
+  int bm, n_tile, stages, splits, kbps;
   int64_t tiles_m, tiles_n;
   size_t smem, ws;
 };
@@ -330,6 +335,23 @@ TcPlan tc_plan(int64_t M, int64_t N, int64_t K, int want_splits) {
   splits = static_cast<int>(imax(1, imin(splits, total_kb)));
   p.kbps = static_cast<int>(ceil_div(total_kb, splits));
   p.splits = static_cast<int>(ceil_div(total_kb, p.kbps));
+  // balanced row tiles: when one wave of 128-row tiles leaves SMs idle, give
+  // each CTA about M / (SMs / (tiles_n x splits)) rows (a multiple of 4, at
+  // least 64) so the stream of X covers every SM; the MMA still runs 128 rows
+  // and the epilogue drops the rest
+  p.bm = kBM;
+  {
+    const int64_t sms = sm_count();
+    const int64_t per = p.tiles_n * p.splits;
+    if (p.tiles_m * per < sms && per <= sms) {
+      const int64_t want_m = sms / per;
+      const int64_t bm = imin(kBM, imax(64, ceil_div(ceil_div(M, want_m), 4) * 4));
+      if (bm < kBM) {
+        p.bm = static_cast<int>(bm);
+        p.tiles_m = ceil_div(M, bm);
+      }
+    }
+  }
   p.smem = static_cast<size_t>(p.stages) * stage_bytes + 1024;
   p.ws = (p.splits > 1 ? static_cast<size_t>(p.splits) * M * N * sizeof(float) : 0) + 256;
   return p;
@@ -371,14 +393,14 @@ extern "C" int rla_gemm_bf16_tc(int64_t M, int64_t N, int64_t K, const void* X, 
     }
   }
   CUtensorMap mx, mw;
-  int rc = make_map(&mx, X, M, K, ldx, kBM);
+  int rc = make_map(&mx, X, M, K, ldx, pl.bm);
   if (rc) return rc;
   rc = make_map(&mw, W, N, K, ldw, pl.n_tile);
   if (rc) return rc;
   int* err = reinterpret_cast<int*>(ws);
   RLA_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), st));
   TcParams p{};
-  p.M = M; p.N = N; p.K = K; p.n_tile = pl.n_tile; p.stages = pl.stages; p.kblocks_per_split = pl.kbps;
+  p.M = M; p.N = N; p.K = K; p.bm = pl.bm; p.n_tile = pl.n_tile; p.stages = pl.stages; p.kblocks_per_split = pl.kbps;
   p.out_trans = out_trans; p.alpha = alpha; p.beta = beta; p.D = D; p.ldd = ldd; p.err = err;
   p.part = pl.splits > 1 ? reinterpret_cast<float*>(static_cast<char*>(ws) + 256) : nullptr;
   dim3 grid(static_cast<unsigned>(pl.tiles_m), static_cast<unsigned>(pl.tiles_n), static_cast<unsigned>(pl.splits));
