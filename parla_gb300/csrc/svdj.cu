@@ -325,6 +325,251 @@ __global__ void __launch_bounds__(512, 1) svd_jacobi_f32_kernel(JacArgs a) {
   cluster.sync();  // peers read rank 0's shared memory above
 }
 
+// ------------------------------------- block one-sided Jacobi (cluster)
+// The columns form 2 cs blocks of b; CTA k of the cluster holds two blocks
+// (top, bottom).  A sweep is 2 cs - 1 outer rounds.  In the first, each CTA
+// runs a full round-robin (circle) sweep over its 2 b columns (the pairs
+// inside both blocks and across them); in the others it rotates the b x b
+// cross pairs of its two blocks in b local rounds, pairs (A_i, B_(i+r) mod b).
+// Local rounds rotate in place and end with a block barrier; between outer
+// rounds the blocks move along the same ring as the columns of the column
+// kernel (top[0] stays, top[k] -> top[k+1], top[P-1] -> bottom[P-1],
+// bottom[k] -> bottom[k-1], bottom[0] -> top[1]) through distributed shared
+// memory, one cluster barrier.  Every pair of columns meets once per sweep,
+// with 2 cs - 1 cluster barriers instead of ~n.
+struct JacBArgs {
+  int n, b, cs;
+  const float* Ct;
+  int64_t ldc;
+  float* U;
+  int64_t ldu;
+  float* s;
+  int* info;
+  int max_sweeps;
+  float tol;
+};
+
+template <int E>
+__global__ void __launch_bounds__(512, 1) svd_jacobi_block_kernel(JacBArgs a) {
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = static_cast<int>(cluster.block_rank());
+  const int tid = threadIdx.x, lane = tid & 31, hl = lane & 15, half = lane >> 4, warp = tid >> 5;
+  const int hw = 2 * warp + half;
+  constexpr int LD = 16 * E + 8;
+  const int b = a.b, b2 = 2 * b, N = 2 * a.cs * b;
+  extern __shared__ __align__(16) float sm[];
+  float* cols = sm;                                                   // [2 buf][2b slots][LD]
+  int* ids = reinterpret_cast<int*>(cols + 2 * b2 * LD);              // [2 buf][2b]
+  unsigned* total = reinterpret_cast<unsigned*>(ids + 2 * b2);        // [4] (rank 0)
+  float* sig = reinterpret_cast<float*>(total + 4);                   // [N] (rank 0)
+  auto slot = [&](int buf, int sl) { return cols + (buf * b2 + sl) * LD; };
+
+  for (int sl = hw; sl < b2; sl += 2 * (blockDim.x >> 5)) {
+    const int c = (2 * rank + (sl >= b ? 1 : 0)) * b + (sl >= b ? sl - b : sl);
+    float* dst = slot(0, sl);
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      const int i = hl + 16 * e;
+      dst[i] = (c < a.n && i < a.n) ? a.Ct[static_cast<int64_t>(c) * a.ldc + i] : 0.f;
+    }
+    if (hl == 0) ids[sl] = c;
+  }
+  if (rank == 0 && tid == 0) *total = 0u;
+  // ring destinations of this CTA's top and bottom blocks (P = cs block pairs)
+  const int P = a.cs;
+  int tk, ttb, bk, btb;
+  if (rank == 0) { tk = 0; ttb = 0; }
+  else if (rank < P - 1) { tk = rank + 1; ttb = 0; }
+  else { tk = rank; ttb = 1; }
+  if (rank == 0) { bk = P > 1 ? 1 : 0; btb = P > 1 ? 0 : 1; }
+  else { bk = rank - 1; btb = 1; }
+  float* rcols_t = cluster.map_shared_rank(cols, tk);
+  float* rcols_b = cluster.map_shared_rank(cols, bk);
+  int* rids_t = cluster.map_shared_rank(ids, tk);
+  int* rids_b = cluster.map_shared_rank(ids, bk);
+  unsigned* total0 = cluster.map_shared_rank(total, 0);
+  cluster.sync();
+
+  const float tol2 = a.tol * a.tol;
+  unsigned seen = 0, rotated = 0;
+  int cur = 0, sweeps = 0;
+  bool converged = false;
+  while (!converged && sweeps < a.max_sweeps) {
+    for (int orr = 0; orr < 2 * P - 1; ++orr) {
+      const int lrounds = orr == 0 ? b2 - 1 : b;
+      for (int r = 0; r < lrounds; ++r) {
+        const bool act = hw < b;
+        int ps, qs;
+        if (orr == 0) {
+          ps = hw == 0 ? 0 : 1 + (hw - 1 + r) % (b2 - 1);
+          qs = 1 + (b2 - 2 - hw + r) % (b2 - 1);
+        } else {
+          ps = hw;
+          qs = b + (hw + r) % b;
+        }
+        float* sx = slot(cur, act ? ps : 0);
+        float* sy = slot(cur, act ? qs : 0);
+        float x[E], y[E];
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+          x[e] = act ? sx[hl + 16 * e] : 0.f;
+          y[e] = act ? sy[hl + 16 * e] : 0.f;
+        }
+        float app0 = 0.f, aqq0 = 0.f, apq0 = 0.f, app1 = 0.f, aqq1 = 0.f, apq1 = 0.f;
+#pragma unroll
+        for (int e = 0; e < E; e += 2) {
+          app0 = fmaf(x[e], x[e], app0);
+          aqq0 = fmaf(y[e], y[e], aqq0);
+          apq0 = fmaf(x[e], y[e], apq0);
+          if (e + 1 < E) {
+            app1 = fmaf(x[e + 1], x[e + 1], app1);
+            aqq1 = fmaf(y[e + 1], y[e + 1], aqq1);
+            apq1 = fmaf(x[e + 1], y[e + 1], apq1);
+          }
+        }
+        float app = app0 + app1, aqq = aqq0 + aqq1, apq = apq0 + apq1;
+#pragma unroll
+        for (int o = 8; o > 0; o >>= 1) {
+          app += __shfl_xor_sync(0xffffffffu, app, o);
+          aqq += __shfl_xor_sync(0xffffffffu, aqq, o);
+          apq += __shfl_xor_sync(0xffffffffu, apq, o);
+        }
+        app = __shfl_sync(0xffffffffu, app, half * 16);
+        aqq = __shfl_sync(0xffffffffu, aqq, half * 16);
+        apq = __shfl_sync(0xffffffffu, apq, half * 16);
+        if (act && apq * apq > tol2 * app * aqq) {
+          const float d = aqq - app;
+          const float den = fabsf(d) + sqrtf(fmaf(d, d, 4.f * apq * apq));
+          const float t = copysignf(1.f, d) * (2.f * apq) / den;
+          const float x1 = fmaf(t, t, 1.f);
+          float c = rsqrtf(x1);
+          c = c * fmaf(-0.5f * x1, c * c, 1.5f);
+          const float sn = t * c;
+          const float tau = sn * __frcp_rn(1.f + c);
+          // x' = x - s (y + tau x), y' = y + s (x - tau y), tau = tan(theta/2)
+#pragma unroll
+          for (int e = 0; e < E; ++e) {
+            const float xe = x[e], ye = y[e];
+            sx[hl + 16 * e] = fmaf(-sn, fmaf(tau, xe, ye), xe);
+            sy[hl + 16 * e] = fmaf(sn, fmaf(-tau, ye, xe), ye);
+          }
+          if (hl == 0) ++rotated;
+        }
+        __syncthreads();
+      }
+      if (P > 1) {
+        const int nxt = cur ^ 1;
+        const float4* st = reinterpret_cast<const float4*>(slot(cur, 0));
+        const float4* sb = reinterpret_cast<const float4*>(slot(cur, b));
+        float4* dt = reinterpret_cast<float4*>(rcols_t + (nxt * b2 + ttb * b) * LD);
+        float4* db = reinterpret_cast<float4*>(rcols_b + (nxt * b2 + btb * b) * LD);
+        const int nv = b * LD / 4;
+        for (int e = tid; e < nv; e += blockDim.x) {
+          dt[e] = st[e];
+          db[e] = sb[e];
+        }
+        for (int e = tid; e < b; e += blockDim.x) {
+          rids_t[nxt * b2 + ttb * b + e] = ids[cur * b2 + e];
+          rids_b[nxt * b2 + btb * b + e] = ids[cur * b2 + b + e];
+        }
+        cluster.sync();
+        cur = nxt;
+      }
+    }
+    ++sweeps;
+    if (rotated) atomicAdd(total0, rotated);
+    rotated = 0;
+    cluster.sync();
+    const unsigned now = *total0;  // same value in every thread of the cluster
+    converged = (now == seen);
+    seen = now;
+    cluster.sync();  // all reads done before the next sweep adds again
+  }
+
+  // singular values: norms of the final columns; rank them (descending)
+  for (int sb = 2 * warp; sb < b2; sb += 2 * (blockDim.x >> 5)) {
+    const int sl = sb + half;
+    const bool act = sl < b2;
+    float nn = 0.f;
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      const float v = act ? slot(cur, sl)[hl + 16 * e] : 0.f;
+      nn = fmaf(v, v, nn);
+    }
+#pragma unroll
+    for (int o = 8; o > 0; o >>= 1) nn += __shfl_xor_sync(0xffffffffu, nn, o);
+    nn = __shfl_sync(0xffffffffu, nn, half * 16);
+    if (act && hl == 0) {
+      const int id = ids[cur * b2 + sl];
+      cluster.map_shared_rank(sig, 0)[id] = id < a.n ? sqrtf(nn) : -1.f;
+    }
+  }
+  cluster.sync();
+  const float* sig0 = cluster.map_shared_rank(sig, 0);
+  for (int sb = 2 * warp; sb < b2; sb += 2 * (blockDim.x >> 5)) {
+    const int sl = sb + half;
+    const int id = sl < b2 ? ids[cur * b2 + sl] : a.n;
+    const bool act = id < a.n;
+    const float sv = act ? sig0[id] : 0.f;
+    int cnt = 0;
+    if (act)
+      for (int i = hl; i < N; i += 16) {
+        const float o = sig0[i];
+        cnt += (o > sv || (o == sv && i < id)) ? 1 : 0;
+      }
+#pragma unroll
+    for (int o = 8; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    if (act) {
+      const float* col = slot(cur, sl);
+      const float inv = sv > 0.f ? 1.f / sv : 0.f;
+#pragma unroll
+      for (int e = 0; e < E; ++e) {
+        const int i = hl + 16 * e;
+        if (i < a.n) a.U[static_cast<int64_t>(i) * a.ldu + cnt] = col[i] * inv;
+      }
+      if (hl == 0) a.s[cnt] = sv;
+    }
+  }
+  if (rank == 0 && tid == 0) {
+    a.info[0] = converged ? 0 : 1;
+    a.info[1] = sweeps;
+  }
+  cluster.sync();  // peers read rank 0's shared memory above
+}
+
+template <int E>
+int launch_jacobi_block(JacBArgs a, cudaStream_t st) {
+  constexpr int LD = 16 * E + 8;
+  const int N = 2 * a.cs * a.b;
+  const size_t smem = static_cast<size_t>(2 * 2 * a.b) * LD * sizeof(float) + 2 * 2 * a.b * sizeof(int) +
+                      4 * sizeof(unsigned) + static_cast<size_t>(N) * sizeof(float);
+  if (smem > 225 * 1024) return RLA_ERR_UNSUPPORTED;
+  const int threads = 32 * (a.b < 4 ? 2 : (a.b + 1) / 2);
+  if (threads > 512) return RLA_ERR_UNSUPPORTED;
+  static thread_local int attr_dev = -1;
+  int dev = 0;
+  RLA_CUDA_TRY(cudaGetDevice(&dev));
+  if (attr_dev != dev) {
+    RLA_CUDA_TRY(cudaFuncSetAttribute(svd_jacobi_block_kernel<E>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      225 * 1024));
+    attr_dev = dev;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(a.cs, 1, 1);
+  cfg.blockDim = dim3(threads, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = a.cs;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  RLA_CUDA_TRY(cudaLaunchKernelEx(&cfg, svd_jacobi_block_kernel<E>, a));
+  return RLA_OK;
+}
+
 template <int E>
 int launch_jacobi(JacArgs a, int cs, int threads, cudaStream_t st) {
   const size_t smem = (static_cast<size_t>(4) * a.ppc * JacLayout<E>::kSlot) * sizeof(float) +
@@ -392,11 +637,41 @@ extern "C" int rla_svd_jacobi(int dtype, int64_t n, const void* Ct, int64_t ldc,
   RLA_CUDA_TRY(cudaMemsetAsync(info, 0, 2 * sizeof(int), st));
   if (n == 0) return RLA_OK;
   if (!Ct || !U || !s) return RLA_ERR_ARG;
+  if (cluster == 0) {
+    // block Jacobi: up to 8 CTAs, two blocks of b columns each
+    JacBArgs ab;
+    ab.n = static_cast<int>(n);
+    ab.cs = static_cast<int>(n <= 28 ? 1 : (n + 27) / 28);
+    if (ab.cs > kJacMaxCluster) ab.cs = kJacMaxCluster;
+    ab.b = static_cast<int>((n + 2 * ab.cs - 1) / (2 * ab.cs));
+    ab.Ct = static_cast<const float*>(Ct);
+    ab.ldc = ldc;
+    ab.U = static_cast<float*>(U);
+    ab.ldu = ldu;
+    ab.s = static_cast<float*>(s);
+    ab.info = info;
+    ab.max_sweeps = max_sweeps;
+    ab.tol = 2.0f * 5.96e-8f * sqrtf(static_cast<float>(n));
+    const int ept = static_cast<int>((n + 15) / 16);
+    if (ept <= 1) return launch_jacobi_block<1>(ab, st);
+    if (ept <= 2) return launch_jacobi_block<2>(ab, st);
+    if (ept <= 4) return launch_jacobi_block<4>(ab, st);
+    if (ept <= 6) return launch_jacobi_block<6>(ab, st);
+    if (ept <= 8) return launch_jacobi_block<8>(ab, st);
+    if (ept <= 10) return launch_jacobi_block<10>(ab, st);
+    if (ept <= 12) return launch_jacobi_block<12>(ab, st);
+    if (ept <= 14) return launch_jacobi_block<14>(ab, st);
+    if (ept <= 16) return launch_jacobi_block<16>(ab, st);
+    if (ept <= 20) return launch_jacobi_block<20>(ab, st);
+    if (ept <= 24) return launch_jacobi_block<24>(ab, st);
+    return launch_jacobi_block<28>(ab, st);
+  }
   JacArgs a;
   a.n = static_cast<int>(n);
   a.P = static_cast<int>((n + 1) / 2);
-  // default: about 14 pairs (7 warps) per CTA, at most 8 CTAs (portable cluster size)
-  int cs = cluster > 0 ? cluster : (a.P + 13) / 14;
+  // explicit cluster size: the column kernel, one column pair per half-warp,
+  // about 14 pairs (7 warps) per CTA
+  int cs = cluster;
   cs = cs < 1 ? 1 : (cs > kJacMaxCluster ? kJacMaxCluster : cs);
   a.ppc = (a.P + cs - 1) / cs;
   cs = (a.P + a.ppc - 1) / a.ppc;

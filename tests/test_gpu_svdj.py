@@ -50,11 +50,15 @@ def test_potrf_df_small_reports_pivot(K):
     assert int(flag.item()) == 4
 
 
-@pytest.mark.parametrize("n", [1, 2, 3, 31, 33, 100, 210, 300, 448])
-def test_svd_jacobi_random(K, n):
+@pytest.mark.parametrize("n,cluster", [(1, 0), (2, 0), (3, 0), (28, 0), (29, 0), (31, 0), (33, 0), (100, 0),
+                                       (210, 0), (300, 0), (448, 0), (33, 2), (210, 8), (448, 8)])
+def test_svd_jacobi_random(K, n, cluster):
+    """cluster=0: block Jacobi (two column blocks per CTA, block barriers
+    inside an outer round); cluster > 0: the column kernel (ring exchange of
+    single columns every round)."""
     rng = np.random.default_rng(100 + n)
     C = rng.standard_normal((n, n)).astype(np.float32)
-    U, s, info = K.svd_jacobi(torch.from_numpy(C.T.copy()).cuda())
+    U, s, info = K.svd_jacobi(torch.from_numpy(C.T.copy()).cuda(), cluster=cluster)
     U, s, info = U.cpu().numpy().astype(float), s.cpu().numpy().astype(float), info.cpu().numpy()
     sl = np.linalg.svd(C.astype(float), compute_uv=False)
     assert info[0] == 0 and 1 <= info[1] <= 20
