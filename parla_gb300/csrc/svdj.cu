@@ -336,7 +336,8 @@ __global__ void __launch_bounds__(512, 1) svd_jacobi_f32_kernel(JacArgs a) {
 // kernel (top[0] stays, top[k] -> top[k+1], top[P-1] -> bottom[P-1],
 // bottom[k] -> bottom[k-1], bottom[0] -> top[1]) through distributed shared
 // memory, one cluster barrier.  Every pair of columns meets once per sweep,
-// with 2 cs - 1 cluster barriers instead of ~n.
+// with 2 cs - 1 cluster barriers instead of ~n.  Lane l of a half-warp holds
+// rows l E .. l E + E - 1 of a column (64-bit shared-memory accesses).
 struct JacBArgs {
   int n, b, cs;
   const float* Ct;
@@ -348,6 +349,33 @@ struct JacBArgs {
   int max_sweeps;
   float tol;
 };
+
+// A lane's E consecutive elements of a column slot: 64-bit shared-memory
+// accesses when E is even (slots start on 32-byte boundaries).
+template <int E>
+__device__ __forceinline__ void jac_load(float (&v)[E], const float* p, bool act) {
+  if constexpr (E % 2 == 0) {
+#pragma unroll
+    for (int e = 0; e < E; e += 2) {
+      const float2 w = act ? reinterpret_cast<const float2*>(p)[e / 2] : make_float2(0.f, 0.f);
+      v[e] = w.x;
+      v[e + 1] = w.y;
+    }
+  } else {
+#pragma unroll
+    for (int e = 0; e < E; ++e) v[e] = act ? p[e] : 0.f;
+  }
+}
+template <int E>
+__device__ __forceinline__ void jac_store(float* p, const float (&v)[E]) {
+  if constexpr (E % 2 == 0) {
+#pragma unroll
+    for (int e = 0; e < E; e += 2) reinterpret_cast<float2*>(p)[e / 2] = make_float2(v[e], v[e + 1]);
+  } else {
+#pragma unroll
+    for (int e = 0; e < E; ++e) p[e] = v[e];
+  }
+}
 
 template <int E>
 __global__ void __launch_bounds__(512, 1) svd_jacobi_block_kernel(JacBArgs a) {
@@ -369,7 +397,7 @@ __global__ void __launch_bounds__(512, 1) svd_jacobi_block_kernel(JacBArgs a) {
     float* dst = slot(0, sl);
 #pragma unroll
     for (int e = 0; e < E; ++e) {
-      const int i = hl + 16 * e;
+      const int i = hl * E + e;
       dst[i] = (c < a.n && i < a.n) ? a.Ct[static_cast<int64_t>(c) * a.ldc + i] : 0.f;
     }
     if (hl == 0) ids[sl] = c;
@@ -410,11 +438,8 @@ __global__ void __launch_bounds__(512, 1) svd_jacobi_block_kernel(JacBArgs a) {
         float* sx = slot(cur, act ? ps : 0);
         float* sy = slot(cur, act ? qs : 0);
         float x[E], y[E];
-#pragma unroll
-        for (int e = 0; e < E; ++e) {
-          x[e] = act ? sx[hl + 16 * e] : 0.f;
-          y[e] = act ? sy[hl + 16 * e] : 0.f;
-        }
+        jac_load<E>(x, sx + hl * E, act);
+        jac_load<E>(y, sy + hl * E, act);
         float app0 = 0.f, aqq0 = 0.f, apq0 = 0.f, app1 = 0.f, aqq1 = 0.f, apq1 = 0.f;
 #pragma unroll
         for (int e = 0; e < E; e += 2) {
@@ -438,21 +463,27 @@ __global__ void __launch_bounds__(512, 1) svd_jacobi_block_kernel(JacBArgs a) {
         aqq = __shfl_sync(0xffffffffu, aqq, half * 16);
         apq = __shfl_sync(0xffffffffu, apq, half * 16);
         if (act && apq * apq > tol2 * app * aqq) {
+          // t = tan(theta): approximate square root and quotients are enough
+          // for the angle; c = 1/sqrt(1 + t^2) gets one Newton step, so the
+          // rotation applied (c, s = t c) is orthogonal to working precision
           const float d = aqq - app;
-          const float den = fabsf(d) + sqrtf(fmaf(d, d, 4.f * apq * apq));
-          const float t = copysignf(1.f, d) * (2.f * apq) / den;
+          const float r2 = fmaf(d, d, 4.f * apq * apq);
+          const float den = fabsf(d) + r2 * rsqrtf(r2);
+          const float t = copysignf(1.f, d) * __fdividef(2.f * apq, den);
           const float x1 = fmaf(t, t, 1.f);
           float c = rsqrtf(x1);
           c = c * fmaf(-0.5f * x1, c * c, 1.5f);
           const float sn = t * c;
-          const float tau = sn * __frcp_rn(1.f + c);
+          const float tau = __fdividef(sn, 1.f + c);
           // x' = x - s (y + tau x), y' = y + s (x - tau y), tau = tan(theta/2)
 #pragma unroll
           for (int e = 0; e < E; ++e) {
             const float xe = x[e], ye = y[e];
-            sx[hl + 16 * e] = fmaf(-sn, fmaf(tau, xe, ye), xe);
-            sy[hl + 16 * e] = fmaf(sn, fmaf(-tau, ye, xe), ye);
+            x[e] = fmaf(-sn, fmaf(tau, xe, ye), xe);
+            y[e] = fmaf(sn, fmaf(-tau, ye, xe), ye);
           }
+          jac_store<E>(sx + hl * E, x);
+          jac_store<E>(sy + hl * E, y);
           if (hl == 0) ++rotated;
         }
         __syncthreads();
@@ -493,7 +524,7 @@ __global__ void __launch_bounds__(512, 1) svd_jacobi_block_kernel(JacBArgs a) {
     float nn = 0.f;
 #pragma unroll
     for (int e = 0; e < E; ++e) {
-      const float v = act ? slot(cur, sl)[hl + 16 * e] : 0.f;
+      const float v = act ? slot(cur, sl)[hl * E + e] : 0.f;
       nn = fmaf(v, v, nn);
     }
 #pragma unroll
@@ -524,7 +555,7 @@ __global__ void __launch_bounds__(512, 1) svd_jacobi_block_kernel(JacBArgs a) {
       const float inv = sv > 0.f ? 1.f / sv : 0.f;
 #pragma unroll
       for (int e = 0; e < E; ++e) {
-        const int i = hl + 16 * e;
+        const int i = hl * E + e;
         if (i < a.n) a.U[static_cast<int64_t>(i) * a.ldu + cnt] = col[i] * inv;
       }
       if (hl == 0) a.s[cnt] = sv;
