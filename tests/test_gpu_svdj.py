@@ -30,7 +30,7 @@ def spd(n, rng, cond=1e6):
     return (Q * lam) @ Q.T
 
 
-@pytest.mark.parametrize("n", [1, 5, 64, 210, 232])
+@pytest.mark.parametrize("n", [1, 5, 16, 17, 64, 210, 216, 217, 232])
 def test_potrf_df_small_matches_lapack(K, n):
     rng = np.random.default_rng(n)
     G = spd(n, rng)
@@ -42,12 +42,13 @@ def test_potrf_df_small_matches_lapack(K, n):
     assert np.allclose(R32.cpu().numpy(), Rl.astype(np.float32), rtol=1e-6, atol=1e-7 * np.abs(Rl).max())
 
 
-def test_potrf_df_small_reports_pivot(K):
-    G = np.eye(6)
-    G[3, 3] = -1.0
+@pytest.mark.parametrize("n,bad", [(6, 3), (40, 37), (220, 200)])
+def test_potrf_df_small_reports_pivot(K, n, bad):
+    G = np.eye(n)
+    G[bad, bad] = -1.0
     flag = torch.zeros(1, dtype=torch.int32, device="cuda")
     K.potrf_df_small(torch.from_numpy(G).cuda(), info=flag)
-    assert int(flag.item()) == 4
+    assert int(flag.item()) == bad + 1
 
 
 @pytest.mark.parametrize("n,cluster", [(1, 0), (2, 0), (3, 0), (28, 0), (29, 0), (31, 0), (33, 0), (100, 0),
