@@ -402,7 +402,10 @@ __device__ __forceinline__ void lsqr_body(const LsqrArgs& a, const int G, const 
   if (a.has_x0) {
     mat_M(a.z, 1.0);
   } else {
+    // z = 0 and y = M z = 0: the first fused pass multiplies y by zero, and
+    // the workspace may hold anything (0 x NaN would poison u)
     for (int64_t c = gtid; c < a.p; c += gthreads) a.z[c] = 0.0;
+    for (int64_t j = gtid; j < a.n; j += gthreads) a.y[j] = 0.0;
   }
   RLA_SYNC();
   const double bnorm = sqrt(sum_parts<V>(a.part, G));

@@ -239,6 +239,22 @@ def test_lsqr_run_matches_oracle(K, mode, case):
     assert np.max(np.abs(arn[:k] - ref[7][:k]) / np.abs(ref[7][:k])) <= 1e-6
 
 
+@pytest.mark.parametrize("mode", ["f64", "df"])
+def test_lsqr_run_ignores_stale_workspace(K, monkeypatch, mode):
+    """No start point: the solve must not read the workspace before writing
+    it (every byte 0xFF, i.e. NaN in binary64)."""
+    rng = np.random.default_rng(5)
+    A = rng.standard_normal((600, 30))
+    b = rng.standard_normal(600)
+    M = la.inv(la.qr(A, mode="economic")[1])
+    monkeypatch.setattr(K, "workspace",
+                        lambda nb: torch.full((max(int(nb), 1),), 255, dtype=torch.uint8, device="cuda"))
+    z, istop, itn, arn = K.lsqr_run(dev(A), dev(M), dev(b), None, 0.0, 1e-12, 1e-12, 1e8, 100, mode)
+    x = M @ z.cpu().numpy()
+    xr = la.lstsq(A, b)[0]
+    assert la.norm(A @ (x - xr)) / la.norm(A @ xr) <= 1e-10
+
+
 def test_lsqr_iter_limit_one(K):
     rng = np.random.default_rng(2)
     A = rng.standard_normal((200, 10))
