@@ -131,6 +131,17 @@ int rla_gemm(int dtype, int transa, int transb, int64_t M, int64_t N, int64_t K,
              int64_t ldb, double beta, void* C, int64_t ldc, void* ws,
              size_t* ws_bytes, rla_stream_t stream);
 
+/* Symmetric product C = alpha op(A) op(A)^T + beta C (N x N): op(A) = A
+ * (N x K) for trans = 0, A^T (A is K x N) for trans = 1.  Only the tiles on
+ * and above the diagonal are computed, the others are mirrored (with
+ * beta != 0, C must be symmetric on entry).  The Gram matrices of the
+ * reference's small SVDs and CholeskyQR (`B @ B.T`, `Q.T @ Q`,
+ * parla/utils/linalg_wrappers.py, parla/drivers/svd.py:165).  Workspace
+ * protocol as rla_gemm. */
+int rla_syrk(int dtype, int trans, int64_t N, int64_t K, double alpha,
+             const void* A, int64_t lda, double beta, void* C, int64_t ldc,
+             void* ws, size_t* ws_bytes, rla_stream_t stream);
+
 /* Tensor-core GEMM (tcgen05.mma kind::f16, TMA-fed, FP32 accumulation in
  * TMEM): D (M x N, fp32) = alpha X W^T + beta D with X (M x K) and W (N x K)
  * bf16 row-major (both K-major; ldx, ldw multiples of 8, 16-byte aligned

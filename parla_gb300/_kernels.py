@@ -91,6 +91,26 @@ def _ld(t):
 
 
 # ------------------------------------------------------------------ GEMM
+def syrk(A, trans=False, mode=None):
+    """Symmetric Gram: A A^T (trans=False) or A^T A (trans=True), upper tiles
+    computed, lower tiles mirrored."""
+    if mode is None:
+        mode = "f32" if A.dtype == torch.float32 else "f64"
+    code = MODES[mode]
+    tdt = torch.float32 if code == RLA_F32 else torch.float64
+    assert A.dtype == tdt and A.dim() == 2 and A.is_contiguous()
+    N = A.shape[1] if trans else A.shape[0]
+    Kd = A.shape[0] if trans else A.shape[1]
+    out = torch.empty((N, N), dtype=tdt, device=A.device)
+    args = (code, int(trans), N, Kd, 1.0, ptr(A), _ld(A), 0.0, ptr(out), _ld(out))
+    need = size_query("rla_syrk", *args)
+    ws = workspace(need) if need else None
+    nb = C.c_size_t(need)
+    _timed(f"gemm_{mode}", 2 if need else 1, call, "rla_syrk", *args, ptr(ws) if ws is not None else None,
+           C.byref(nb) if ws is not None else None, stream())
+    return out
+
+
 def gemm(A, B, transa=False, transb=False, alpha=1.0, beta=0.0, out=None, mode=None):
     """out = alpha op(A) op(B) + beta out with the library's SIMT GEMM.
 

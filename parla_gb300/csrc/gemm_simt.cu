@@ -78,8 +78,10 @@ gemm_tile_kernel(int64_t M, int64_t N, int64_t K, int64_t kchunk, double alpha,
                  const typename P::In* __restrict__ A, int64_t lda,
                  const typename P::In* __restrict__ B, int64_t ldb, double beta,
                  typename P::Out* __restrict__ C, int64_t ldc,
-                 typename P::Part* __restrict__ part) {
+                 typename P::Part* __restrict__ part, int sym) {
   constexpr int BM = P::BM, BN = P::BN, BK = P::BK, TM = P::TM, TN = P::TN;
+  static_assert(BM == BN, "symmetric products mirror tiles");
+  if (sym && blockIdx.y > blockIdx.x) return;  // lower tile of a symmetric product
   constexpr int TX = BN / TN, TY = BM / TM, NT = TX * TY;
   constexpr int LA = BM * BK / NT, LB = BN * BK / NT;
   using Sm = typename P::Sm;
@@ -181,26 +183,38 @@ gemm_tile_kernel(int64_t M, int64_t N, int64_t K, int64_t kchunk, double alpha,
 template <typename Part, typename Out>
 __global__ void splitk_reduce_kernel(int64_t M, int64_t N, int splits, double alpha,
                                      const Part* __restrict__ part, double beta,
-                                     Out* __restrict__ C, int64_t ldc) {
+                                     Out* __restrict__ C, int64_t ldc, int sym_tile) {
   int64_t idx = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (idx >= M * N) return;
   int64_t i = idx / N, j = idx % N;
+  // symmetric product: lower tiles were not computed, read the mirror entry
+  const bool mir = sym_tile > 0 && i / sym_tile > j / sym_tile;
+  const int64_t pi = mir ? j : i, pj = mir ? i : j;
   double s = 0.0;
-  for (int z = 0; z < splits; ++z) s += static_cast<double>(part[(static_cast<int64_t>(z) * M + i) * N + j]);
+  for (int z = 0; z < splits; ++z) s += static_cast<double>(part[(static_cast<int64_t>(z) * M + pi) * N + pj]);
   double r = alpha * s;
   if (beta != 0.0) r += beta * static_cast<double>(C[i * ldc + j]);
   C[i * ldc + j] = static_cast<Out>(r);
 }
 
+// Lower tiles of a symmetric product from the upper ones (unsplit case).
+template <typename Out>
+__global__ void sym_mirror_kernel(int64_t N, Out* __restrict__ C, int64_t ldc, int tile) {
+  int64_t idx = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= N * N) return;
+  int64_t i = idx / N, j = idx % N;
+  if (i / tile > j / tile) C[i * ldc + j] = C[j * ldc + i];
+}
+
 template <class P>
 int gemm_launch(int ta, int tb, int64_t M, int64_t N, int64_t K, double alpha,
                 const void* A, int64_t lda, const void* B, int64_t ldb, double beta,
-                void* C, int64_t ldc, void* ws, size_t* ws_bytes, cudaStream_t st) {
+                void* C, int64_t ldc, void* ws, size_t* ws_bytes, cudaStream_t st, int sym = 0) {
   using In = typename P::In;
   using Out = typename P::Out;
   using Part = typename P::Part;
   const int64_t tiles_m = ceil_div(M, P::BM), tiles_n = ceil_div(N, P::BN);
-  const int64_t tiles = tiles_m * tiles_n;
+  const int64_t tiles = sym ? tiles_m * (tiles_m + 1) / 2 : tiles_m * tiles_n;
   int splits = 1;
   const int sms = sm_count();
   if (tiles < 2 * sms && K >= 512) {
@@ -231,7 +245,8 @@ int gemm_launch(int ta, int tb, int64_t M, int64_t N, int64_t K, double alpha,
   auto* b = static_cast<const In*>(B);
   auto* c = static_cast<Out*>(C);
 #define RLA_GEMM_CASE(TA_, TB_) \
-  gemm_tile_kernel<P, TA_, TB_><<<grid, block, 0, st>>>(M, N, K, kchunk, alpha, a, lda, b, ldb, beta, c, ldc, part)
+  gemm_tile_kernel<P, TA_, TB_><<<grid, block, 0, st>>>(M, N, K, kchunk, alpha, a, lda, b, ldb, beta, c, ldc, part, \
+                                                        sym)
   if (ta && tb) RLA_GEMM_CASE(true, true);
   else if (ta) RLA_GEMM_CASE(true, false);
   else if (tb) RLA_GEMM_CASE(false, true);
@@ -241,7 +256,10 @@ int gemm_launch(int ta, int tb, int64_t M, int64_t N, int64_t K, double alpha,
   if (splits > 1) {
     int64_t total = M * N;
     splitk_reduce_kernel<Part, Out><<<static_cast<unsigned>(ceil_div(total, 256)), 256, 0, st>>>(
-        M, N, splits, alpha, part, beta, c, ldc);
+        M, N, splits, alpha, part, beta, c, ldc, sym ? P::BM : 0);
+    RLA_LAUNCH_CHECK();
+  } else if (sym && tiles_m > 1) {
+    sym_mirror_kernel<Out><<<static_cast<unsigned>(ceil_div(N * N, 256)), 256, 0, st>>>(N, c, ldc, P::BM);
     RLA_LAUNCH_CHECK();
   }
   return RLA_OK;
@@ -265,6 +283,28 @@ extern "C" int rla_gemm(int dtype, int transa, int transb, int64_t M, int64_t N,
     case RLA_F32: return rla::gemm_launch<rla::PolF32>(transa, transb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, ws, ws_bytes, st);
     case RLA_F64: return rla::gemm_launch<rla::PolF64>(transa, transb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, ws, ws_bytes, st);
     case RLA_DF: return rla::gemm_launch<rla::PolDF>(transa, transb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, ws, ws_bytes, st);
+    default: return RLA_ERR_ARG;
+  }
+}
+
+// C = alpha op(A) op(A)^T + beta C (N x N) with op(A) = A (N x K, trans = 0)
+// or A^T (A is K x N, trans = 1): only the tiles on and above the diagonal
+// are computed; the lower tiles are copied from them (with beta != 0, C must
+// be symmetric on entry).
+extern "C" int rla_syrk(int dtype, int trans, int64_t N, int64_t K, double alpha, const void* A, int64_t lda,
+                        double beta, void* C, int64_t ldc, void* ws, size_t* ws_bytes, rla_stream_t stream) {
+  if (N < 0 || K < 0) return RLA_ERR_ARG;
+  const bool query = (ws == nullptr && ws_bytes != nullptr);
+  if (!query) {
+    if (N > 0 && C == nullptr) return RLA_ERR_ARG;
+    if (K > 0 && N > 0 && A == nullptr) return RLA_ERR_ARG;
+  }
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  const int ta = trans ? 1 : 0, tb = trans ? 0 : 1;
+  switch (dtype) {
+    case RLA_F32: return rla::gemm_launch<rla::PolF32>(ta, tb, N, N, K, alpha, A, lda, A, lda, beta, C, ldc, ws, ws_bytes, st, 1);
+    case RLA_F64: return rla::gemm_launch<rla::PolF64>(ta, tb, N, N, K, alpha, A, lda, A, lda, beta, C, ldc, ws, ws_bytes, st, 1);
+    case RLA_DF: return rla::gemm_launch<rla::PolDF>(ta, tb, N, N, K, alpha, A, lda, A, lda, beta, C, ldc, ws, ws_bytes, st, 1);
     default: return RLA_ERR_ARG;
   }
 }

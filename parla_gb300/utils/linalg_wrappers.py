@@ -31,7 +31,7 @@ def cholqr(Y, passes=2):
     Q = Y
     for p in range(passes):
         Q64 = Q if Q.dtype == torch.float64 else Q.to(torch.float64)
-        G = K.gemm(Q64, Q64, transa=True, mode="df")
+        G = K.syrk(Q64.contiguous(), trans=True, mode="df")
         k = G.shape[0]
         chol = (lambda X: K.potrf_df_small(X, want64=True)[1]) if k <= JACOBI_MAX else \
             (lambda X: K.potrf_upper(X.clone(), mode="df"))
@@ -97,7 +97,7 @@ def small_svd_wide(B):
     Returned in descending order.
     """
     B64 = B if B.dtype == torch.float64 else B.to(torch.float64)
-    G = K.gemm(B64, B64, transb=True, mode="df")
+    G = K.syrk(B64, mode="df")
     if B.dtype == torch.float32 and B.shape[0] <= JACOBI_MAX:
         res = _svd_from_gram(G)
         if res is not None:
@@ -116,7 +116,7 @@ def small_svd_wide(B):
 def small_svd_tall(B):
     """Thin SVD of a tall n x k device matrix B (k << n) through B^T B."""
     B64 = B if B.dtype == torch.float64 else B.to(torch.float64)
-    G = K.gemm(B64, B64, transa=True, mode="df")
+    G = K.syrk(B64, trans=True, mode="df")
     if B.dtype == torch.float32 and B.shape[1] <= JACOBI_MAX:
         res = _svd_from_gram(G)
         if res is not None:
@@ -180,7 +180,7 @@ def orth_tc(Y, passes=1):
             Yb = K.convert(Qt, torch.bfloat16)
             G = K.gemm_tc(Yb, Yb)
         else:
-            G = K.gemm(Qt, Qt, transb=True, mode="f32")
+            G = K.syrk(Qt, mode="f32")
         Rinv = _chol_inv_f32(G)
         Qt = K.gemm(Rinv, Qt, transa=True, mode="f32")
     return Qt.t()

@@ -49,6 +49,25 @@ def test_gemm(K, mode, tol, ta, tb, shape):
     assert rel(out.cpu().numpy(), ref) <= tol * (1 + np.sqrt(Kd) * (mode == "f32"))
 
 
+@pytest.mark.parametrize("mode,tol", [("f64", 1e-13), ("df", 1e-12), ("f32", 2e-5)])
+@pytest.mark.parametrize("trans", [False, True])
+@pytest.mark.parametrize("n,k", [(5, 40), (64, 300), (130, 2000), (210, 8192)])
+def test_syrk_symmetric_gram(K, mode, tol, trans, n, k):
+    """Upper tiles computed, lower tiles mirrored: equal to the full product
+    and symmetric (bitwise for binary32/64), with and without split-K."""
+    rng = np.random.default_rng(n + k)
+    A = rng.standard_normal((k, n) if trans else (n, k))
+    dt = torch.float32 if mode == "f32" else torch.float64
+    G = K.syrk(dev(A, dt), trans=trans, mode=mode).cpu().numpy().astype(np.float64)
+    Ad = A.astype(np.float32).astype(np.float64) if mode == "f32" else A
+    ref = Ad.T @ Ad if trans else Ad @ Ad.T
+    assert rel(G, ref) <= tol * max(1.0, np.sqrt(k) / 30)
+    if mode == "df":  # diagonal tiles sum the cross terms of x*y and y*x in another order
+        assert np.max(np.abs(G - G.T)) <= 1e-15 * np.max(np.abs(G))
+    else:
+        assert np.array_equal(G, G.T)
+
+
 def test_gemm_alpha_beta(K):
     rng = np.random.default_rng(3)
     A, B, Cm = rng.standard_normal((50, 40)), rng.standard_normal((40, 30)), rng.standard_normal((50, 30))
