@@ -63,7 +63,7 @@ def test_syrk_symmetric_gram(K, mode, tol, trans, n, k):
     ref = Ad.T @ Ad if trans else Ad @ Ad.T
     assert rel(G, ref) <= tol * max(1.0, np.sqrt(k) / 30)
     if mode == "df":  # diagonal tiles sum the cross terms of x*y and y*x in another order
-        assert np.max(np.abs(G - G.T)) <= 1e-15 * np.max(np.abs(G))
+        assert np.max(np.abs(G - G.T)) <= 1e-13 * np.max(np.abs(G))
     else:
         assert np.array_equal(G, G.T)
 
