@@ -18,7 +18,7 @@ reference so that the same seed yields the same sketching operator.
 from oracle.sketching import (gaussian_operator, sjlt_operator, generate_srct,
                               apply_srct, srct_apply_dense, orthonormal_operator)
 from oracle.lsqr import lsqr
-from oracle.least_squares import (dim_checks, spo, sso1, pcss2,
+from oracle.least_squares import (dim_checks, spo, sso1, pcss2, pcss2_under, spu1,
                                   svd_right_precond, SketchAndPrecondLog)
 from oracle.lowrank import orth, rs1, rf1, qb1, qb2, qb3, svd1, evd1, evd2
 

@@ -2,9 +2,9 @@
 
 Test infrastructure only (see ``oracle/__init__.py``).
 
-Restates ``parla/drivers/least_squares.py`` (dim_checks, SSO1, SPO),
+Restates ``parla/drivers/least_squares.py`` (dim_checks, SSO1, SPO, SPU1),
 ``parla/comps/preconditioning.py`` (a_lift_precond, svd_right_precond),
-``parla/comps/determiter/saddle.py`` (PcSS2, overdetermined branch) and
+``parla/comps/determiter/saddle.py`` (PcSS2, both branches) and
 ``parla/comps/determiter/logging.py`` (SketchAndPrecondLog).
 """
 import time
@@ -204,3 +204,50 @@ def sso1(A, b, delta, S, lapack_driver=None):
         a_ske = np.vstack((a_ske, np.sqrt(delta) * np.eye(n)))
         b_ske = np.concatenate((b_ske, np.zeros(n)))
     return la.lstsq(a_ske, b_ske, lapack_driver=lapack_driver)[0]
+
+
+def pcss2_under(A, c, delta, tol, iter_lim, R, upper_tri):
+    """Preconditioned LSQR for the underdetermined problem min ||y|| s.t. A'y = c.
+
+    ``parla/comps/determiter/saddle.py:203-214``: LSQR(atol=btol=tol) on the
+    transposed operator (M' [A; sqrt(delta) I]') with right-hand side M'c,
+    started at zero; y is its solution (first m entries when delta > 0) and
+    x = (A'y - c) / delta, or NaN when delta = 0.  Returns (x, y, arnorms, raw).
+    """
+    m, n = A.shape
+    matvec, rmatvec, _, madj = _precond_operator(A, delta, R, upper_tri)
+    c_pc = madj(c)
+    rows = m + (n if delta > 0 else 0)
+    res = lsqr(rmatvec, matvec, rows, c_pc, atol=tol, btol=tol, iter_lim=iter_lim)
+    y = res[0]
+    if delta > 0:
+        y = y[:m]
+        x = (A.T @ y - c) / delta
+    else:
+        x = np.full(n, np.nan)
+    return x, y, res[7], res
+
+
+def spu1(A, c, tol, iter_lim, S, logging=True):
+    """SPU1 given an already generated sketching operator S (d x m).
+
+    ``parla/drivers/least_squares.py:459-494``: sketch A, right
+    preconditioner M = V / sigma from the SVD of the sketch, then the
+    underdetermined branch of PcSS2 with delta = 0.  The log's initial error
+    is ||A M M' c|| (``:486``).  Returns (y, log, info).
+    """
+    apply = S if callable(S) else (lambda X: S @ X)
+    clock = time.perf_counter if logging else (lambda: 0.0)
+    log = SketchAndPrecondLog()
+    t0 = clock()
+    a_ske = apply(A)
+    log.time_sketch = clock() - t0
+    t0 = clock()
+    M, _, _, _ = svd_right_precond(a_ske)
+    log.time_factor = clock() - t0
+    t0 = clock()
+    _, y, errs, raw = pcss2_under(A, c, 0.0, tol, iter_lim, M, False)
+    log.time_iterate = clock() - t0
+    if logging:
+        log.wrap_up(errs, la.norm(A @ (M @ (M.T @ c))))
+    return y, log, {"M": M, "lsqr": raw}

@@ -70,3 +70,118 @@ def lsqr(A, b, damp=0.0, atol=1e-8, btol=1e-8, conlim=1e8, iter_lim=None, show=F
         print(f"LSQR (device): istop={istop} itn={itn}")
     nan = float("nan")
     return z, istop, itn, nan, nan, nan, nan, arn, nan, None
+
+
+def _givens(a, b):
+    """(c, s, r) with c a + s b = r, r >= 0 (``parla/comps/determiter/lsqr.py:63-95``)."""
+    if b == 0.0:
+        return float(np.sign(a)), 0.0, abs(a)
+    if a == 0.0:
+        return 0.0, float(np.sign(b)), abs(b)
+    if abs(b) > abs(a):
+        t = a / b
+        s = float(np.sign(b)) / np.sqrt(1.0 + t * t)
+        return s * t, s, b / s
+    t = b / a
+    c = float(np.sign(a)) / np.sqrt(1.0 + t * t)
+    return c, c * t, a / c
+
+
+def lsqr_stepped(matvec, rmatvec, n, b, atol=1e-8, btol=1e-8, conlim=1e8, iter_lim=None):
+    """LSQR for an operator given only by its two products, started at zero.
+
+    The Golub-Kahan recurrence and stopping tests of
+    ``parla/comps/determiter/lsqr.py:98-574`` (Paige & Saunders 1982) with
+    device vectors and host scalars: each iteration is one ``matvec`` and one
+    ``rmatvec`` (library GEMM products) and reads back the two norms.  Used
+    for operators the fused LSQR kernel does not cover, e.g. the transposed
+    preconditioned operator of the underdetermined solver.
+
+    Returns (x, istop, itn, r1norm, r2norm, anorm, acond, arnorms, xnorm, None).
+    """
+    if iter_lim is None:
+        iter_lim = 2 * n
+    nrm = lambda v: float(torch.linalg.vector_norm(v))
+    ctol = 1.0 / conlim if conlim > 0 else 0.0
+    eps = np.finfo(np.float64).eps
+    x = torch.zeros(n, dtype=torch.float64, device=b.device)
+    anorm = acond = ddnorm = res2 = xnorm = xxnorm = z = 0.0
+    cs2, sn2 = -1.0, 0.0
+    istop = itn = 0
+    bnorm = beta = nrm(b)
+    u = b.clone()
+    alfa = 0.0
+    v = torch.zeros_like(x)
+    if beta > 0:
+        u.mul_(1.0 / beta)
+        v = rmatvec(u)
+        alfa = nrm(v)
+    if alfa > 0:
+        v.mul_(1.0 / alfa)
+    w = v.clone()
+    rhobar, phibar = alfa, beta
+    r1norm = r2norm = beta
+    arnorm = alfa * beta
+    arnorms = []
+    if arnorm == 0:
+        return x, istop, itn, r1norm, r2norm, anorm, acond, np.array([]), xnorm, None
+    while itn < iter_lim:
+        arnorms.append(arnorm)
+        itn += 1
+        u = matvec(v).sub_(u, alpha=alfa)
+        beta = nrm(u)
+        if beta > 0:
+            u.mul_(1.0 / beta)
+            anorm = np.sqrt(anorm ** 2 + alfa ** 2 + beta ** 2)
+            v = rmatvec(u).sub_(v, alpha=beta)
+            alfa = nrm(v)
+            if alfa > 0:
+                v.mul_(1.0 / alfa)
+        # the reference's damping rotation with damp = 0 still flips the sign
+        rhobar1 = np.sqrt(rhobar ** 2)
+        phibar = (rhobar / rhobar1) * phibar
+        cs, sn, rho = _givens(rhobar1, beta)
+        theta = sn * alfa
+        rhobar = -cs * alfa
+        phi = cs * phibar
+        phibar = sn * phibar
+        tau = sn * phi
+        ddnorm += (nrm(w) / rho) ** 2
+        x.add_(w, alpha=phi / rho)
+        w = v - (theta / rho) * w
+        # ||x|| estimate through a second rotation
+        delta = sn2 * rho
+        gambar = -cs2 * rho
+        rhs = phi - delta * z
+        zbar = rhs / gambar
+        xnorm = np.sqrt(xxnorm + zbar ** 2)
+        gamma = np.sqrt(gambar ** 2 + theta ** 2)
+        cs2, sn2 = gambar / gamma, theta / gamma
+        z = rhs / gamma
+        xxnorm += z ** 2
+        acond = anorm * np.sqrt(ddnorm)
+        rnorm = np.sqrt(phibar ** 2 + res2)
+        arnorm = alfa * abs(tau)
+        r1norm = r2norm = rnorm
+        test1 = rnorm / bnorm
+        test2 = arnorm / (anorm * rnorm + eps)
+        test3 = 1.0 / (acond + eps)
+        t1 = test1 / (1.0 + anorm * xnorm / bnorm)
+        rtol = btol + atol * anorm * xnorm / bnorm
+        if itn >= iter_lim:
+            istop = 7
+        if 1.0 + test3 <= 1.0:
+            istop = 6
+        if 1.0 + test2 <= 1.0:
+            istop = 5
+        if 1.0 + t1 <= 1.0:
+            istop = 4
+        if test3 <= ctol:
+            istop = 3
+        if test2 <= atol:
+            istop = 2
+        if test1 <= rtol:
+            istop = 1
+        if istop != 0:
+            break
+    return x, istop, itn, r1norm, r2norm, anorm, acond, np.asarray(arnorms), xnorm, None

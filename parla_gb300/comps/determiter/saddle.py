@@ -1,12 +1,15 @@
-"""Preconditioned saddle-point solver PcSS2 (overdetermined branch) on the device.
+"""Preconditioned saddle-point solver PcSS2 on the device.
 
-Counterpart of ``parla/comps/determiter/saddle.py:99-217``.
+Counterpart of ``parla/comps/determiter/saddle.py:99-217``: the
+overdetermined branch (c = 0) runs the fused LSQR kernel on [A; sqrt(delta) I] M;
+the underdetermined branch (b = 0) runs LSQR on the transposed operator
+M' [A; sqrt(delta) I]' with library GEMM products.
 """
 import numpy as np
 import torch
 
 from ... import _kernels as K
-from .lsqr import PrecondOperator
+from .lsqr import PrecondOperator, lsqr_stepped
 
 
 class PrecondSaddleSolver:
@@ -30,9 +33,12 @@ class PcSS2(PrecondSaddleSolver):
 
     def __call__(self, A, b, c, delta, tol, iter_lim, R, upper_tri, z0, M=None, split=None):
         Ad = K.to_dev(A, torch.float64)
+        c_zero = c is None or float(torch.linalg.vector_norm(K.to_dev(c))) == 0.0
+        if not c_zero:
+            if b is not None and float(torch.linalg.vector_norm(K.to_dev(b))) != 0.0:
+                raise ValueError('One of "b" or "c" must be zero.')
+            return self._under(Ad, K.to_dev(c, torch.float64), delta, tol, iter_lim, R, upper_tri, M)
         bd = K.to_dev(b, torch.float64)
-        if c is not None and float(torch.linalg.vector_norm(K.to_dev(c))) != 0.0:
-            raise NotImplementedError("PcSS2 on the device covers the overdetermined case (c = 0)")
         if M is None:
             Rd = K.to_dev(R, torch.float64)
             M = K.trtri_upper(Rd, mode=self.precision) if upper_tri else Rd
@@ -44,3 +50,40 @@ class PcSS2(PrecondSaddleSolver):
         y = bd - K.gemm(Ad, x)
         self.last = dict(istop=istop, itn=itn, z=z)
         return x, y, arn
+
+    def _under(self, Ad, cd, delta, tol, iter_lim, R, upper_tri, M):
+        """min ||y|| s.t. [A; sqrt(delta) I]' y = c (``saddle.py:203-214``).
+
+        LSQR from zero on B = M' [A; sqrt(delta) I]' with right-hand side M'c;
+        y is its solution (the first m entries when delta > 0) and
+        x = (A'y - c) / delta, or NaN when delta = 0.
+        """
+        mode = "f64" if self.precision == "f32" else self.precision
+        if M is None:
+            Rd = K.to_dev(R, torch.float64)
+            M = K.trtri_upper(Rd, mode=mode) if upper_tri else Rd
+        m, n = Ad.shape
+        sd = float(np.sqrt(delta))
+        rows = m + (n if delta > 0 else 0)
+
+        def bmat(v):   # v (rows) -> M' (A' v[:m] + sd v[m:])
+            w = K.gemm(Ad, v[:m].contiguous(), transa=True, mode=mode)
+            if delta > 0:
+                w = w + sd * v[m:]
+            return K.gemm(M, w, transa=True, mode=mode)
+
+        def bmat_t(u):  # u (r) -> [A; sd I] M u
+            t = K.gemm(M, u, mode=mode)
+            out = K.gemm(Ad, t, mode=mode)
+            return torch.cat((out, sd * t)) if delta > 0 else out
+
+        c_pc = K.gemm(M, cd, transa=True, mode=mode)
+        res = lsqr_stepped(bmat, bmat_t, rows, c_pc, atol=tol, btol=tol, conlim=1e8, iter_lim=iter_lim)
+        y = res[0]
+        if delta > 0:
+            y = y[:m].contiguous()
+            x = (K.gemm(Ad, y, transa=True, mode=mode) - cd) / delta
+        else:
+            x = torch.full((n,), float("nan"), dtype=torch.float64, device=Ad.device)
+        self.last = dict(istop=res[1], itn=res[2], z=None)
+        return x, y, res[7]

@@ -215,3 +215,59 @@ class SPO(OverLstsqSolver):
             log.wrap_up(arnorms, float(torch.linalg.vector_norm(ar0)))
             log.error_desc = self.iterative_solver.ERROR_METRIC_INFO
         return K.like_input(x, A), log
+
+
+class UnderLstsqSolver:
+    """``parla/drivers/least_squares.py:372-416``: (A, c, tol, iter_lim, rng) -> (y, log)
+    for min ||y|| subject to A'y = c, A tall."""
+
+    def __call__(self, A, c, tol, iter_lim, rng, logging=False):
+        raise NotImplementedError()
+
+
+class SPU1(UnderLstsqSolver):
+    """SVD-based sketch-and-precondition for underdetermined least squares.
+
+    ``parla/drivers/least_squares.py:425-494``: sketch A (d = sf * n rows),
+    M = V / sigma from the sketch's SVD (``svd_right_precond``), then LSQR on
+    the transposed preconditioned operator (the underdetermined branch of
+    PcSS2).  The log measures ||(A M)((A M)'y - M'c)|| per iteration, starting
+    from ||A M M' c||.
+    """
+
+    def __init__(self, sketch_op_gen, sampling_factor, precision="f64"):
+        self.sketch_op_gen = sketch_op_gen
+        self.sampling_factor = sampling_factor
+        self.precision = precision
+        self.iterative_solver = PcSS2(precision)
+
+    def __call__(self, A, c, tol, iter_lim, rng, logging=True):
+        prec = self.precision
+        Ad, cd = K.to_dev(A), K.to_dev(c)
+        m, n = Ad.shape
+        d = dim_checks(self.sampling_factor, m, n)
+        rng = np.random.default_rng(rng)
+        clock = _clock(logging)
+        log = SketchAndPrecondLog()
+        tic = clock()
+        S = self.sketch_op_gen(d, m, rng)
+        A_ske = _apply(S, Ad, prec)
+        log.time_sketch = clock() - tic
+        tic = clock()
+        M, U, sigma, Vh = svd_right_precond(A_ske, prec)
+        log.time_factor = clock() - tic
+        tic = clock()
+        x, y, arnorms = self.iterative_solver(Ad, None, cd, 0.0, tol, iter_lim, M, False, None, M=M)
+        log.time_iterate = clock() - tic
+        info = self.iterative_solver.last
+        log.istop, log.itn = info["istop"], info["itn"]
+        if logging:
+            mode = "f64" if prec == "f32" else prec
+            e0 = K.gemm(Ad, K.gemm(M, K.gemm(M, cd, transa=True, mode=mode), mode=mode), mode=mode)
+            log.wrap_up(arnorms, float(torch.linalg.vector_norm(e0)))
+            log.error_desc = """
+            The logs produced by this algorithm measure error as
+                || (A M) (A M)' y - (A M) (M' c) ||_2,
+            where "M" is a right-preconditioner for A.
+            """
+        return K.like_input(y, A), log

@@ -2,7 +2,7 @@
 
 Run in a container that holds the reference source tree::
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py /root/reference [fixture names ...]
 
 The reference targets NumPy 1.x; two names it uses were removed in NumPy 2
 (``np.NaN`` and ``np.row_stack``), so they are restored as aliases before the
@@ -124,6 +124,37 @@ def spo_cases(parla):
     return out
 
 
+def spu_cases(parla):
+    """SPU1 (underdetermined LS) as the reference's own tests set it up:
+    A = U diag(spectrum) V' of full column rank, c = A' y0."""
+    import parla.comps.sketchers.oblivious as sko
+    import parla.utils.sketching as usk
+    from parla.drivers.least_squares import SPU1
+    out = {}
+    for tag, (m, n, kind, cond, gen, seed) in {
+            'lin': (300, 30, 'lin', 1e5, 'sj', 51),
+            'log': (400, 25, 'log', 1e5, 'ga', 52),
+            'tight': (200, 20, 'lin', 1e3, 'sj', 53)}.items():
+        rng = np.random.default_rng(seed)
+        if kind == 'lin':
+            spec = np.linspace(cond ** 0.5, cond ** -0.5, num=n)
+        else:
+            spec = np.logspace(np.log10(cond) / 2, -np.log10(cond) / 2, num=n)
+        U = usk.orthonormal_operator(m, n, rng)
+        Vt = usk.orthonormal_operator(n, n, rng)
+        A = (U * spec) @ Vt
+        c = A.T @ rng.standard_normal(m)
+        alg = SPU1(sko.SkOpSJ(8) if gen == 'sj' else sko.SkOpGA(), 3)
+        tol, lim = (0.0, n) if tag == 'tight' else (1e-12, 50)
+        y, log = alg(A, c, tol, lim, np.random.default_rng(seed + 100))
+        out[f'{tag}_A'], out[f'{tag}_c'] = A, c
+        out[f'{tag}_gen'] = np.array(gen)
+        out[f'{tag}_seed'] = np.array(seed + 100)
+        out[f'{tag}_tol'], out[f'{tag}_lim'] = np.array(tol), np.array(lim)
+        out[f'{tag}_y'], out[f'{tag}_errors'] = y, log.errors
+    return out
+
+
 def lowrank_cases(parla):
     import parla.comps.sketchers.oblivious as sko
     from parla.comps.sketchers.aware import RS1
@@ -186,12 +217,16 @@ def lowrank_cases(parla):
     return out
 
 
-def main(ref_path):
+def main(ref_path, only=None):
+    """Write every fixture, or only those named in ``only``."""
     parla = _import_reference(ref_path)
     meta = dict(numpy=np.__version__, scipy=scipy.__version__,
                 parla=parla.__version__)
     for name, fn in (('sketch', sketches), ('lsqr', lsqr_case),
-                     ('spo', spo_cases), ('lowrank', lowrank_cases)):
+                     ('spo', spo_cases), ('spu', spu_cases),
+                     ('lowrank', lowrank_cases)):
+        if only and name not in only:
+            continue
         data = fn(parla)
         data['_versions'] = np.array(repr(meta))
         path = os.path.join(HERE, f'{name}.npz')
@@ -200,4 +235,4 @@ def main(ref_path):
 
 
 if __name__ == '__main__':
-    main(sys.argv[1] if len(sys.argv) > 1 else '/root/reference')
+    main(sys.argv[1] if len(sys.argv) > 1 else '/root/reference', sys.argv[2:])

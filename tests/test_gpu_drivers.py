@@ -101,6 +101,44 @@ def test_sso1(pg, golden):
     assert pred_err(A, x, g["sso_x"]) <= 1e-9
 
 
+@pytest.mark.parametrize("tag", ["lin", "log", "tight"])
+@pytest.mark.parametrize("precision", ["f64", "df"])
+def test_spu1_matches_reference(pg, golden, tag, precision):
+    """Underdetermined LS (min ||y|| s.t. A'y = c): the device SPU1 with the
+    reference's own sketch draws against the reference's y; the reference's
+    property checks (test_underdet_least_squares.py:50-75) at 1e-6."""
+    g = golden("spu")
+    A, c = g[f"{tag}_A"], g[f"{tag}_c"]
+    gen = str(g[f"{tag}_gen"])
+    skop = pg.SkOpSJ(8, seed_compat=True) if gen == "sj" else pg.SkOpGA(seed_compat=True)
+    y, log = pg.SPU1(skop, 3, precision=precision)(A, c, float(g[f"{tag}_tol"]), int(g[f"{tag}_lim"]),
+                                                   int(g[f"{tag}_seed"]))
+    ref = g[f"{tag}_y"]
+    assert isinstance(y, np.ndarray) and y.shape == ref.shape
+    assert la.norm(y - ref) <= 1e-9 * la.norm(ref)
+    s0 = la.norm(A, 2)
+    assert la.norm(A.T @ y - c) / s0 <= 1e-6
+    assert la.norm(y) <= la.norm(ref) + 1e-6 * s0
+    assert log.errors.size >= 2 and log.errors[-1] <= 1e-6 * log.errors[0]
+
+
+def test_spu1_ridge_branch_and_errors(pg):
+    """PcSS2's underdetermined branch with delta > 0 returns x = (A'y - c)/delta
+    and y minimising ||y||^2 + ||x||^2 delta-weighted as in the oracle; b and c
+    both nonzero is a ValueError (saddle.py:216-217)."""
+    rng = np.random.default_rng(3)
+    A = rng.standard_normal((120, 10))
+    c = rng.standard_normal(10)
+    R = la.qr(A, mode="economic")[1]
+    solver = pg.PcSS2("f64")
+    x, y, errs = solver(A, None, c, 0.5, 1e-13, 200, R, True, None)
+    xo, yo, eo, _ = oracle.pcss2_under(A, c, 0.5, 1e-13, 200, R, True)
+    assert la.norm(y.cpu().numpy() - yo) <= 1e-10 * la.norm(yo)
+    assert la.norm(x.cpu().numpy() - xo) <= 1e-9 * la.norm(xo)
+    with pytest.raises(ValueError):
+        solver(A, rng.standard_normal(120), c, 0.0, 1e-12, 50, R, True, None)
+
+
 def _gauss(n_rows, n_cols, rng):
     return osk.gaussian_operator(n_rows, n_cols, rng)
 

@@ -116,6 +116,25 @@ def test_spo_ridge_and_sso(golden):
     close(oracle.sso1(A, b, 0.0, S, "gelsd"), g["sso_x"], 1e-9)
 
 
+@pytest.mark.parametrize("tag", ["lin", "log", "tight"])
+def test_spu1(golden, tag):
+    """Underdetermined LS: the oracle's SPU1 reproduces the reference's y
+    (min-norm solution of A'y = c) and its per-iteration error log."""
+    g = golden("spu")
+    A, c = g[f"{tag}_A"], g[f"{tag}_c"]
+    rng = np.random.default_rng(int(g[f"{tag}_seed"]))
+    d = oracle.dim_checks(3, *A.shape)
+    S = GENS[str(g[f"{tag}_gen"])](d, A.shape[0], rng)
+    y, log, _ = oracle.spu1(A, c, float(g[f"{tag}_tol"]), int(g[f"{tag}_lim"]), S)
+    ref = g[f"{tag}_y"]
+    assert la.norm(y - ref) <= 1e-10 * la.norm(ref)
+    assert log.errors.size == g[f"{tag}_errors"].size
+    close(log.errors, g[f"{tag}_errors"], 1e-6)
+    # the reference's own acceptance properties (test_underdet_least_squares.py:50-75)
+    s0 = la.norm(A, 2)
+    assert la.norm(A.T @ y - c) / s0 <= 1e-6
+
+
 def _gauss(n_rows, n_cols, rng):
     return osk.gaussian_operator(n_rows, n_cols, rng)
 
