@@ -12,7 +12,9 @@
 //                     through distributed shared memory, and one partial per
 //                     cluster goes to the workspace for a fixed-order sum.
 // rla_sjlt_apply_right - Y = A S for a tall S (RS1 / learned-sketch use).
-// Binary32 inputs with d <= 2048 take the chunked path of sjlt_chunked.cu.
+// With d <= 4096 and nnz <= 16, rla_sjlt_apply takes the gather path of
+// sjlt_chunked.cu instead (A read once, no atomics); the kernel here serves
+// larger sketches and the allocation-free entry point.
 #include <climits>
 #include <cooperative_groups.h>
 #include "common.cuh"
@@ -23,6 +25,9 @@ namespace rla {
 size_t sjlt_chunked_ws(int64_t d, int64_t m, int nnz);
 int sjlt_apply_chunked_f32(int64_t d, int64_t m, int64_t n, int nnz, const int32_t* rows, const int8_t* signs,
                            double scale, const float* A, int64_t lda, float* Y, int64_t ldy, void* ws,
+                           cudaStream_t st);
+int sjlt_apply_chunked_f64(int64_t d, int64_t m, int64_t n, int nnz, const int32_t* rows, const int8_t* signs,
+                           double scale, const double* A, int64_t lda, double* Y, int64_t ldy, void* ws,
                            cudaStream_t st);
 namespace {
 
@@ -301,24 +306,29 @@ int rla_sjlt_apply(int dtype, int64_t d, int64_t m, int64_t n, int nnz, const in
     if ((m > 0 && (!rows || !signs || !A)) || (d * n > 0 && !Y) || lda < n || ldy < n) return RLA_ERR_ARG;
   }
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-  switch (dtype) {
-    case RLA_F64: return rla::sjlt_apply_impl<double>(d, m, n, nnz, rows, signs, scale, A, lda, Y, ldy, ws, ws_bytes, st);
-    case RLA_F32: {
-      // binary32 with d <= 2048: the chunked bandwidth path (its own workspace)
-      const size_t cws = rla::sjlt_chunked_ws(d, m, nnz);
-      if (cws > 0 && n > 0) {
-        if (ws == nullptr && ws_bytes != nullptr) {
-          *ws_bytes = cws;
-          return RLA_OK;
-        }
-        if (!ws_bytes || *ws_bytes < cws) return RLA_ERR_WORKSPACE;
-        return rla::sjlt_apply_chunked_f32(d, m, n, nnz, rows, signs, scale, static_cast<const float*>(A), lda,
-                                           static_cast<float*>(Y), ldy, ws, st);
-      }
-      return rla::sjlt_apply_impl<float>(d, m, n, nnz, rows, signs, scale, A, lda, Y, ldy, ws, ws_bytes, st);
+  if (dtype != RLA_F64 && dtype != RLA_F32) return RLA_ERR_ARG;
+  // d <= 4096, nnz <= 16: the gather path of sjlt_chunked.cu (its own
+  // workspace).  Binary64 takes it for matrices larger than L2 (>= 2^24
+  // elements), where it reads A once at twice the rate of the atomic kernel
+  // below; smaller binary64 problems (the batched solver's typical size)
+  // run faster on the atomic kernel, whose two passes hit in L2.
+  const size_t cws = rla::sjlt_chunked_ws(d, m, nnz);
+  const bool gather = dtype == RLA_F32 || m * n >= (int64_t(1) << 24);
+  if (cws > 0 && n > 0 && gather) {
+    if (ws == nullptr && ws_bytes != nullptr) {
+      *ws_bytes = cws;
+      return RLA_OK;
     }
-    default: return RLA_ERR_ARG;
+    if (!ws_bytes || *ws_bytes < cws) return RLA_ERR_WORKSPACE;
+    if (dtype == RLA_F32)
+      return rla::sjlt_apply_chunked_f32(d, m, n, nnz, rows, signs, scale, static_cast<const float*>(A), lda,
+                                         static_cast<float*>(Y), ldy, ws, st);
+    return rla::sjlt_apply_chunked_f64(d, m, n, nnz, rows, signs, scale, static_cast<const double*>(A), lda,
+                                       static_cast<double*>(Y), ldy, ws, st);
   }
+  if (dtype == RLA_F64)
+    return rla::sjlt_apply_impl<double>(d, m, n, nnz, rows, signs, scale, A, lda, Y, ldy, ws, ws_bytes, st);
+  return rla::sjlt_apply_impl<float>(d, m, n, nnz, rows, signs, scale, A, lda, Y, ldy, ws, ws_bytes, st);
 }
 
 int rla_sjlt_apply_right(int dtype, int64_t m, int64_t n, int64_t k, int nnz, const int32_t* rows,

@@ -115,11 +115,12 @@ def test_sjlt_apply_matches_reference_operator(K, dtype, d, m, n):
 
 
 @pytest.mark.parametrize("d,m,n,nnz,pad", [(2048, 50000, 40, 8, 0), (1000, 3000, 33, 16, 3), (64, 1024, 16, 8, 0),
-                                           (3000, 5000, 70, 8, 4),
-                                           (512, 7777, 100, 4, 4)])
+                                           (3000, 5000, 70, 8, 4), (4096, 6000, 50, 16, 1),
+                                           (512, 7777, 100, 4, 4), (7, 600, 5, 4, 0)])
 def test_sjlt_apply_f32_chunked_path(K, d, m, n, nnz, pad):
-    """Binary32 inputs with d <= 2048 take the chunked kernel: ragged slabs and
-    chunks, padded leading dimensions, and bitwise repeatable results."""
+    """Binary32 inputs with d <= 4096 take the gather kernel: ragged slabs and
+    chunks, padded and odd leading dimensions, several target parts, and
+    bitwise repeatable results."""
     rng = np.random.default_rng(d + m)
     rows, signs = K.sjlt_pattern(d, m, nnz, 17)
     A = rng.standard_normal((m, n + pad)).astype(np.float32)
@@ -134,6 +135,60 @@ def test_sjlt_apply_f32_chunked_path(K, d, m, n, nnz, pad):
         np.add.at(ref, r[:, t], sg[:, t, None] * A[:, :n].astype(np.float64))
     ref *= nnz ** -0.5
     assert rel(Y.cpu().numpy(), ref) <= 1e-5
+
+
+@pytest.mark.parametrize("d,m,n,nnz,pad", [(2048, 20000, 40, 8, 0), (3000, 5000, 35, 16, 3), (4096, 9000, 17, 16, 0),
+                                           (64, 1024, 16, 8, 0), (1000, 3000, 33, 16, 2), (5, 700, 3, 8, 0)])
+def test_sjlt_apply_f64_fixed_point(K, d, m, n, nnz, pad):
+    """Binary64 SJLT apply (fixed-point accumulation).  The magnitude grows 12
+    decades down the rows; every output is within a few quanta of the exact
+    sum (reference in extended precision), ragged slabs, odd and padded
+    leading dimensions, duplicates, bitwise repeatable."""
+    rng = np.random.default_rng(d + m + n)
+    rows = rng.integers(0, d, size=m * nnz).astype(np.int32)  # duplicates allowed (d = 5 < nnz)
+    signs = (rng.integers(0, 2, size=m * nnz) * 2 - 1).astype(np.int8)
+    A = rng.standard_normal((m, n + pad)) * np.logspace(-6, 6, m)[:, None]
+    Ad = dev(A)[:, :n]
+    scale = nnz ** -0.5
+    Y = K.sjlt_apply(dev(rows), dev(signs), nnz, d, Ad, scale)
+    Y2 = K.sjlt_apply(dev(rows), dev(signs), nnz, d, Ad, scale)
+    assert torch.equal(Y, Y2)
+    r = rows.reshape(m, nnz)
+    sg = signs.reshape(m, nnz).astype(np.longdouble)
+    ref = np.zeros((d, n), dtype=np.longdouble)
+    Al = A[:, :n].astype(np.longdouble)
+    for t in range(nnz):
+        np.add.at(ref, r[:, t], sg[:, t, None] * Al)
+    ref *= np.longdouble(scale)
+    err = np.abs(Y.cpu().numpy().astype(np.longdouble) - ref).max(axis=0)
+    colmax = np.abs(Al).max(axis=0)
+    # quantum ~ 2 max|A_j| 2^-(62 - h), h <= 15 here; a few quanta per output
+    assert np.all(err <= 1e-13 * colmax)
+    assert rel(Y.cpu().numpy(), ref.astype(np.float64)) <= 1e-14
+
+
+@pytest.mark.parametrize("d,n,pad", [(2048, 256, 0), (1000, 261, 3)])
+def test_sjlt_apply_f64_gather_path_exact(K, d, n, pad):
+    """Binary64 matrices of >= 2^24 elements take the gather kernel (A read
+    once, per-column scale following the running maximum exponent).  Entries
+    are integers times 2^-10 .. 2^10, growing down the rows, so every partial
+    sum is exact in binary64 and in the kernel's fixed point: the result must
+    equal the exact product bit for bit (ragged slabs and an odd leading
+    dimension included)."""
+    import scipy.sparse as sp
+    m, nnz = 65536, 8
+    rows, signs = K.sjlt_pattern(d, m, nnz, 23)
+    rng = np.random.default_rng(d + n)
+    A = rng.integers(-2 ** 15, 2 ** 15, size=(m, n + pad)).astype(np.float64)
+    A *= np.exp2(np.round(np.linspace(-10, 10, m)))[:, None]
+    Ad = dev(A)[:, :n]
+    scale = nnz ** -0.5
+    Y = K.sjlt_apply(rows, signs, nnz, d, Ad, scale)
+    assert torch.equal(Y, K.sjlt_apply(rows, signs, nnz, d, Ad, scale))
+    S = sp.csc_matrix((signs.cpu().numpy().astype(np.float64), rows.cpu().numpy(), np.arange(0, m * nnz + 1, nnz)),
+                      shape=(d, m))
+    ref = (S @ A[:, :n]) * scale
+    assert np.array_equal(Y.cpu().numpy(), ref)
 
 
 def test_sjlt_apply_with_replacement_duplicates(K):
