@@ -20,6 +20,7 @@ from oracle.sketching import (gaussian_operator, sjlt_operator, generate_srct,
 from oracle.lsqr import lsqr
 from oracle.least_squares import (dim_checks, spo, sso1, pcss2, pcss2_under, spu1,
                                   svd_right_precond, SketchAndPrecondLog)
+from oracle.saddle import pcg, pcss1, sps1, sps2
 from oracle.lowrank import orth, rs1, rf1, qb1, qb2, qb3, svd1, evd1, evd2
 
 __all__ = [

@@ -87,3 +87,61 @@ class PcSS2(PrecondSaddleSolver):
             x = torch.full((n,), float("nan"), dtype=torch.float64, device=Ad.device)
         self.last = dict(istop=res[1], itn=res[2], z=None)
         return x, y, res[7]
+
+
+class PcSS1(PrecondSaddleSolver):
+    """PCG on the normal equations (A'A + delta I) x = A'b - c (``saddle.py:86-180``).
+
+    ``R`` is an SVD-based preconditioner with pc_dim columns (M = R R'); when
+    pc_dim < n it becomes R R' + (I - V V') with V the normalised columns of R
+    and R rescaled by sqrt(s^2 + delta) / its smallest value.  The Gram and
+    preconditioner products are library GEMMs on the device.
+    """
+
+    ERROR_METRIC_INFO = """
+        2-norm of the residual from the normal equations
+    """
+
+    def __init__(self, precision="f64"):
+        self.precision = precision
+        self.last = None
+
+    def __call__(self, A, b, c, delta, tol, iter_lim, R, upper_tri, z0):
+        from .pcg import pcg
+        if upper_tri:
+            raise NotImplementedError()
+        mode = "f64" if self.precision == "f32" else self.precision
+        Ad = K.to_dev(A, torch.float64)
+        m, n = Ad.shape
+        bd = torch.zeros(m, dtype=torch.float64, device=Ad.device) if b is None else K.to_dev(b, torch.float64)
+        if bd.dim() != 1:
+            raise NotImplementedError()
+        Rd = K.to_dev(R, torch.float64).contiguous()
+        full = Rd.shape[1] == n
+        V = None
+        if not full:
+            sv = 1.0 / torch.linalg.vector_norm(Rd, dim=0)
+            V = (Rd * sv).contiguous()
+            sv = torch.sqrt(sv * sv + delta)
+            Rd = (V / (sv / sv[-1])).contiguous()
+
+        def mv_pre(v):
+            out = K.gemm(Rd, K.gemm(Rd, v, transa=True, mode=mode), mode=mode)
+            if not full:
+                out = out + v - K.gemm(V, K.gemm(V, v, transa=True, mode=mode), mode=mode)
+            return out
+
+        def mv_gram(v):
+            return K.gemm(Ad, K.gemm(Ad, v, mode=mode), transa=True, mode=mode) + delta * v
+
+        rhs = K.gemm(Ad, bd, transa=True, mode=mode)
+        if c is not None:
+            rhs = rhs - K.to_dev(c, torch.float64)
+        if z0 is None or not full:
+            x0 = torch.zeros(n, dtype=torch.float64, device=Ad.device)
+        else:
+            x0 = K.gemm(Rd, K.to_dev(z0, torch.float64), mode=mode)
+        x, resid = pcg(mv_gram, rhs, mv_pre, iter_lim, tol, x0)
+        y = bd - K.gemm(Ad, x, mode=mode)
+        self.last = dict(itn=len(resid))
+        return x, y, resid

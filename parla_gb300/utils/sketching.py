@@ -51,6 +51,10 @@ class DeviceOperator:
         eye = torch.eye(self.shape[1], dtype=torch.float64, device=K.device())
         return self._left(eye)
 
+    def t_matvec(self, v):
+        """S' v for a device vector v (the reference operators' ``S.T @ v``)."""
+        raise NotImplementedError(f"{type(self).__name__} has no transpose product")
+
 
 def _as_operand(X):
     if isinstance(X, torch.Tensor) and X.is_cuda and X.dtype in (torch.float32, torch.float64):
@@ -72,6 +76,10 @@ class DenseOperator(DeviceOperator):
     def _right(self, X):
         S = self.S if self.S.dtype == X.dtype else self.S.to(X.dtype)
         return K.gemm(X, S)
+
+    def t_matvec(self, v):
+        S = self.S if self.S.dtype == v.dtype else self.S.to(v.dtype)
+        return K.gemm(S, v, transa=True)
 
 
 class GaussianOperator(DenseOperator):
@@ -118,6 +126,15 @@ class SJLTOperator(DeviceOperator):
 
     def dense(self):
         return self.dense_matrix()
+
+    def t_matvec(self, v):
+        """S' v for the wide operator: entry j is scale * sum_k sign[j,k] v[rows[j,k]]
+        (a gather of nnz values per column of S)."""
+        if self.tall:  # the transpose of the tall operator is the wide pattern itself
+            return K.sjlt_apply(self.rows, self.signs, self.nnz, self.k, v, self.scale)
+        r = self.rows.view(self.n, self.nnz).long()
+        g = self.signs.view(self.n, self.nnz).to(v.dtype)
+        return (g * v[r]).sum(dim=1) * self.scale
 
 
 class SRCTOperator(DeviceOperator):

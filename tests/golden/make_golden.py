@@ -155,6 +155,52 @@ def spu_cases(parla):
     return out
 
 
+def _saddle_problem(m, n, spec, delta, seed):
+    """A = U diag(spec) V' (full column rank); b 70 % in range(A); c ~ N(0, I)."""
+    import parla.utils.sketching as usk
+    rng = np.random.default_rng(seed)
+    U = usk.orthonormal_operator(m, n, rng)
+    Vt = usk.orthonormal_operator(n, n, rng)
+    A = (U * spec) @ Vt
+    b0 = rng.standard_normal(m)
+    br = U @ (U.T @ b0)
+    bo = b0 - br
+    b = 0.7 * br * (np.mean(spec) / np.linalg.norm(br)) + 0.3 * bo * (np.mean(spec) / np.linalg.norm(bo))
+    c = rng.standard_normal(n)
+    return A, b, c
+
+
+def sps_cases(parla):
+    """SPS1 (PCG; full-rank and both Nystrom strategies) and SPS2 (LSQR)."""
+    import parla.comps.sketchers.oblivious as sko
+    from parla.drivers.saddlesys import SPS1, SPS2
+    out = {}
+    cases = {
+        'full0': ('sps1', 'ga', 3, 'left', 0.0, 61),
+        'full5': ('sps1', 'sj', 3, 'left', 0.5, 62),
+        'left': ('sps1', 'ga', 0.5, 'left', 0.5, 63),
+        'right': ('sps1', 'ga', 0.5, 'right', 0.5, 64),
+        'two0': ('sps2', 'sj', 3, None, 0.0, 65),
+        'two1': ('sps2', 'ga', 3, None, 1.0, 66),
+    }
+    for tag, (alg_name, gen, sf, strat, delta, seed) in cases.items():
+        A, b, c = _saddle_problem(300, 30, np.linspace(1e2, 1e-2, 30), delta, seed)
+        op = sko.SkOpSJ(8) if gen == 'sj' else sko.SkOpGA()
+        if alg_name == 'sps1':
+            alg = SPS1(op, sf, None)
+            alg.nystrom_strategy = strat
+            tol = 1e-12
+        else:
+            alg = SPS2(op, sf, None)
+            tol = 1e-12
+        x, y, log = alg(A, b, c, delta, tol, 100, np.random.default_rng(seed + 100), logging=True)
+        for k, v in (('A', A), ('b', b), ('c', c), ('x', x), ('y', y), ('errors', log.errors)):
+            out[f'{tag}_{k}'] = v
+        out[f'{tag}_meta'] = np.array(repr(dict(alg=alg_name, gen=gen, sf=sf, strategy=strat, delta=delta,
+                                                seed=seed + 100, tol=tol, iter_lim=100)))
+    return out
+
+
 def lowrank_cases(parla):
     import parla.comps.sketchers.oblivious as sko
     from parla.comps.sketchers.aware import RS1
@@ -223,7 +269,7 @@ def main(ref_path, only=None):
     meta = dict(numpy=np.__version__, scipy=scipy.__version__,
                 parla=parla.__version__)
     for name, fn in (('sketch', sketches), ('lsqr', lsqr_case),
-                     ('spo', spo_cases), ('spu', spu_cases),
+                     ('spo', spo_cases), ('spu', spu_cases), ('sps', sps_cases),
                      ('lowrank', lowrank_cases)):
         if only and name not in only:
             continue

@@ -1,5 +1,5 @@
-"""Driver-level parity on the GPU: parla_gb300's SPO / SSO1 / RS1 / RF1 / QB1 /
-SVD1 / EVD1 / EVD2 against the CPU oracle (pinned to the reference) on the
+"""Driver-level parity on the GPU: parla_gb300's SPO / SSO1 / SPU1 / SPS1 / SPS2 /
+RS1 / RF1 / QB1 / SVD1 / EVD1 / EVD2 against the CPU oracle (pinned to the reference) on the
 golden inputs, with operators drawn exactly as the reference draws them
 (``seed_compat=True``).
 
@@ -137,6 +137,49 @@ def test_spu1_ridge_branch_and_errors(pg):
     assert la.norm(x.cpu().numpy() - xo) <= 1e-9 * la.norm(xo)
     with pytest.raises(ValueError):
         solver(A, rng.standard_normal(120), c, 0.0, 1e-12, 50, R, True, None)
+
+
+@pytest.mark.parametrize("tag", ["full0", "full5", "left", "right", "two0", "two1"])
+def test_sps_matches_reference(pg, golden, tag):
+    """Saddle-point systems [I A; A' -delta I][y; x] = [b; c]: the device SPS1
+    (PCG; full-rank sketch and both Nystrom strategies) and SPS2 (LSQR) with
+    the reference's own sketch draws against the reference's x and y, and the
+    normal equations (A'A + delta I) x = A'b - c (test_saddlesys.py:110-120)."""
+    import ast
+    g = golden("sps")
+    meta = ast.literal_eval(str(g[f"{tag}_meta"]))
+    A, b, c = g[f"{tag}_A"], g[f"{tag}_b"], g[f"{tag}_c"]
+    op = pg.SkOpSJ(8, seed_compat=True) if meta["gen"] == "sj" else pg.SkOpGA(seed_compat=True)
+    if meta["alg"] == "sps1":
+        alg = pg.SPS1(op, meta["sf"], None)
+        alg.nystrom_strategy = meta["strategy"]
+        tol_x = 1e-6   # PCG on the normal equations: x to ~kappa(A'A) * 1e-12
+    else:
+        alg = pg.SPS2(op, meta["sf"], None)
+        tol_x = 1e-9
+    x, y, log = alg(A, b, c, meta["delta"], meta["tol"], meta["iter_lim"], meta["seed"], logging=True)
+    xr, yr = g[f"{tag}_x"], g[f"{tag}_y"]
+    assert isinstance(x, np.ndarray) and x.shape == xr.shape and y.shape == yr.shape
+    assert la.norm(x - xr) <= tol_x * (1 + la.norm(xr))
+    assert la.norm(y - yr) <= tol_x * (1 + la.norm(yr))
+    rhs = A.T @ b - c
+    assert la.norm(A.T @ (A @ x) + meta["delta"] * x - rhs) <= 1e-6 * la.norm(rhs)
+    assert abs(log.errors.size - g[f"{tag}_errors"].size) <= 3
+    np.testing.assert_allclose(log.errors[0], g[f"{tag}_errors"][0], rtol=1e-10)
+
+
+def test_pcss1_pcg_on_device(pg):
+    """PcSS1 with a full-rank preconditioner from an exact QR: the device PCG
+    against the oracle's on the same data (same iteration count, x to 1e-10)."""
+    rng = np.random.default_rng(9)
+    A = rng.standard_normal((200, 12)) @ np.diag(np.logspace(0, -2, 12))
+    b, c = rng.standard_normal(200), rng.standard_normal(12)
+    R = la.qr(A, mode="economic")[1]
+    M = la.solve_triangular(R, np.eye(12))
+    x, y, res = pg.PcSS1()(A, b, c, 0.1, 1e-10, 50, M, False, None)
+    xo, yo, ro = oracle.pcss1(A, b, c, 0.1, 1e-10, 50, M, None)
+    assert len(res) == len(ro)
+    assert la.norm(x.cpu().numpy() - xo) <= 1e-10 * la.norm(xo)
 
 
 def _gauss(n_rows, n_cols, rng):

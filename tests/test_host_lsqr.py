@@ -1,6 +1,7 @@
-"""Host logic of the stepped LSQR (used by the underdetermined solver) on CPU
-tensors: same iterates, stop code and error log as the oracle's LSQR, which is
-pinned to the reference's own outputs."""
+"""Host logic of the stepped LSQR (used by the underdetermined solver) and of
+the PCG (used by the saddle-point solver) on CPU tensors: same iterates, stop
+codes and error logs as the oracle's, which is pinned to the reference's own
+outputs."""
 import numpy as np
 import pytest
 import scipy.linalg as la
@@ -48,3 +49,23 @@ def test_lsqr_stepped_zero_rhs():
     A = torch.eye(4, dtype=torch.float64)
     res = lsqr_stepped(lambda v: A @ v, lambda u: A.T @ u, 4, torch.zeros(4, dtype=torch.float64))
     assert res[2] == 0 and res[7].size == 0 and float(res[0].abs().max()) == 0.0
+
+
+def test_pcg_matches_oracle():
+    """Host logic of the device PCG on CPU tensors against the oracle's PCG
+    (pinned to the reference through the saddle-point goldens)."""
+    from parla_gb300.comps.determiter.pcg import pcg
+    rng = np.random.default_rng(4)
+    B = rng.standard_normal((40, 10))
+    G = B.T @ B + 0.5 * np.eye(10)
+    P = np.linalg.inv(np.linalg.cholesky(G)).T
+    P = P @ P.T  # exact inverse of G as preconditioner, slightly perturbed below
+    P += 1e-3 * np.diag(rng.random(10))
+    rhs = rng.standard_normal(10)
+    Gt, Pt = torch.from_numpy(G), torch.from_numpy(P)
+    x, res = pcg(lambda v: Gt @ v, torch.from_numpy(rhs), lambda v: Pt @ v, 30, 1e-10,
+                 torch.zeros(10, dtype=torch.float64))
+    xo, ro = oracle.pcg(lambda v: G @ v, rhs, lambda v: P @ v, 30, 1e-10, np.zeros(10))
+    assert len(res) == len(ro)
+    np.testing.assert_allclose(res, ro, rtol=1e-8)
+    assert la.norm(x.numpy() - xo) <= 1e-12 * la.norm(xo)

@@ -135,6 +135,46 @@ def test_spu1(golden, tag):
     assert la.norm(A.T @ y - c) / s0 <= 1e-6
 
 
+SPS_TAGS = ["full0", "full5", "left", "right", "two0", "two1"]
+
+
+def sps_setup(g, tag):
+    """Inputs and the reference's sketch draw for a saddle-point golden case."""
+    import ast
+    meta = ast.literal_eval(str(g[f"{tag}_meta"]))
+    A, b, c = g[f"{tag}_A"], g[f"{tag}_b"], g[f"{tag}_c"]
+    m, n = A.shape
+    rng = np.random.default_rng(meta["seed"])
+    if meta["alg"] == "sps1":
+        d = int(meta["sf"] * n)
+        shape = (n, d) if (d < n and meta["strategy"] == "right") else (d, m)
+    else:
+        d = oracle.dim_checks(meta["sf"], m, n)
+        shape = (d, m)
+    S = GENS[meta["gen"]](shape[0], shape[1], rng)
+    return meta, A, b, c, d, S
+
+
+@pytest.mark.parametrize("tag", SPS_TAGS)
+def test_sps(golden, tag):
+    """Saddle-point systems: the oracle's SPS1 (PCG, full-rank and Nystrom
+    preconditioners) and SPS2 (LSQR) reproduce the reference's x, y and log."""
+    g = golden("sps")
+    meta, A, b, c, d, S = sps_setup(g, tag)
+    if meta["alg"] == "sps1":
+        x, y, log = oracle.sps1(A, b, c, meta["delta"], meta["tol"], meta["iter_lim"], S, d, meta["strategy"])
+    else:
+        x, y, log = oracle.sps2(A, b, c, meta["delta"], meta["tol"], meta["iter_lim"], S)
+    xr, yr = g[f"{tag}_x"], g[f"{tag}_y"]
+    assert la.norm(x - xr) <= 1e-9 * la.norm(xr)
+    assert la.norm(y - yr) <= 1e-9 * la.norm(yr)
+    assert log.errors.size == g[f"{tag}_errors"].size
+    close(log.errors[:3], g[f"{tag}_errors"][:3], 1e-6)
+    # the normal equations hold (test_saddlesys.py:110-120)
+    rhs = A.T @ b - c
+    assert la.norm(A.T @ (A @ x) + meta["delta"] * x - rhs) <= 1e-6 * la.norm(rhs)
+
+
 def _gauss(n_rows, n_cols, rng):
     return osk.gaussian_operator(n_rows, n_cols, rng)
 
