@@ -18,6 +18,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -61,7 +62,7 @@ class ClockSampler:
     def __init__(self, index=0):
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        self.path = os.path.join(tempfile.gettempdir(), f"rla_bench_clocks_{os.getpid()}.csv")
 
     def __enter__(self):
         try:
