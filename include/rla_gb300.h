@@ -74,9 +74,13 @@ int rla_sjlt_pattern(int64_t d, int64_t m, int nnz, uint64_t seed,
                      int32_t* rows, int8_t* signs, rla_stream_t stream);
 
 /* Y (d x n) = S A for a wide SJLT S (d x m) given as (rows, signs) with
- * `nnz` entries per column, each of value sign*scale.  Accumulation is exact
- * 64-bit fixed point per column tile, so results do not depend on the order
- * of the scatter.  dtype RLA_F64 or RLA_F32 (same type for A and Y).
+ * `nnz` entries per column, each of value sign*scale.  Binary64 accumulates
+ * in exact 64-bit fixed point per column, so results do not depend on the
+ * summation order; binary32 with d <= 4096 and nnz <= 16 sums in FP32 in a
+ * fixed order (bitwise repeatable).  With d <= 4096 and nnz <= 16, binary32
+ * and binary64 inputs of at least 2^24 elements take the gather kernel that
+ * reads A once; the workspace query reports what the chosen kernel needs.
+ * dtype RLA_F64 or RLA_F32 (same type for A and Y).
  * Replaces the CSC product `S @ A` (parla/utils/sketching.py:73-74 and
  * parla/drivers/least_squares.py:303) for S from SkOpSJ. */
 int rla_sjlt_apply(int dtype, int64_t d, int64_t m, int64_t n, int nnz,
