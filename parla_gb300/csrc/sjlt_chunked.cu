@@ -31,7 +31,6 @@
 //      At the end the Q CTAs of a part sum their partials through
 //      distributed shared memory in a fixed order and write Y.  The result
 //      does not depend on scheduling.
-#include <climits>
 #include <type_traits>
 #include <cooperative_groups.h>
 
