@@ -401,7 +401,7 @@ def bench_learned(torch, n_eval):
                        "8 nnz/col; network trained on 16384 matrices (seeds 0..16383)",
            "held_out_seeds": f"{T.HELD_OUT_SEED0}..{T.HELD_OUT_SEED0 + n_eval - 1}"}
     net = L.SketchNet.load()
-    out["cfg5"] = T.summary(T.evaluate(net, list(range(T.HELD_OUT_SEED0, T.HELD_OUT_SEED0 + n_eval)), 74, 64))
+    out["held_out"] = T.summary(T.evaluate(net, list(range(T.HELD_OUT_SEED0, T.HELD_OUT_SEED0 + n_eval)), 74, 64))
     kw = {"coherent": True, "noise": 0.05, "decay": 24.0, "rank_range": (32, 128)}
     netc = L.SketchNet.load(os.path.join(ROOT, "parla_gb300", "learned", "sketchnet_k64_d74_coherent.npz"))
     out["coherent"] = T.summary(T.evaluate(netc, list(range(T.HELD_OUT_SEED0, T.HELD_OUT_SEED0 + min(256, n_eval))),
@@ -415,14 +415,32 @@ def bench_learned(torch, n_eval):
     return out
 
 
+def _ls_single_problem(torch, m=20000, n=200, seed=11):
+    """A = U diag(s) V^T (Haar U, V; s logspaced 1 .. 1e-8), b = A x* + 1e-6 r_perp
+    with x* ~ N(0, 1) and r_perp a unit vector orthogonal to range(A)."""
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    dev, f64 = torch.device("cuda"), torch.float64
+    U, R = torch.linalg.qr(torch.randn((m, n), generator=g, device=dev, dtype=f64))
+    U = U * torch.sign(torch.diagonal(R))
+    V, R = torch.linalg.qr(torch.randn((n, n), generator=g, device=dev, dtype=f64))
+    V = V * torch.sign(torch.diagonal(R))
+    s = torch.logspace(0, -8, n, dtype=f64, device=dev)
+    A = ((U * s) @ V.t()).contiguous()
+    x = torch.randn(n, generator=g, device=dev, dtype=f64)
+    r = torch.randn(m, generator=g, device=dev, dtype=f64)
+    r -= U @ (U.t() @ r)
+    r -= U @ (U.t() @ r)
+    b = A @ x + 1e-6 * r / torch.linalg.vector_norm(r)
+    return A, b.contiguous()
+
+
 def bench_ls_single(torch, pg):
     """Sketch-and-precondition LS as the reference runs it (20000 x 200, kappa 1e8):
     A 20000 x 200, kappa 1e8, Gaussian sketch d = 4n, QR preconditioner,
     tolerance 1e-12; plain FP64 GPU path vs the double-float path.
     Gated error: ||A (x - x_lapack)|| / ||A x_lapack|| (x_lapack: FP64 LAPACK on the host)."""
     import scipy.linalg as la
-    from parla_gb300.drivers.batched import make_problem
-    A, b, _ = make_problem(20000, 200, 1e8, 1e-6, 11)
+    A, b = _ls_single_problem(torch)
     An, bn = A.cpu().numpy(), b.cpu().numpy()
     xr = la.lstsq(An, bn)[0]
     out = {"workload": "SPO(SkOpGA, 4, 'qr') 20000x200 kappa=1e8, tol 1e-12"}
@@ -480,15 +498,35 @@ def bench_ls_batched(torch, pg, count):
     dtp = time.perf_counter() - t0
     out["plain_fp64"] = {"solves_per_s": count / dtp, "ms": dtp * 1e3}
     out["speedup"] = out["batched"]["solves_per_s"] / out["plain_fp64"]["solves_per_s"]
-    worst, worst_p = 0.0, 0.0
-    idx = [i for i in range(count) if shapes[i][0] * shapes[i][1] <= 4e6][:12]
+    idx = _stratified_sample(shapes, 48)
+    worst, worst_p, errs = 0.0, 0.0, []
     for i in idx:
         An = probs[i][0].cpu().numpy()
-        xr = la.lstsq(An, probs[i][1].cpu().numpy())[0]
-        worst = max(worst, float(la.norm(An @ (xs[i].cpu().numpy() - xr)) / la.norm(An @ xr)))
+        xr = la.lstsq(An, probs[i][1].cpu().numpy(), lapack_driver="gelsy")[0]
+        e = float(la.norm(An @ (xs[i].cpu().numpy() - xr)) / la.norm(An @ xr))
+        worst = max(worst, e)
         worst_p = max(worst_p, float(la.norm(An @ (xp[i].cpu().numpy() - xr)) / la.norm(An @ xr)))
-    out["pred_err_sampled"] = {"batched": worst, "plain_fp64": worst_p, "problems_checked": len(idx)}
+        errs.append(e)
+    out["pred_err_sampled"] = {
+        "batched": worst, "plain_fp64": worst_p, "problems_checked": len(idx), "median_batched": float(np.median(errs)),
+        "sample": "stratified: the 12 largest m*n, the 12 largest kappa, 24 spread over the rest "
+                  f"(largest m*n checked {max(shapes[i][0] * shapes[i][1] for i in idx)}, "
+                  f"largest kappa {max(shapes[i][2] for i in idx):.2e}); LAPACK gelsy in binary64 on the host"}
     return out
+
+
+def _stratified_sample(shapes, count):
+    """Indices: the largest problems, the worst conditioned, and an even spread."""
+    order_size = sorted(range(len(shapes)), key=lambda i: -shapes[i][0] * shapes[i][1])
+    order_kap = sorted(range(len(shapes)), key=lambda i: -shapes[i][2])
+    pick = []
+    for i in order_size[:count // 4] + order_kap[:count // 4]:
+        if i not in pick:
+            pick.append(i)
+    rest = [i for i in range(len(shapes)) if i not in pick]
+    step = max(1, len(rest) // max(1, count - len(pick)))
+    pick += rest[::step][:count - len(pick)]
+    return sorted(pick)
 
 
 def cpu_baseline(A, budget_s=30.0, steps=None):

@@ -104,9 +104,10 @@ int rla_sjlt_apply_right(int dtype, int64_t m, int64_t n, int64_t k, int nnz,
  * array compiled into the library, held by every GPU context that loads the
  * library until exit; problems that need more return RLA_ERR_WORKSPACE.  The
  * first call on a device resolves the array's address (call it before any
- * stream capture on that device).  All calls share the array: calls that
- * overlap on the GPU race and must be serialised by the caller.  Allocates
- * nothing. */
+ * stream capture on that device); a call under a different CUDA context on
+ * the device resolves it again, and a cudaDeviceReset between calls is not
+ * supported.  All calls share the array: calls that overlap on the GPU race
+ * and must be serialised by the caller.  Allocates nothing. */
 int rla_sjlt_apply_noalloc(int dtype, int64_t d, int64_t m, int64_t n, int nnz,
                            const int32_t* rows, const int8_t* signs,
                            double scale, const void* A, int64_t lda, void* Y,
@@ -246,7 +247,9 @@ int rla_chol_inv_f32(int64_t n, const float* G, int64_t ldg, float* Rinv,
  * has_x0, LSQR iterate on exit; the caller forms x = M z.  arnorms (HOST
  * array of iter_lim doubles) receives the per-iteration ||Abar' r||
  * estimates, itn/istop (host) the iteration count and Paige-Saunders stop
- * code.  Synchronises `stream`.  Replaces lsqr,
+ * code, norms (HOST array of 5 doubles, or NULL) the final r1norm, r2norm,
+ * anorm, acond and xnorm (positions 3-6 and 8 of the reference's return
+ * tuple; no damping, so r1norm = r2norm).  Synchronises `stream`.  Replaces lsqr,
  * parla/comps/determiter/lsqr.py:98-574, with the operator of
  * a_lift_precond, parla/comps/preconditioning.py:16-67, as called by PcSS2,
  * parla/comps/determiter/saddle.py:266-280. */
@@ -255,17 +258,23 @@ int rla_lsqr_run(int dtype, int64_t m, int64_t n, int64_t p, const double* A,
                  const double* M, int64_t ldm, double sqrt_delta,
                  const double* b, double* z, int has_x0, double atol,
                  double btol, double conlim, int iter_lim, double* arnorms,
-                 int* itn, int* istop, void* ws, size_t* ws_bytes,
-                 rla_stream_t stream);
+                 int* itn, int* istop, double* norms, void* ws,
+                 size_t* ws_bytes, rla_stream_t stream);
 
 /* Asynchronous form of rla_lsqr_run for batched solves: nothing is copied to
  * the host and the stream is not synchronised.  out (device int[3]) receives
  * itn, istop and the grid-barrier status; arnorms is a DEVICE array of
  * iter_lim doubles.  max_ctas (0 = all SMs) caps the cooperative grid so that
- * several problems can run concurrently on different streams.  ptol > 0 adds
- * a stopping rule on the prediction error: stop (istop = 9) once the change
- * ||Abar (z_k - z_{k-1})|| <= ptol ||b|| (at LSQR's linear rate this bounds
- * the remaining ||Abar (z - z*)||).  dtype RLA_F64,
+ * several problems can run concurrently on different streams.  norms (DEVICE
+ * double[5] or NULL) receives r1norm, r2norm, anorm, acond, xnorm.  ptol > 0
+ * adds a stopping rule on the prediction error (istop = 9): the step's
+ * prediction change |phi_k| = ||Abar (z_k - z_{k-1})|| (exact, no difference
+ * of residual norms) and the observed contraction rate rho (the larger of
+ * 1/2 and the last two ratios |phi_j / phi_{j-1}|; rule off above 0.95)
+ * bound the remaining ||Abar (z_k - z*)|| by |phi_k| rho / sqrt(1 - rho^2);
+ * stop once that is <= ptol times a lower bound on ||Abar z*||:
+ * sqrt(sum_j phi_j^2) from a zero start, sqrt(||b||^2 - ||r_k||^2) from a
+ * start point.  dtype RLA_F64,
  * RLA_DF, or RLA_F32 (A_hi read as binary32, binary32 arithmetic: the
  * low-precision inner solve of iterative refinement). */
 int rla_lsqr_launch(int dtype, int64_t m, int64_t n, int64_t p, const double* A,
@@ -273,8 +282,8 @@ int rla_lsqr_launch(int dtype, int64_t m, int64_t n, int64_t p, const double* A,
                     const double* M, int64_t ldm, double sqrt_delta,
                     const double* b, double* z, int has_x0, double atol,
                     double btol, double conlim, double ptol, int iter_lim,
-                    int max_ctas, int* out, double* arnorms, void* ws,
-                    size_t* ws_bytes, rla_stream_t stream);
+                    int max_ctas, int* out, double* arnorms, double* norms,
+                    void* ws, size_t* ws_bytes, rla_stream_t stream);
 
 /* ---------------------------------------------- batched least squares */
 
@@ -308,7 +317,8 @@ size_t rla_trtri_record_size(void);
 int rla_trtri_hl_batched(const void* probs, int nprob, int64_t total_cols,
                          int64_t nmax, rla_stream_t stream);
 
-/* (x, when not NULL, receives M z at the end of the solve.) */
+/* (x, when not NULL, receives M z at the end of the solve; norms, when not
+ * NULL, a device double[5] as for rla_lsqr_launch.) */
 size_t rla_lsqr_record_size(void);
 size_t rla_lsqr_problem_ws(int64_t m, int64_t n, int64_t p, int iter_lim);
 int rla_lsqr_record(void* rec, int64_t m, int64_t n, int64_t p,
@@ -316,8 +326,8 @@ int rla_lsqr_record(void* rec, int64_t m, int64_t n, int64_t p,
                     int64_t lda, const double* M, int64_t ldm,
                     double sqrt_delta, const double* b, double* z, int has_x0,
                     double atol, double btol, double conlim, double ptol,
-                    int iter_lim, int* out, double* arnorms, double* x,
-                    void* ws);
+                    int iter_lim, int* out, double* arnorms, double* norms,
+                    double* x, void* ws);
 /* One thread-block cluster of `cluster` CTAs (1..8) per problem, largest
  * first by `order`; at most max_ctas CTAs resident (0: all that fit), so that
  * launches of several width classes can share the device side by side. */

@@ -34,12 +34,21 @@ def sym_ortho(a, b):
 
 
 def lsqr(matvec, rmatvec, n, b, damp=0.0, atol=1e-8, btol=1e-8, conlim=1e8,
-         iter_lim=None, x0=None):
+         iter_lim=None, x0=None, ptol=0.0):
     """Solve min ||A x - b||^2 + damp^2 ||x||^2 with A given by its products.
 
     Scalings are written as (1/beta) * u, as in the reference, so the
     stopping tests trip on the same iteration when they sit near rounding
     level.
+
+    ``ptol > 0`` (damp = 0 only) adds the device library's prediction-error
+    rule, which has no counterpart in the reference: istop = 9 once
+    |phi_k| rho / sqrt(1 - rho^2) <= ptol * scale, with rho the larger of 1/2
+    and the last two ratios |phi_j / phi_{j-1}| (rule off above 0.95) and
+    scale a lower bound on ||A x*||: sqrt(sum_j phi_j^2) from a zero start,
+    sqrt(max(||b||^2 - ||r_k||^2, 0)) from x0.  It restates the rule of the
+    device kernel (``parla_gb300/csrc/lsqr.cu``) so that its stopping point
+    can be checked on the CPU.
 
     Returns (x, istop, itn, r1norm, r2norm, anorm, acond, arnorms, xnorm),
     matching positions 0-8 of ``parla/comps/determiter/lsqr.py:574``.
@@ -80,6 +89,7 @@ def lsqr(matvec, rmatvec, n, b, damp=0.0, atol=1e-8, btol=1e-8, conlim=1e8,
         return x, istop, itn, r1norm, r2norm, anorm, acond, np.array([]), xnorm
 
     arnorms = []
+    pred2 = aphi1 = aphi2 = 0.0
     while itn < iter_lim:
         arnorms.append(arnorm)
         itn += 1
@@ -152,6 +162,19 @@ def lsqr(matvec, rmatvec, n, b, damp=0.0, atol=1e-8, btol=1e-8, conlim=1e8,
             istop = 2
         if test1 <= rtol:
             istop = 1
+        if ptol > 0:
+            aphi = abs(phi)
+            pred2 += phi * phi
+            rate = 0.5
+            if aphi1 > 0:
+                rate = max(rate, aphi / aphi1)
+            if aphi2 > 0 and aphi1 > 0:
+                rate = max(rate, aphi1 / aphi2)
+            if itn >= 3 and rate <= 0.95:
+                scale = sqrt(pred2 if x0 is None else max(bnorm * bnorm - rnorm * rnorm, 0.0))
+                if aphi * rate / sqrt(1.0 - rate * rate) <= ptol * scale:
+                    istop = 9
+            aphi2, aphi1 = aphi1, aphi
         if istop != 0:
             break
     return (x, istop, itn, r1norm, r2norm, anorm, acond, np.array(arnorms),

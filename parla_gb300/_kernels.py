@@ -488,8 +488,12 @@ def convert_bf16_pair(x, want_y=True, want_t=True):
     return y, yt
 
 
-def lsqr_run(A, M, b, z0, sqrt_delta, atol, btol, conlim, iter_lim, mode="f64", split=None):
-    """Device LSQR on [A; sd I] M.  Returns (z, istop, itn, arnorms)."""
+def lsqr_run(A, M, b, z0, sqrt_delta, atol, btol, conlim, iter_lim, mode="f64", split=None, norms=None):
+    """Device LSQR on [A; sd I] M.  Returns (z, istop, itn, arnorms).
+
+    ``norms``, when given, is a float64 numpy array of 5 entries that
+    receives r1norm, r2norm, anorm, acond and xnorm at exit.
+    """
     m, n = A.shape
     p = M.shape[1]
     z = torch.zeros(p, dtype=torch.float64, device=A.device) if z0 is None else z0.clone().contiguous()
@@ -502,7 +506,8 @@ def lsqr_run(A, M, b, z0, sqrt_delta, atol, btol, conlim, iter_lim, mode="f64", 
         hi, lo = split_f64(A)
     head = (code, m, n, p, ptr(A), ptr(hi), ptr(lo), A.stride(0), ptr(M), M.stride(0), float(sqrt_delta),
             ptr(b), ptr(z), int(z0 is not None), float(atol), float(btol), float(conlim), int(iter_lim),
-            arn.ctypes.data_as(C.c_void_p), C.byref(itn), C.byref(istop))
+            arn.ctypes.data_as(C.c_void_p), C.byref(itn), C.byref(istop),
+            norms.ctypes.data_as(C.c_void_p) if norms is not None else None)
     need = size_query("rla_lsqr_run", *head)
     ws = workspace(need)
     nb = C.c_size_t(need)
@@ -525,8 +530,8 @@ def geqrf_colmajor_async(T, n, mode="df", max_ctas=0):
 class LsqrHandle:
     """Device-side results of an asynchronous LSQR launch."""
 
-    def __init__(self, z, out, arn):
-        self.z, self.out, self.arn = z, out, arn
+    def __init__(self, z, out, arn, nrm=None):
+        self.z, self.out, self.arn, self.nrm = z, out, arn, nrm
 
     def result(self):
         o = self.out.cpu().numpy()
@@ -543,16 +548,17 @@ def lsqr_launch(A, M, b, z0, sqrt_delta, atol, btol, conlim, iter_lim, mode="df"
     z = torch.zeros(p, dtype=torch.float64, device=dev) if z0 is None else z0.clone().contiguous()
     out = torch.zeros(3, dtype=torch.int32, device=dev)
     arn = torch.zeros(max(iter_lim, 1), dtype=torch.float64, device=dev)
+    nrm = torch.zeros(5, dtype=torch.float64, device=dev)
     hi, lo = split if split is not None else (None, None)
     lda = A.stride(0) if A is not None else hi.stride(0)
     head = (MODES[mode], m, n, p, ptr(A), ptr(hi), ptr(lo), lda, ptr(M), M.stride(0), float(sqrt_delta), ptr(b),
             ptr(z), int(z0 is not None), float(atol), float(btol), float(conlim), float(ptol), int(iter_lim),
-            int(max_ctas), ptr(out), ptr(arn))
+            int(max_ctas), ptr(out), ptr(arn), ptr(nrm))
     need = size_query("rla_lsqr_launch", *head)
     ws = workspace(need)
     nb = C.c_size_t(need)
     _timed("lsqr", 1, call, "rla_lsqr_launch", *head, ptr(ws), C.byref(nb), stream())
-    return LsqrHandle(z, out, arn)
+    return LsqrHandle(z, out, arn, nrm)
 
 
 def residual_df(hi, lo, x, b):

@@ -52,14 +52,14 @@ SIGNATURES = {
     "rla_geqrf": [_i32, _i64, _i64, _i64, _p, _i64, _p, _p, _psz, _p],
     "rla_geqrf_ctas": [_i32, _i64, _i64, _i64, _p, _i64, _p, _i32, _p, _psz, _p],
     "rla_lsqr_launch": [_i32, _i64, _i64, _i64, _p, _p, _p, _i64, _p, _i64, _f64, _p, _p, _i32, _f64, _f64,
-                        _f64, _f64, _i32, _i32, _p, _p, _p, _psz, _p],
+                        _f64, _f64, _i32, _i32, _p, _p, _p, _p, _psz, _p],
     "rla_residual_df": [_i64, _i64, _p, _p, _i64, _p, _p, _p, _p],
     "rla_geqrf_batched": [_i32, _p, _p, _i32, _p, _p],
     "rla_geqrf_hl_batched": [_p, _p, _i32, _i64, _p, _p],
     "rla_trtri_hl_batched": [_p, _i32, _i64, _i64, _p],
     "rla_lsqr_batched": [_i32, _p, _p, _i32, _i64, _i32, _i32, _p, _p],
     "rla_lsqr_record": [_p, _i64, _i64, _i64, _p, _p, _p, _i64, _p, _i64, _f64, _p, _p, _i32, _f64, _f64, _f64,
-                        _f64, _i32, _p, _p, _p, _p],
+                        _f64, _i32, _p, _p, _p, _p, _p],
     "rla_orgqr": [_i32, _i64, _i64, _p, _i64, _p, _p, _i64, _p, _psz, _p],
     "rla_potrf_upper": [_i32, _i64, _p, _i64, _p, _p, _psz, _p],
     "rla_chol_inv_f32": [_i64, _p, _i64, _p, _i64, _p, _i64, _p, _p],
@@ -77,7 +77,7 @@ SIGNATURES = {
     "rla_svd_jacobi": [_i32, _i64, _p, _i64, _p, _i64, _p, _p, _i32, _i32, _p],
     "rla_trtri_upper": [_i32, _i64, _p, _i64, _p, _i64, _p],
     "rla_lsqr_run": [_i32, _i64, _i64, _i64, _p, _p, _p, _i64, _p, _i64, _f64, _p, _p, _i32, _f64, _f64,
-                     _f64, _i32, _p, _p, _p, _p, _psz, _p],
+                     _f64, _i32, _p, _p, _p, _p, _p, _psz, _p],
     "rla_convert": [_i32, _i32, _i32, _i64, _i64, _p, _i64, _p, _i64, _p],
     "rla_convert_bf16_pair": [_i32, _i64, _i64, _p, _i64, _p, _i64, _p, _i64, _p],
     "rla_split_f64": [_i64, _i64, _p, _i64, _p, _p, _i64, _p],

@@ -42,9 +42,10 @@ def lsqr(A, b, damp=0.0, atol=1e-8, btol=1e-8, conlim=1e8, iter_lim=None, show=F
     """Device LSQR.  ``A`` is a ``PrecondOperator`` or a dense matrix.
 
     Returns (x, istop, itn, r1norm, r2norm, anorm, acond, arnorms, xnorm, var)
-    like the reference; the norms the device loop does not export are NaN.
-    ``damp`` must be 0 (regularisation enters through the operator, as in the
-    reference's sketch-and-precondition drivers).
+    like the reference (``var`` is None: ``calc_var`` is not supported); the
+    norms are the device loop's final estimates.  ``damp`` must be 0
+    (regularisation enters through the operator, as in the reference's
+    sketch-and-precondition drivers), so r1norm = r2norm.
     """
     if damp != 0.0:
         raise NotImplementedError("damp: pass sqrt(delta) through PrecondOperator instead")
@@ -64,12 +65,13 @@ def lsqr(A, b, damp=0.0, atol=1e-8, btol=1e-8, conlim=1e8, iter_lim=None, show=F
         else:
             raise ValueError("b must have A.shape[0] entries (zeros for the lifted rows)")
     z0 = None if x0 is None else K.to_dev(x0, torch.float64)
+    nrm = np.zeros(5, dtype=np.float64)
     z, istop, itn, arn = K.lsqr_run(A.A, A.M, bd, z0, A.sqrt_delta, atol, btol, conlim, iter_lim,
-                                    A.precision, A.split)
+                                    A.precision, A.split, norms=nrm)
+    r1norm, r2norm, anorm, acond, xnorm = (float(v) for v in nrm)
     if show:
-        print(f"LSQR (device): istop={istop} itn={itn}")
-    nan = float("nan")
-    return z, istop, itn, nan, nan, nan, nan, arn, nan, None
+        print(f"LSQR (device): istop={istop} itn={itn} r1norm={r1norm:.3e} anorm={anorm:.3e} acond={acond:.3e}")
+    return z, istop, itn, r1norm, r2norm, anorm, acond, arn, xnorm, None
 
 
 def _givens(a, b):

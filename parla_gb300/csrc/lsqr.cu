@@ -39,12 +39,13 @@ struct LsqrArgs {
   const double* b;
   double* z; int has_x0;
   double atol, btol, conlim;
-  double ptol;      // > 0: stop once the prediction change per step is below ptol * ||b||
+  double ptol;      // > 0: prediction-error stopping rule (istop 9), see the main loop
   int iter_lim;
   double* arn;      // [iter_lim] device
   int* out;         // [2] itn, istop
   double* u; double* uext; double* v; double* w; double* y; double* t;
   double* x;        // optional: x = M z written at the end (null: skip)
+  double* nrm;      // optional [5]: r1norm, r2norm, anorm, acond, xnorm at exit (null: skip)
   double* part;     // [G] per-CTA partial sums
   double* tpart;    // [G][n] per-CTA partial A^T u
   GridBar bar;
@@ -123,7 +124,8 @@ template <> struct Elem<df> {
 };
 
 struct Scal {  // LSQR recurrence state (binary64, shared memory, advanced by thread 0)
-  double rhobar, phibar, anorm, acond, ddnorm, res2, xnorm, xxnorm, zz, cs2, sn2, bnorm, arnorm, rnorm_prev;
+  double rhobar, phibar, anorm, acond, ddnorm, res2, xnorm, xxnorm, zz, cs2, sn2, bnorm, arnorm;
+  double rnorm, pred2, aphi1, aphi2;  // prediction-error rule: sum of phi^2, the last two |phi|
 };
 
 // Sum of the G per-CTA partials, identical in every CTA: warp 0 reads them in
@@ -442,7 +444,10 @@ __device__ __forceinline__ void lsqr_body(const LsqrArgs& a, const int G, const 
     alfa = sqrt(sum_parts<V>(a.part, G));
   }
   if (alfa * beta == 0.0) {
-    if (blk == 0 && tid == 0) { a.out[0] = 0; a.out[1] = 0; }
+    if (blk == 0 && tid == 0) {
+      a.out[0] = 0; a.out[1] = 0;
+      if (a.nrm != nullptr) { a.nrm[0] = a.nrm[1] = beta; a.nrm[2] = a.nrm[3] = a.nrm[4] = 0.0; }
+    }
     if (a.x != nullptr) {
       RLA_SYNC();
       mat_M_to(a.z, 1.0, a.x);
@@ -463,7 +468,8 @@ __device__ __forceinline__ void lsqr_body(const LsqrArgs& a, const int G, const 
     s.rhobar = alfa; s.phibar = beta;
     s.anorm = s.acond = s.ddnorm = s.res2 = s.xnorm = s.xxnorm = s.zz = 0.0;
     s.cs2 = -1.0; s.sn2 = 0.0;
-    s.rnorm_prev = beta;
+    s.rnorm = beta;
+    s.pred2 = s.aphi1 = s.aphi2 = 0.0;
   }
   RLA_SYNC();
   int itn = 0, istop = 0;
@@ -536,9 +542,7 @@ __device__ __forceinline__ void lsqr_body(const LsqrArgs& a, const int G, const 
       s.xxnorm += s.zz * s.zz;
       s.acond = s.anorm * sqrt(s.ddnorm);
       double rnorm = sqrt(s.phibar * s.phibar + s.res2);
-      // ||r_{k-1}||^2 - ||r_k||^2 = ||Abar (z_k - z_{k-1})||^2: the prediction change
-      const double dpred2 = fmax(s.rnorm_prev * s.rnorm_prev - rnorm * rnorm, 0.0);
-      s.rnorm_prev = rnorm;
+      s.rnorm = rnorm;
       s.arnorm = alfa * fabs(tau);
       const double eps = 2.220446049250313e-16;
       const double ctol = a.conlim > 0.0 ? 1.0 / a.conlim : 0.0;
@@ -555,9 +559,32 @@ __device__ __forceinline__ void lsqr_body(const LsqrArgs& a, const int G, const 
       if (test3 <= ctol) st = 3;
       if (test2 <= a.atol) st = 2;
       if (test1 <= rtol) st = 1;
-      // prediction-error rule: with linear convergence at rate <= 1/2 the
-      // remaining ||Abar (z - z*)|| is at most the last change
-      if (a.ptol > 0.0 && itn >= 2 && sqrt(dpred2) <= a.ptol * s.bnorm) st = 9;
+      // Prediction-error rule (istop 9).  The step's change of the
+      // prediction is exactly |phi|: r_{k-1} - r_k = Abar (z_k - z_{k-1}) and
+      // r_k is orthogonal to it, so ||r_{k-1}||^2 - ||r_k||^2 = phi^2 (no
+      // cancellation, unlike the difference of the two squares when the
+      // residual is large).  The steps are mutually orthogonal, so the
+      // remaining error is ||Abar (z_k - z*)||^2 = sum_{j>k} phi_j^2; with a
+      // contraction rate rho per step that is at most
+      // |phi_k| rho / sqrt(1 - rho^2).  rho is the larger of the last two
+      // observed ratios |phi_j / phi_{j-1}| and of 1/2 (the rate that a
+      // sketch of 4n rows guarantees the preconditioned operator with high
+      // probability); above 0.95 the rule stays off.  The error is compared
+      // with ptol times a lower bound on ||Abar z*||: from a zero start
+      // sum_{j<=k} phi_j^2 = ||Abar z_k||^2, which grows to ||Abar z*||^2
+      // without cancellation; from a start point, ||b||^2 - ||r_k||^2 <=
+      // ||b||^2 - ||r*||^2 = ||Abar z*||^2.
+      const double aphi = fabs(phi);
+      s.pred2 += phi * phi;
+      double rate = 0.5;
+      if (s.aphi1 > 0.0) rate = fmax(rate, aphi / s.aphi1);
+      if (s.aphi2 > 0.0 && s.aphi1 > 0.0) rate = fmax(rate, s.aphi1 / s.aphi2);
+      if (a.ptol > 0.0 && itn >= 3 && rate <= 0.95) {
+        const double scale = sqrt(a.has_x0 ? fmax(s.bnorm * s.bnorm - rnorm * rnorm, 0.0) : s.pred2);
+        if (aphi * rate / sqrt(1.0 - rate * rate) <= a.ptol * scale) st = 9;
+      }
+      s.aphi2 = s.aphi1;
+      s.aphi1 = aphi;
       if (!isfinite(s.arnorm) || !isfinite(rnorm)) st = 8;
       s_istop = st;
     }
@@ -573,7 +600,12 @@ __device__ __forceinline__ void lsqr_body(const LsqrArgs& a, const int G, const 
     mat_M(a.v, vscale);
     RLA_SYNC();
   }
-  if (blk == 0 && tid == 0) { a.out[0] = itn; a.out[1] = istop; }
+  if (blk == 0 && tid == 0) {
+    a.out[0] = itn; a.out[1] = istop;
+    if (a.nrm != nullptr) {  // damp = 0: r1norm = r2norm = ||r||
+      a.nrm[0] = s.rnorm; a.nrm[1] = s.rnorm; a.nrm[2] = s.anorm; a.nrm[3] = s.acond; a.nrm[4] = s.xnorm;
+    }
+  }
   if (a.x != nullptr) {  // x = M z
     RLA_SYNC();
     mat_M_to(a.z, 1.0, a.x);
@@ -712,7 +744,7 @@ int lsqr_plan(int dtype, int64_t m, int64_t n, int max_ctas, size_t* smem) {
 int lsqr_enqueue(int dtype, int64_t m, int64_t n, int64_t p, const double* A, const float* A_hi, const float* A_lo,
                  int64_t lda, const double* M, int64_t ldm, double sqrt_delta, const double* b, double* z, int has_x0,
                  double atol, double btol, double conlim, double ptol, int iter_lim, int max_ctas, int* out,
-                 double* arn, void* ws, size_t* ws_bytes, cudaStream_t st) {
+                 double* arn, double* nrm, void* ws, size_t* ws_bytes, cudaStream_t st) {
   size_t smem = 0;
   int G = lsqr_plan(dtype, m, n, max_ctas, &smem);
   LsqrWs L = lsqr_ws_layout(m, n, p, G, iter_lim);
@@ -733,6 +765,7 @@ int lsqr_enqueue(int dtype, int64_t m, int64_t n, int64_t p, const double* A, co
   a.iter_lim = iter_lim;
   a.arn = arn;
   a.out = out;
+  a.nrm = nrm;
   a.u = reinterpret_cast<double*>(base + L.u);
   a.uext = reinterpret_cast<double*>(base + L.uext);
   a.v = reinterpret_cast<double*>(base + L.v);
@@ -758,29 +791,32 @@ int lsqr_enqueue(int dtype, int64_t m, int64_t n, int64_t p, const double* A, co
 extern "C" int rla_lsqr_run(int dtype, int64_t m, int64_t n, int64_t p, const double* A, const float* A_hi,
                             const float* A_lo, int64_t lda, const double* M, int64_t ldm, double sqrt_delta,
                             const double* b, double* z, int has_x0, double atol, double btol, double conlim,
-                            int iter_lim, double* arnorms, int* itn, int* istop, void* ws, size_t* ws_bytes,
-                            rla_stream_t stream) {
+                            int iter_lim, double* arnorms, int* itn, int* istop, double* norms, void* ws,
+                            size_t* ws_bytes, rla_stream_t stream) {
   using namespace rla;
   if (m < 0 || n <= 0 || p <= 0 || iter_lim < 0 || lda < n || ldm < p) return RLA_ERR_ARG;
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-  // the sync entry point keeps its out/arn in the tail of the workspace
+  // the sync entry point keeps out (int[3] at +0), the norms (double[5] at
+  // +64) and arn (at +256) in the tail of the workspace
   const size_t tail = 256 + sizeof(double) * static_cast<size_t>(max(iter_lim, 1));
   size_t core = 0;
   int rc = lsqr_enqueue(dtype, m, n, p, A, A_hi, A_lo, lda, M, ldm, sqrt_delta, b, z, has_x0, atol, btol, conlim,
-                        0.0, iter_lim, 0, nullptr, nullptr, nullptr, &core, st);
+                        0.0, iter_lim, 0, nullptr, nullptr, nullptr, nullptr, &core, st);
   if (rc) return rc;
   if (ws == nullptr && ws_bytes != nullptr) { *ws_bytes = core + tail; return RLA_OK; }
   if (!ws || (ws_bytes && *ws_bytes < core + tail)) return RLA_ERR_WORKSPACE;
   if (!arnorms || !itn || !istop) return RLA_ERR_ARG;
   char* base = static_cast<char*>(ws);
   int* out = reinterpret_cast<int*>(base + core);
+  double* nrm = reinterpret_cast<double*>(base + core + 64);
   double* arn = reinterpret_cast<double*>(base + core + 256);
   size_t cb = core;
   rc = lsqr_enqueue(dtype, m, n, p, A, A_hi, A_lo, lda, M, ldm, sqrt_delta, b, z, has_x0, atol, btol, conlim,
-                    0.0, iter_lim, 0, out, arn, ws, &cb, st);
+                    0.0, iter_lim, 0, out, arn, nrm, ws, &cb, st);
   if (rc) return rc;
   int hout[3] = {0, 0, 0};
   RLA_CUDA_TRY(cudaMemcpyAsync(hout, out, sizeof(hout), cudaMemcpyDeviceToHost, st));
+  if (norms) RLA_CUDA_TRY(cudaMemcpyAsync(norms, nrm, 5 * sizeof(double), cudaMemcpyDeviceToHost, st));
   if (iter_lim > 0) RLA_CUDA_TRY(cudaMemcpyAsync(arnorms, arn, sizeof(double) * iter_lim, cudaMemcpyDeviceToHost, st));
   RLA_CUDA_TRY(cudaStreamSynchronize(st));
   *itn = hout[0];
@@ -793,12 +829,13 @@ extern "C" int rla_lsqr_run(int dtype, int64_t m, int64_t n, int64_t p, const do
 extern "C" int rla_lsqr_launch(int dtype, int64_t m, int64_t n, int64_t p, const double* A, const float* A_hi,
                                const float* A_lo, int64_t lda, const double* M, int64_t ldm, double sqrt_delta,
                                const double* b, double* z, int has_x0, double atol, double btol, double conlim,
-                               double ptol, int iter_lim, int max_ctas, int* out, double* arnorms, void* ws,
-                               size_t* ws_bytes, rla_stream_t stream) {
+                               double ptol, int iter_lim, int max_ctas, int* out, double* arnorms, double* norms,
+                               void* ws, size_t* ws_bytes, rla_stream_t stream) {
   using namespace rla;
   if (m < 0 || n <= 0 || p <= 0 || iter_lim < 0 || lda < n || ldm < p || max_ctas < 0 || ptol < 0) return RLA_ERR_ARG;
   return lsqr_enqueue(dtype, m, n, p, A, A_hi, A_lo, lda, M, ldm, sqrt_delta, b, z, has_x0, atol, btol, conlim,
-                      ptol, iter_lim, max_ctas, out, arnorms, ws, ws_bytes, reinterpret_cast<cudaStream_t>(stream));
+                      ptol, iter_lim, max_ctas, out, arnorms, norms, ws, ws_bytes,
+                      reinterpret_cast<cudaStream_t>(stream));
 }
 
 extern "C" int rla_split_f64(int64_t rows, int64_t cols, const double* x, int64_t ldx, float* hi, float* lo,
@@ -920,7 +957,8 @@ extern "C" size_t rla_lsqr_record_size(void) { return sizeof(rla::LsqrArgs); }
 extern "C" int rla_lsqr_record(void* rec, int64_t m, int64_t n, int64_t p, const double* A, const float* A_hi,
                                const float* A_lo, int64_t lda, const double* M, int64_t ldm, double sqrt_delta,
                                const double* b, double* z, int has_x0, double atol, double btol, double conlim,
-                               double ptol, int iter_lim, int* out, double* arnorms, double* x, void* ws) {
+                               double ptol, int iter_lim, int* out, double* arnorms, double* norms, double* x,
+                               void* ws) {
   using namespace rla;
   if (!rec || m < 0 || n <= 0 || p <= 0 || lda < n || ldm < p || !ws || !out || !arnorms) return RLA_ERR_ARG;
   LsqrWs L = lsqr_ws_layout(m, n, p, kLsqrMaxCluster, iter_lim);
@@ -928,7 +966,7 @@ extern "C" int rla_lsqr_record(void* rec, int64_t m, int64_t n, int64_t p, const
   LsqrArgs a{};
   a.m = m; a.n = n; a.p = p; a.A = A; a.Ahi = A_hi; a.Alo = A_lo; a.lda = lda; a.M = M; a.ldm = ldm;
   a.sd = sqrt_delta; a.b = b; a.z = z; a.has_x0 = has_x0; a.atol = atol; a.btol = btol; a.conlim = conlim;
-  a.ptol = ptol; a.iter_lim = iter_lim; a.arn = arnorms; a.out = out; a.x = x;
+  a.ptol = ptol; a.iter_lim = iter_lim; a.arn = arnorms; a.out = out; a.x = x; a.nrm = norms;
   a.u = reinterpret_cast<double*>(base + L.u);
   a.uext = reinterpret_cast<double*>(base + L.uext);
   a.v = reinterpret_cast<double*>(base + L.v);

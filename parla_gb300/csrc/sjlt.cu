@@ -371,13 +371,20 @@ int rla_sjlt_apply_right(int dtype, int64_t m, int64_t n, int64_t k, int nnz, co
 //   the library holds it until the process exits.
 // - Problems whose partials exceed it are rejected with RLA_ERR_WORKSPACE.
 // - The first call on a device looks up the array's device address with
-//   cudaGetSymbolAddress (with that device current) and caches it; make that
-//   first call before any stream capture on the device.
+//   cudaGetSymbolAddress (with that device current) and caches it together
+//   with the CUDA context that was current; make that first call before any
+//   stream capture on the device.  A call under another context on the same
+//   device (a non-primary context) looks the address up again.  After
+//   cudaDeviceReset the primary context may come back under the same handle,
+//   so the cached address must not outlive a reset: do not reset a device
+//   between calls of this entry point.
 // - All calls share the array.  Every partial is written before it is read,
 //   so nothing has to be cleared between calls, but calls that overlap on the
 //   GPU (different streams, or different host threads) race on it and must
 //   be serialised by the caller.
 // - No cudaMalloc, cudaFree or allocating library routine is called.
+#include <cuda.h>
+
 #include <mutex>
 
 static constexpr size_t kNoAllocScratchBytes = size_t(16) << 20;
@@ -386,19 +393,48 @@ static __device__ __align__(256) double rla_noalloc_scratch[kNoAllocScratchBytes
 namespace rla {
 namespace {
 std::mutex g_noalloc_mu;
-double* g_noalloc_ptr[64] = {};
+struct NoAllocSlot {
+  CUcontext ctx;
+  double* ptr;
+};
+NoAllocSlot g_noalloc[64] = {};
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+
+// The current CUDA context through the driver entry point that the runtime
+// hands out (no link against the driver library).
+int current_context(CUcontext* ctx) {
+  if (g_ctx_get_current == nullptr) {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    RLA_CUDA_TRY(cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 4000, cudaEnableDefault, &q));
+    if (fn == nullptr || q != cudaDriverEntryPointSuccess) return RLA_ERR_UNSUPPORTED;
+    g_ctx_get_current = reinterpret_cast<CtxGetCurrentFn>(fn);
+  }
+  if (g_ctx_get_current(ctx) != CUDA_SUCCESS) return RLA_ERR_CUDA;
+  return RLA_OK;
+}
 
 int noalloc_scratch_ptr(double** out) {
   int dev = 0;
   RLA_CUDA_TRY(cudaGetDevice(&dev));
   if (dev < 0 || dev >= 64) return RLA_ERR_UNSUPPORTED;
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (g_noalloc_ptr[dev] == nullptr) {
+  CUcontext ctx = nullptr;
+  int rc = current_context(&ctx);
+  if (rc != RLA_OK) return rc;
+  NoAllocSlot& slot = g_noalloc[dev];
+  if (slot.ptr == nullptr || ctx == nullptr || slot.ctx != ctx) {
+    // (the lookup also makes the device's primary context current when no
+    // context is, so the context is read again after it)
     void* p = nullptr;
     RLA_CUDA_TRY(cudaGetSymbolAddress(&p, rla_noalloc_scratch));
-    g_noalloc_ptr[dev] = static_cast<double*>(p);
+    rc = current_context(&ctx);
+    if (rc != RLA_OK) return rc;
+    slot.ptr = static_cast<double*>(p);
+    slot.ctx = ctx;
   }
-  *out = g_noalloc_ptr[dev];
+  *out = slot.ptr;
   return RLA_OK;
 }
 

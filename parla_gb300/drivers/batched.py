@@ -202,7 +202,7 @@ class BatchedSPO:
             n = it["n"]
             _lib.call("rla_lsqr_launch", K.MODES["df"], it["m"], n, n, None, K.ptr(it["hi"]), K.ptr(it["lo"]), n,
                       K.ptr(it["Rinv"]), n, 0.0, K.ptr(b), K.ptr(it["z"]), 1, 0.0, 0.0, 0.0, float(self.ptol),
-                      int(self.iter_lim), 0, K.ptr(it["out"]), K.ptr(it["arn"]), K.ptr(it["coop_ws"]),
+                      int(self.iter_lim), 0, K.ptr(it["out"]), K.ptr(it["arn"]), None, K.ptr(it["coop_ws"]),
                       C.byref(C.c_size_t(it["coop_ws"].numel())), K.stream())
         # one persistent launch per cluster size, each on its own stream with
         # its CTA budget, so that the classes run side by side
@@ -234,7 +234,7 @@ class BatchedSPO:
             _lib.call("rla_lsqr_record", C.c_void_p(rec), it["m"], it["n"], it["n"], None, K.ptr(it["hi"]),
                       K.ptr(it["lo"]), it["n"], K.ptr(it["Rinv"]), it["n"], 0.0, K.ptr(b), K.ptr(it["z"]), 1,
                       0.0, 0.0, 0.0, float(self.ptol), int(self.iter_lim), K.ptr(it["out"]), K.ptr(it["arn"]),
-                      K.ptr(it["x"]), K.ptr(it["ws"]))
+                      None, K.ptr(it["x"]), K.ptr(it["ws"]))
         dev = K.device()
         order = plan["order"]
         qr_big = []
@@ -259,7 +259,7 @@ class BatchedSPO:
             need = _lib.size_query("rla_lsqr_launch", K.MODES["df"], it["m"], n, n, None, K.ptr(it["hi"]),
                                    K.ptr(it["lo"]), n, K.ptr(it["Rinv"]), n, 0.0, K.ptr(plan["problems"][i][1]),
                                    K.ptr(it["z"]), 1, 0.0, 0.0, 0.0, float(self.ptol), int(self.iter_lim), 0,
-                                   K.ptr(it["out"]), K.ptr(it["arn"]))
+                                   K.ptr(it["out"]), K.ptr(it["arn"]), None)
             it["coop_ws"] = torch.empty(max(need, 256), dtype=torch.uint8, device=dev)
         plan.update(qr_big=qr_big, ls_big=ls_big, n_qr_small=len(qr_small), n_ls_small=len(ls_small))
         import struct

@@ -2,7 +2,7 @@
 
 Run in a container that holds the reference source tree::
 
-    python tests/golden/make_golden.py /root/reference [fixture names ...]
+    python tests/golden/make_golden.py <reference source tree> [fixture names ...]
 
 The reference targets NumPy 1.x; two names it uses were removed in NumPy 2
 (``np.NaN`` and ``np.row_stack``), so they are restored as aliases before the
@@ -263,6 +263,29 @@ def lowrank_cases(parla):
     return out
 
 
+def ls_fixtures(parla):
+    """SHA-256 digests of the reference test suite's least-squares problems.
+
+    The builders live in the reference's test module
+    (parla/tests/test_drivers/test_optim/test_overdet_least_squares.py:11-108);
+    the arrays are large, so only digests of A and b and the small x_opt are
+    kept.  ``tests/lsfixtures.py`` restates the builders and must match.
+    """
+    sys.path.insert(0, HERE)
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    from tests.lsfixtures import digest
+    import importlib
+    mod = importlib.import_module('parla.tests.test_drivers.test_optim.test_overdet_least_squares')
+    out = {}
+    for name in ('consistent_tall', 'consistent_lowrank', 'consistent_square', 'inconsistent_orthog',
+                 'inconsistent_gen', 'inconsistent_stackid'):
+        ath = getattr(mod, name)()
+        out[f'{name}_A'] = digest(ath.A)
+        out[f'{name}_b'] = digest(ath.b)
+        out[f'{name}_x'] = np.asarray(ath.x_opt, dtype=np.float64)
+    return out
+
+
 def main(ref_path, only=None):
     """Write every fixture, or only those named in ``only``."""
     parla = _import_reference(ref_path)
@@ -270,7 +293,7 @@ def main(ref_path, only=None):
                 parla=parla.__version__)
     for name, fn in (('sketch', sketches), ('lsqr', lsqr_case),
                      ('spo', spo_cases), ('spu', spu_cases), ('sps', sps_cases),
-                     ('lowrank', lowrank_cases)):
+                     ('lowrank', lowrank_cases), ('lsfix', ls_fixtures)):
         if only and name not in only:
             continue
         data = fn(parla)
@@ -281,4 +304,6 @@ def main(ref_path, only=None):
 
 
 if __name__ == '__main__':
-    main(sys.argv[1] if len(sys.argv) > 1 else '/root/reference', sys.argv[2:])
+    if len(sys.argv) < 2:
+        sys.exit('usage: make_golden.py <path to the reference source tree> [fixture names ...]')
+    main(sys.argv[1], sys.argv[2:])

@@ -87,3 +87,51 @@ def test_batched_single_large_problem_cooperative(pg):
     xs = solver(probs, rng=6)
     assert solver.last_layout["cooperative"] == 1
     _check(probs, xs, solver.last_info)
+
+
+def _pred_err(A, x, b):
+    """||A (x - x*)|| / ||A x*|| against LAPACK; ||A x|| / ||b|| when x* = 0."""
+    xr = la.lstsq(A, b)[0]
+    axr = la.norm(A @ xr)
+    if axr <= 1e-12 * la.norm(b):
+        return la.norm(A @ x) / la.norm(b)
+    return la.norm(A @ (x - xr)) / axr
+
+
+@pytest.fixture(scope="module")
+def hard_batch(pg):
+    """The reference test suite's six least-squares problems (three of them
+    inconsistent) and problems of the batched workload's shapes with large
+    residuals."""
+    from tests import lsfixtures as F
+    items = [(name, *fn()[:2]) for name, fn in sorted(F.ALL.items())]
+    items += [(f"large_residual{args}", *F.large_residual(*args)[:2]) for args in F.LARGE_RESIDUAL_BATCH]
+    return items
+
+
+@pytest.mark.parametrize("route", ["call_mixed", "call_f64", "graph_replay"])
+def test_batched_hard_problems(pg, hard_batch, route):
+    """BatchedSPO on inconsistent and large-residual problems, through the
+    plain call and through a captured CUDA graph replayed twice (outputs
+    poisoned with NaN before each replay), at the 1e-10 prediction gate."""
+    probs = [(torch.from_numpy(A).cuda(), torch.from_numpy(b).cuda()) for _, A, b in hard_batch]
+    if route == "graph_replay":
+        solver = pg.BatchedSPO(precision="mixed", streams=4)
+        replay = solver.capture(probs, rng=9)
+        for _ in range(2):
+            for it in replay.plan["items"]:
+                it["x"].fill_(float("nan"))
+            xs = replay()
+            torch.cuda.synchronize()
+            infos = solver.info_from_plan(replay.plan)
+            for (name, A, b), x, info in zip(hard_batch, xs, infos):
+                err = _pred_err(A, x.cpu().numpy(), b)
+                assert err <= 1e-10, (name, info, err)
+                assert info["err"] == 0
+        return
+    solver = pg.BatchedSPO(precision="mixed" if route == "call_mixed" else "f64", streams=4)
+    xs = solver(probs, rng=9)
+    for (name, A, b), x, info in zip(hard_batch, xs, solver.last_info):
+        err = _pred_err(A, x.cpu().numpy(), b)
+        assert err <= 1e-10, (name, info, err)
+        assert info["err"] == 0

@@ -345,3 +345,79 @@ def test_evd2_bf16_rbf_eigenvalues(pg):
     assert np.all(lam64[top] <= lam_ref[top] * (1 + 1e-9))
     Vd = V.double()
     assert float((Vd.t() @ Vd - torch.eye(lam.size, dtype=torch.float64, device="cuda")).abs().max()) <= 1e-4
+
+
+# --- the reference test suite's least-squares problems and checks
+# (parla/tests/test_drivers/test_optim/test_overdet_least_squares.py:113-320)
+
+def _lstsq_pred_err(A, x, b):
+    xr = la.lstsq(A, b)[0]
+    axr = la.norm(A @ xr)
+    if axr <= 1e-12 * la.norm(b):          # b orthogonal to range(A): x* = 0
+        return la.norm(A @ x) / la.norm(b)
+    return la.norm(A @ (x - xr)) / axr
+
+
+def _reference_properties(A, b, x, x_opt, tol):
+    """test_residual_proj, test_x_angle and test_x_norm of the reference."""
+    U, _, Vt = la.svd(A, full_matrices=False)
+    res = A @ x - b
+    assert la.norm(U @ (U.T @ res)) / la.norm(res) <= tol
+    y_opt, y = Vt @ x_opt, Vt @ x
+    if la.norm(y_opt) < 1e-8:
+        assert abs(la.norm(y) - la.norm(y_opt)) <= tol
+    else:
+        assert np.dot(y / la.norm(y), y_opt / la.norm(y_opt)) >= 1 - tol
+    assert la.norm(y) <= (1 + tol) * la.norm(y_opt) + tol
+    assert (1 - tol) * la.norm(y_opt) <= la.norm(y)
+
+
+@pytest.mark.parametrize("precision", ["f64", "df"])
+@pytest.mark.parametrize("name", ["inconsistent_orthog", "inconsistent_gen"])
+def test_spo_reference_inconsistent(pg, precision, name):
+    """SPO(SkOpGA(), 3) at tol 1e-12, iter_lim 100 over the reference's seeds
+    (its test_inconsistent_orth_qr / test_inconsistent_gen_qr), plus the
+    1e-10 prediction gate against LAPACK."""
+    from tests import lsfixtures as F
+    A, b, x_opt = F.ALL[name]()
+    for seed in (1, 4, 15, 31, 42):
+        x, _ = pg.SPO(pg.SkOpGA(), 3, "qr", precision)(A, b, 0.0, 1e-12, 100, seed)
+        _reference_properties(A, b, x, x_opt, 1e-6)
+        assert _lstsq_pred_err(A, x, b) <= 1e-10, seed
+
+
+@pytest.mark.parametrize("gname", ["ga", "sj", "tc"])
+@pytest.mark.parametrize("mode", ["qr", "chol"])
+@pytest.mark.parametrize("name", ["inconsistent_gen", "inconsistent_stackid"])
+def test_spo_reference_convergence_rate(pg, gname, mode, name):
+    """The reference's _test_convergence_rate: SPO(sampling factor 2) logs a
+    linearly converging error (log-linear fit r^2 >= 0.95, slope < -0.3) that
+    ends at or below 1e-6."""
+    from tests import lsfixtures as F
+    A, b, _ = F.ALL[name]()
+    x, log = pg.SPO(gpu_gen(pg, gname), 2, mode)(A, b, 0.0, 1e-12, 100, 34998751340)
+    e = np.asarray(log.errors)[1:]
+    t = np.arange(e.size)
+    fit = np.polyfit(t, np.log(e), 1)
+    pred = np.polyval(fit, t)
+    r2 = 1 - np.sum((np.log(e) - pred) ** 2) / np.sum((np.log(e) - np.log(e).mean()) ** 2)
+    assert r2 >= 0.95 and fit[0] < -0.3, (r2, fit)
+    assert log.errors[-1] <= 1e-6
+    assert _lstsq_pred_err(A, x, b) <= 1e-10
+
+
+def test_lsqr_returns_reference_norms(pg):
+    """lsqr's 10-tuple: r1norm, r2norm, anorm, acond and xnorm are the device
+    loop's estimates and match the oracle's (same recurrences, binary64)."""
+    from parla_gb300.comps.determiter.lsqr import lsqr as dev_lsqr
+    rng = np.random.default_rng(44)
+    As = rng.standard_normal((500, 30))
+    b = As @ rng.standard_normal(30) + rng.standard_normal(500)      # inconsistent
+    res = dev_lsqr(As, b, atol=1e-10, btol=1e-10, iter_lim=100)
+    ref = oracle.lsqr(lambda v: As @ v, lambda u: As.T @ u, As.shape[1], b, atol=1e-10, btol=1e-10,
+                      iter_lim=100)
+    assert res[1] == ref[1] and res[2] == ref[2]
+    for i in (3, 4, 5, 6, 8):
+        assert np.isfinite(res[i])
+        assert abs(res[i] - ref[i]) <= 1e-8 * abs(ref[i]), (i, res[i], ref[i])
+    assert res[3] == res[4]

@@ -68,7 +68,13 @@ def test_noalloc_matches_regular_twice(lib, dtype, tol):
 
 
 def test_noalloc_rejects_oversized_problem(lib):
-    # 25600 x 4096 outputs need more partial storage than the fixed 16 MiB array
-    st = lib.call_status("rla_sjlt_apply_noalloc", lib.RLA_F64, 12800, 4096 * 64, 4096, 8,
-                         C.c_void_p(8), C.c_void_p(8), 0.35, C.c_void_p(8), 4096, C.c_void_p(8), 4096, None)
+    # a 2048 x 1100 binary64 result needs 18 MB of partial sums, more than the
+    # fixed 16 MiB array; every buffer is real and in bounds
+    d, m, n, nnz = 2048, 64, 1100, 8
+    rows, signs, A = _case(3, d, m, n, nnz, torch.float64)
+    Y = torch.zeros((d, n), dtype=torch.float64, device="cuda")
+    st = lib.call_status("rla_sjlt_apply_noalloc", lib.RLA_F64, d, m, n, nnz, _p(rows), _p(signs), nnz ** -0.5,
+                         _p(A), n, _p(Y), n, None)
+    torch.cuda.synchronize()
     assert st == 8  # RLA_ERR_WORKSPACE
+    assert not torch.any(Y != 0)
