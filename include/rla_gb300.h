@@ -186,6 +186,38 @@ int rla_geqrf_ctas(int dtype, int64_t m, int64_t n, int64_t nrhs, double* A,
                    int64_t lda, double* tau, int max_ctas, void* ws,
                    size_t* ws_bytes, rla_stream_t stream);
 
+/* Householder QR with column pivoting of the first n columns of A
+ * (m x (n + nrhs), COLUMN-major, column stride lda), in place, LAPACK geqp3
+ * semantics: at step i the pivot is the first remaining column with the
+ * largest partial norm, partial norms are downdated and recomputed by
+ * LAPACK's rule, reflectors as dlarfg.  Only kmax <= min(m, n) reflectors are
+ * formed (the first kmax rows of R and the first kmax pivots; kmax =
+ * min(m, n) for the full factorization).  On exit A holds R and the
+ * reflectors in pivoted column order, the nrhs trailing columns hold Q^T
+ * times themselves, tau[kmax] the reflector scalars and jpvt[n] (device
+ * int64) the 0-based pivot order.  dtype RLA_F64 or RLA_DF; one cooperative
+ * launch over all SMs with a bounded grid barrier per reflector (status via
+ * rla_geqp3_status), n <= 24576.  Replaces la.qr(Y, mode='economic',
+ * pivoting=True) at parla/comps/interpolative.py:52,146,153 and
+ * parla/drivers/interpolative.py:163,171,375,383. */
+int rla_geqp3(int dtype, int64_t m, int64_t n, int64_t nrhs, int64_t kmax,
+              double* A, int64_t lda, double* tau, int64_t* jpvt, void* ws,
+              size_t* ws_bytes, rla_stream_t stream);
+
+/* Reads the grid-barrier status (0 or RLA_ERR_TIMEOUT) that the last
+ * rla_geqp3 left in `ws`; synchronises `stream`. */
+int rla_geqp3_status(const void* ws, int* status, rla_stream_t stream);
+
+/* X = R^-1 B for an upper-triangular k x k R (k <= 2048), binary64, all
+ * COLUMN-major (column c of R, B and X at R + c*ldr, B + c*ldb, X + c*ldx):
+ * the layout rla_geqp3 leaves R and Q^T b in.  Replaces
+ * la.solve_triangular(S[:k, :k], S[:k, k:]) at
+ * parla/comps/interpolative.py:53-55 and the triangular solves of the
+ * least-squares pseudo-inverses, parla/utils/linalg_wrappers.py:29-38. */
+int rla_trsm_upper(int64_t k, int64_t nrhs, const double* R, int64_t ldr,
+                   const double* B, int64_t ldb, double* X, int64_t ldx,
+                   rla_stream_t stream);
+
 /* Q (m x n, column-major) = thin orthonormal factor of rla_geqrf's result.
  * Replaces la.qr(Y)[0] at parla/comps/rangefinders.py:187 and orth,
  * parla/utils/linalg_wrappers.py:6-7. */

@@ -2,7 +2,8 @@
 
 Same names and call signatures as the reference package (``parla/__init__.py``):
 sketch generators (SkOpGA, SkOpSJ, SkOpTC), RS1, RF1, QB1, QB2, QB3, SVD1, EVD1,
-EVD2, SPO, SSO1, SPU1, SPS1 and SPS2.  Products, factorizations and LSQR run in the CUDA
+EVD2, SPO, SSO1, SPU1, SPS1, SPS2 and the interpolative decompositions (qrcp_osid,
+ROCS1, OSID1, OSID2, TSID1, CUR1).  Products, factorizations and LSQR run in the CUDA
 kernels of ``librla_gb300.so`` (C ABI in ``include/rla_gb300.h``).
 """
 __version__ = "0.1.0"
@@ -23,5 +24,8 @@ from .drivers.saddlesys import SaddleSolver, SPS1, SPS2
 from .drivers.batched import BatchedSPO
 from .drivers.svd import SVDecomposer, SVD1
 from .drivers.evd import EVDecomposer, EVD1, EVD2
+from .comps.interpolative import qrcp_osid, RowOrColSelection, ROCS1, rocs1
+from .drivers.interpolative import (OneSidedID, OSID1, OSID2, osid1, osid2, TwoSidedID, TSID1, tsid1,
+                                    CURDecomposition, CUR1, cur1)
 from .utils.linalg_wrappers import orth, cholqr
 from .autotune import Tuner

@@ -246,6 +246,43 @@ def geqrf_colmajor(T, n, mode="f64"):
     return tau
 
 
+def geqp3_colmajor(T, n, kmax=None, mode="f64", check=True):
+    """Column-pivoted Householder QR of the column-major matrix stored as T.
+
+    T is (n + nrhs) x m row-major, i.e. an m x (n + nrhs) column-major
+    matrix; the first n columns are factored with pivoting (kmax reflectors,
+    default min(m, n)), the nrhs trailing columns receive Q^T.  On return
+    T[:n] holds R (upper part of T[:n, :kmax].T) and the reflectors in
+    pivoted column order, as LAPACK geqp3 leaves them.  Returns (tau, jpvt)
+    with jpvt the 0-based pivot order (int64, device).
+    """
+    ncols, m = T.shape
+    nrhs = ncols - n
+    kmax = min(m, n) if kmax is None else int(kmax)
+    tau = torch.empty(max(kmax, 1), dtype=torch.float64, device=T.device)
+    jpvt = torch.empty(max(n, 1), dtype=torch.int64, device=T.device)
+    head = (MODES[mode], m, n, nrhs, kmax, ptr(T), T.stride(0), ptr(tau), ptr(jpvt))
+    need = size_query("rla_geqp3", *head)
+    ws = workspace(need)
+    nb = C.c_size_t(need)
+    _timed("geqp3", 1, call, "rla_geqp3", *head, ptr(ws), C.byref(nb), stream())
+    if check:
+        st = C.c_int(0)
+        call("rla_geqp3_status", ptr(ws), C.byref(st), stream())
+        if st.value:
+            raise _lib.RlaError("rla_geqp3", st.value, "grid barrier timed out")
+    return tau[:kmax], jpvt[:n]
+
+
+def trsm_upper_colmajor(k, R, B, X):
+    """X = R^-1 B, all column-major stored as rows of the given tensors:
+    column c of R is R[c, :k], of B is B[c, :k] and of X is X[c, :k]."""
+    nrhs = B.shape[0]
+    _timed("trsm", 1, call, "rla_trsm_upper", k, nrhs, ptr(R), R.stride(0), ptr(B), B.stride(0), ptr(X),
+           X.stride(0), stream())
+    return X
+
+
 def orgqr_colmajor(T, n, tau, mode="f64"):
     """Thin Q (column-major, returned as n x m row-major = Q^T) from geqrf output."""
     m = T.shape[1]

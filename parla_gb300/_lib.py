@@ -51,6 +51,9 @@ SIGNATURES = {
     "rla_gemm_bf16_tc_status": [_p, C.POINTER(C.c_int), _p],
     "rla_geqrf": [_i32, _i64, _i64, _i64, _p, _i64, _p, _p, _psz, _p],
     "rla_geqrf_ctas": [_i32, _i64, _i64, _i64, _p, _i64, _p, _i32, _p, _psz, _p],
+    "rla_geqp3": [_i32, _i64, _i64, _i64, _i64, _p, _i64, _p, _p, _p, _psz, _p],
+    "rla_geqp3_status": [_p, C.POINTER(C.c_int), _p],
+    "rla_trsm_upper": [_i64, _i64, _p, _i64, _p, _i64, _p, _i64, _p],
     "rla_lsqr_launch": [_i32, _i64, _i64, _i64, _p, _p, _p, _i64, _p, _i64, _f64, _p, _p, _i32, _f64, _f64,
                         _f64, _f64, _i32, _i32, _p, _p, _p, _p, _psz, _p],
     "rla_residual_df": [_i64, _i64, _p, _p, _i64, _p, _p, _p, _p],

@@ -184,3 +184,66 @@ def orth_tc(Y, passes=1):
         Rinv = _chol_inv_f32(G)
         Qt = K.gemm(Rinv, Qt, transa=True, mode="f32")
     return Qt.t()
+
+
+# ----------------------------------------------------------------------------
+# Column-pivoted QR and the pseudo-inverse applications of the interpolative
+# decompositions (``parla/utils/linalg_wrappers.py:29-38`` and the
+# ``la.qr(..., pivoting=True)`` calls of ``parla/comps/interpolative.py`` and
+# ``parla/drivers/interpolative.py``), binary64 on the device.
+
+def qrcp(Y, kmax=None, rhs=None):
+    """QR with column pivoting of the device matrix Y (p x q, binary64).
+
+    Returns (T, jpvt): T ((q + r) x p) holds the factored matrix column-major
+    (row j of T is column j of R and of the reflectors, pivoted order), with
+    Q^T rhs in its last r rows when ``rhs`` (p x r) is given; jpvt the 0-based
+    pivot order (device int64).  Only the first ``kmax`` reflectors (default
+    min(p, q)) are formed.
+    """
+    Y = Y if Y.dtype == torch.float64 else Y.to(torch.float64)
+    parts = [Y.t()] if rhs is None else [Y.t(), rhs.to(torch.float64).t()]
+    T = torch.cat(parts, dim=0).contiguous() if rhs is not None else Y.t().contiguous()
+    _, jpvt = K.geqp3_colmajor(T, Y.shape[1], kmax=kmax, mode="f64")
+    return T, jpvt
+
+
+def skeleton(Y, k):
+    """The first k pivots of a QR with column pivoting of Y (device int64)."""
+    return qrcp(Y, kmax=min(k, *Y.shape))[1][:k]
+
+
+def _numerical_rank(T, kmax, p, q):
+    d = torch.abs(torch.diagonal(T[:kmax, :kmax]))
+    if kmax == 0 or float(d[0]) == 0.0:
+        return 0
+    tol = float(d[0]) * max(p, q) * float(torch.finfo(torch.float64).eps)
+    return int(torch.count_nonzero(d > tol))
+
+
+def apply_pinv_on_left(target, operator):
+    """pinv(operator) @ target (least squares, ``parla/utils/linalg_wrappers.py:29-32``).
+
+    Basic solution from a QR with column pivoting, truncated at the numerical
+    rank (|r_ii| > |r_00| max(p, q) eps): operator P = Q R, X[P[:r]] =
+    R11^-1 (Q^T target)[:r], the other rows zero.  With full column rank this
+    is the least-squares solution; with lower rank it is a least-squares
+    solution (operator @ X is the projection of target either way).
+    """
+    target = target if target.dim() == 2 else target.view(-1, 1)
+    p, q = operator.shape
+    r = target.shape[1]
+    kmax = min(p, q)
+    T, jpvt = qrcp(operator, kmax=kmax, rhs=target)
+    rank = _numerical_rank(T, kmax, p, q)
+    X = torch.zeros((q, r), dtype=torch.float64, device=T.device)
+    if rank > 0:
+        Zt = torch.empty((r, rank), dtype=torch.float64, device=T.device)
+        K.trsm_upper_colmajor(rank, T, T[q:], Zt)
+        X[jpvt[:rank]] = Zt.t()
+    return X
+
+
+def apply_pinv_on_right(target, operator):
+    """target @ pinv(operator) (``parla/utils/linalg_wrappers.py:35-38``)."""
+    return apply_pinv_on_left(target.t(), operator.t()).t().contiguous()

@@ -286,6 +286,95 @@ def ls_fixtures(parla):
     return out
 
 
+# (m, n, rank, k, over, axis, seed) of the reference's OSID tests
+# (parla/tests/test_drivers/test_lowrank/test_osid.py:51-81), num_pass 0 / 2
+OSID_CASES = {0: [(100, 30, 29, 29, 0, 0, 0), (100, 30, 28, 28, 1, 0, 2), (100, 30, 3, 3, 0, 0, 2),
+                  (100, 30, 29, 29, 0, 1, 0), (100, 30, 28, 28, 1, 1, 2), (100, 30, 3, 3, 2, 1, 2)],
+              2: [(100, 30, 30, 27, 3, 0, 0), (100, 30, 30, 25, 4, 0, 0), (100, 30, 30, 5, 5, 0, 0),
+                  (30, 100, 30, 27, 3, 1, 0), (30, 100, 30, 25, 4, 1, 0), (30, 100, 30, 5, 5, 0, 0)]}
+# (m, n, rank, k, over, seed) of the TSID tests (test_tsid.py:41-80)
+TSID_CASES = {0: [(1000, 300, 290, 290, 0, 0), (1000, 300, 290, 290, 5, 2), (1000, 300, 30, 30, 0, 2),
+                  (300, 1000, 290, 290, 0, 0), (300, 1000, 290, 290, 5, 2), (300, 1000, 30, 30, 0, 2)],
+              2: [(100, 30, 30, 27, 3, 0), (100, 30, 30, 25, 4, 0), (30, 100, 30, 27, 3, 0),
+                  (30, 100, 30, 25, 4, 0)]}
+# (m, n, rank, k, over, seed) of the CUR tests (test_cur.py:34-75), num_pass 0 / 4
+CUR_CASES = {0: [(100, 30, 24, 25, 3, 0), (100, 30, 5, 5, 1, 2), (30, 100, 24, 25, 3, 0), (30, 100, 5, 5, 1, 2)],
+             4: [(100, 30, 30, 27, 3, 0), (100, 30, 30, 25, 4, 0), (100, 30, 30, 5, 5, 0),
+                 (30, 100, 30, 27, 3, 0), (30, 100, 30, 25, 4, 0), (30, 100, 30, 5, 5, 0)]}
+
+
+def interp_cases(parla):
+    """Outputs of the reference's interpolative decompositions on its own test
+    configurations: the matrix comes from rand_low_rank(m, n, rank, rng) and
+    the algorithm continues the same Generator, as in the reference's tests.
+    Large coefficient matrices are stored as fingerprints (products with a
+    fixed Gaussian vector) next to their digests."""
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    from tests.lsfixtures import digest
+    import parla.tests.matmakers as mm
+    import parla.comps.sketchers.oblivious as obl
+    import parla.utils.linalg_wrappers as ulaw
+    from parla.comps.sketchers.aware import RS1
+    from parla.drivers.interpolative import OSID1, OSID2, TSID1, CUR1
+    from parla.comps.interpolative import ROCS1, qrcp_osid
+    out = {}
+
+    def rs(p):
+        return RS1(sketch_op_gen=obl.SkOpGA(), num_pass=p, stabilizer=ulaw.orth, passes_per_stab=1)
+
+    def keep(tag, M):
+        M = np.asarray(M, dtype=np.float64)
+        if M.size <= 4000:
+            out[tag] = M
+        else:
+            g = np.random.default_rng(99).standard_normal(M.shape[1])
+            out[tag + '_fp'] = M @ g
+            out[tag + '_digest'] = digest(M)
+
+    for p, cases in OSID_CASES.items():
+        for ci, (m, n, rank, k, over, axis, seed) in enumerate(cases):
+            for an, cls in (('osid1', OSID1), ('osid2', OSID2)):
+                rng = np.random.default_rng(seed)
+                A = mm.rand_low_rank(m, n, rank, rng)
+                M, P = cls(rs(p))(A, k, over, axis, rng)
+                tag = f'{an}_p{p}_{ci}'
+                out[tag + '_A'] = digest(A)
+                keep(tag + '_M', M)
+                out[tag + '_P'] = np.asarray(P, dtype=np.int64)
+    for p, cases in TSID_CASES.items():
+        for ci, (m, n, rank, k, over, seed) in enumerate(cases):
+            rng = np.random.default_rng(seed)
+            A = mm.rand_low_rank(m, n, rank, rng)
+            Z, I, X, J = TSID1(OSID1(rs(p)))(A, k, over, rng)
+            tag = f'tsid1_p{p}_{ci}'
+            out[tag + '_A'] = digest(A)
+            keep(tag + '_Z', Z)
+            keep(tag + '_X', X)
+            out[tag + '_I'] = np.asarray(I, dtype=np.int64)
+            out[tag + '_J'] = np.asarray(J, dtype=np.int64)
+    for p, cases in CUR_CASES.items():
+        for ci, (m, n, rank, k, over, seed) in enumerate(cases):
+            rng = np.random.default_rng(seed)
+            A = mm.rand_low_rank(m, n, rank, rng)
+            Js, U, Is = CUR1(OSID1(rs(p)))(A, k, over, rng)
+            tag = f'cur1_p{p}_{ci}'
+            out[tag + '_A'] = digest(A)
+            keep(tag + '_U', U)
+            out[tag + '_Js'] = np.asarray(Js, dtype=np.int64)
+            out[tag + '_Is'] = np.asarray(Is, dtype=np.int64)
+    for ci, (axis, p) in enumerate(((0, 2), (1, 2), (0, 0))):
+        rng = np.random.default_rng(40 + ci)
+        A = mm.rand_low_rank(120, 80, 40, rng)
+        out[f'rocs1_{ci}_A'] = digest(A)
+        out[f'rocs1_{ci}_idx'] = np.asarray(ROCS1(rs(p))(A, 20, 5, axis, rng), dtype=np.int64)
+    Y = np.random.default_rng(50).standard_normal((30, 90))
+    for axis in (0, 1):
+        M, P = qrcp_osid(Y if axis == 1 else Y.T, 20, axis)
+        out[f'qrcp_osid_{axis}_M'] = M
+        out[f'qrcp_osid_{axis}_P'] = np.asarray(P, dtype=np.int64)
+    return out
+
+
 def main(ref_path, only=None):
     """Write every fixture, or only those named in ``only``."""
     parla = _import_reference(ref_path)
@@ -293,7 +382,7 @@ def main(ref_path, only=None):
                 parla=parla.__version__)
     for name, fn in (('sketch', sketches), ('lsqr', lsqr_case),
                      ('spo', spo_cases), ('spu', spu_cases), ('sps', sps_cases),
-                     ('lowrank', lowrank_cases), ('lsfix', ls_fixtures)):
+                     ('lowrank', lowrank_cases), ('lsfix', ls_fixtures), ('interp', interp_cases)):
         if only and name not in only:
             continue
         data = fn(parla)

@@ -1,0 +1,174 @@
+"""Interpolative decompositions on the GPU against the oracle and the reference.
+
+- ``rla_geqp3`` (QR with column pivoting) against LAPACK geqp3 (SciPy):
+  identical pivots, R and Q^T b within 1e-12 relative, on full, partial
+  (kmax < min(m, n)), wide, tall, rank-deficient and one-column cases.
+- ``rla_trsm_upper`` against a dense solve.
+- OSID1, OSID2, TSID1, CUR1, ROCS1 and qrcp_osid with the reference's
+  Gaussian draws (``SkOpGA(seed_compat=True)``) on the reference test suite's
+  configurations: skeleton indices identical to the reference's
+  (``tests/golden/interp.npz``), coefficient matrices within 1e-8, and the
+  reference's own acceptance checks (permuted identity within 1e-8,
+  reconstruction error 1e-12 for the exact cases).
+"""
+import numpy as np
+import pytest
+import scipy.linalg as la
+
+from oracle import interpolative as oid
+from tests.golden.make_golden import CUR_CASES, OSID_CASES, TSID_CASES
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module")
+def pg():
+    import __graft_entry__
+    __graft_entry__.build()
+    import parla_gb300
+    return parla_gb300
+
+
+def _geqp3(pg, Y, kmax, rhs=None):
+    from parla_gb300.utils import linalg_wrappers as law
+    T, J = law.qrcp(torch.from_numpy(Y).cuda(), kmax=kmax, rhs=None if rhs is None else torch.from_numpy(rhs).cuda())
+    return T.cpu().numpy(), J.cpu().numpy()
+
+
+@pytest.mark.parametrize("shape,kmax,rank", [((60, 40), None, None), ((40, 90), None, None), ((200, 50), 20, None),
+                                             ((64, 64), None, 30), ((50, 1), None, None), ((1, 30), None, None),
+                                             ((300, 1000), 290, None)])
+def test_geqp3_matches_lapack(pg, shape, kmax, rank):
+    rng = np.random.default_rng(sum(shape))
+    m, n = shape
+    Y = rng.standard_normal((m, n)) * np.exp(rng.standard_normal(n))[None, :]
+    if rank is not None:
+        Y = rng.standard_normal((m, rank)) @ rng.standard_normal((rank, n))
+    b = rng.standard_normal((m, 3))
+    k = min(m, n) if kmax is None else kmax
+    T, J = _geqp3(pg, Y, k, rhs=b)
+    Q, R, P = la.qr(Y, mode="economic", pivoting=True)
+    kk = k if rank is None else min(k, rank)      # beyond the rank the pivots follow rounding noise
+    assert np.array_equal(J[:kk], P[:kk])
+    Rg = np.triu(T[:n, :k].T)                     # k x n, pivoted columns
+    scale = np.abs(R).max()
+    assert np.max(np.abs(Rg[:kk, :] - R[:kk, :])[:, :kk]) <= 1e-12 * scale * max(m, n)
+    qtb = T[n:, :k].T
+    ref = (Q.T @ b)[:k]
+    assert np.max(np.abs(qtb[:kk] - ref[:kk])) <= 1e-11 * np.abs(b).max() * max(m, n)
+
+
+def test_trsm_upper(pg):
+    from parla_gb300 import _kernels as K
+    rng = np.random.default_rng(3)
+    k, r = 120, 37
+    R = np.triu(rng.standard_normal((k, k))) + 4 * np.eye(k)
+    B = rng.standard_normal((k, r))
+    Rt = torch.from_numpy(np.ascontiguousarray(R.T)).cuda()     # column-major R
+    Bt = torch.from_numpy(np.ascontiguousarray(B.T)).cuda()
+    Xt = torch.empty_like(Bt)
+    K.trsm_upper_colmajor(k, Rt, Bt, Xt)
+    X = Xt.cpu().numpy().T
+    assert np.max(np.abs(X - la.solve_triangular(R, B))) <= 1e-12 * np.abs(X).max()
+
+
+def _rso(pg, p):
+    from parla_gb300.utils import linalg_wrappers as law
+    return pg.RS1(pg.SkOpGA(seed_compat=True), p, law.orth, passes_per_stab=1)
+
+
+def _close(M, ref, tol):
+    assert M.shape == ref.shape
+    assert np.max(np.abs(M - ref)) <= tol * max(1.0, np.abs(ref).max())
+
+
+def _match(g, tag, M, tol=1e-8):
+    if tag in g:
+        _close(np.asarray(M), g[tag], tol)
+    else:
+        fp = np.asarray(M) @ np.random.default_rng(99).standard_normal(M.shape[1])
+        _close(fp, g[tag + "_fp"], tol)
+
+
+@pytest.mark.parametrize("p", sorted(OSID_CASES))
+@pytest.mark.parametrize("name", ["OSID1", "OSID2"])
+def test_osid_matches_reference(pg, golden, p, name):
+    g = golden("interp")
+    for ci, (m, n, rank, k, over, axis, seed) in enumerate(OSID_CASES[p]):
+        rng = np.random.default_rng(seed)
+        A = oid.rand_low_rank(m, n, rank, rng)
+        M, P = getattr(pg, name)(_rso(pg, p))(A, k, over, axis, rng)
+        tag = f"{name.lower()}_p{p}_{ci}"
+        assert isinstance(M, np.ndarray) and P.dtype == np.int64
+        assert np.array_equal(P, g[tag + "_P"]), (tag, P, g[tag + "_P"])
+        _match(g, tag + "_M", M)
+        perm = M[P, :] if axis == 0 else M[:, P]                 # the reference's acceptance checks
+        assert la.norm(perm - np.eye(P.size)) < 1e-8
+        if p == 0:
+            A_id = M @ A[P, :] if axis == 0 else A[:, P] @ M
+            assert la.norm(A - A_id) / la.norm(A) < 1e-12
+
+
+@pytest.mark.parametrize("p", sorted(TSID_CASES))
+def test_tsid1_matches_reference(pg, golden, p):
+    g = golden("interp")
+    for ci, (m, n, rank, k, over, seed) in enumerate(TSID_CASES[p]):
+        rng = np.random.default_rng(seed)
+        A = oid.rand_low_rank(m, n, rank, rng)
+        Z, I, X, J = pg.TSID1(pg.OSID1(_rso(pg, p)))(A, k, over, rng)
+        tag = f"tsid1_p{p}_{ci}"
+        assert np.array_equal(I, g[tag + "_I"]) and np.array_equal(J, g[tag + "_J"]), tag
+        _match(g, tag + "_Z", Z)
+        _match(g, tag + "_X", X)
+        assert la.norm(Z[I, :] - np.eye(k)) < 1e-8 and la.norm(X[:, J] - np.eye(k)) < 1e-8
+        if p == 0:
+            assert la.norm(A - Z @ (A[I, :][:, J] @ X)) / la.norm(A) < 1e-12
+
+
+@pytest.mark.parametrize("p", sorted(CUR_CASES))
+def test_cur1_matches_reference(pg, golden, p):
+    g = golden("interp")
+    for ci, (m, n, rank, k, over, seed) in enumerate(CUR_CASES[p]):
+        rng = np.random.default_rng(seed)
+        A = oid.rand_low_rank(m, n, rank, rng)
+        Js, U, Is = pg.CUR1(pg.OSID1(_rso(pg, p)))(A, k, over, rng)
+        tag = f"cur1_p{p}_{ci}"
+        err = la.norm(A - A[:, Js] @ (U @ A[Is, :])) / la.norm(A)
+        if rank >= k:
+            assert np.array_equal(Js, g[tag + "_Js"]) and np.array_equal(Is, g[tag + "_Is"]), tag
+            _match(g, tag + "_U", U, 1e-7)
+        else:   # k above the rank: the last pivots follow rounding noise in any implementation
+            assert np.array_equal(np.sort(Js[:rank]), np.sort(g[tag + "_Js"][:rank]))
+        if p == 0:
+            assert err < 1e-12, (tag, err)
+
+
+def test_rocs1_and_qrcp_osid_match_reference(pg, golden):
+    g = golden("interp")
+    for ci, (axis, p) in enumerate(((0, 2), (1, 2), (0, 0))):
+        rng = np.random.default_rng(40 + ci)
+        A = oid.rand_low_rank(120, 80, 40, rng)
+        assert np.array_equal(pg.ROCS1(_rso(pg, p))(A, 20, 5, axis, rng), g[f"rocs1_{ci}_idx"])
+    Y = np.random.default_rng(50).standard_normal((30, 90))
+    for axis in (0, 1):
+        M, P = pg.qrcp_osid(Y if axis == 1 else Y.T, 20, axis)
+        assert np.array_equal(P, g[f"qrcp_osid_{axis}_P"])
+        _close(M, g[f"qrcp_osid_{axis}_M"], 1e-10)
+
+
+def test_id_drivers_on_device_tensors(pg):
+    """CUDA tensors in, CUDA tensors out; the module-level wrappers run."""
+    rng = np.random.default_rng(8)
+    A = torch.from_numpy(oid.rand_low_rank(200, 90, 20, rng)).cuda()
+    X, Js = pg.osid1(A, 20, 5, 2, 1, 1)
+    assert isinstance(X, torch.Tensor) and X.is_cuda
+    assert torch.linalg.matrix_norm(A - A[:, Js] @ X) / torch.linalg.matrix_norm(A) < 1e-12
+    Z, Is, X2, Js2 = pg.tsid1(A, 20, 5, 2, 3)
+    assert torch.linalg.matrix_norm(A - Z @ (A[Is][:, Js2] @ X2)) / torch.linalg.matrix_norm(A) < 1e-12
+    Js3, U, Is3 = pg.cur1(A, 20, 5, 3, 4)
+    assert torch.linalg.matrix_norm(A - A[:, Js3] @ (U @ A[Is3])) / torch.linalg.matrix_norm(A) < 1e-12
+    Z2, Is4 = pg.osid2(A, 20, 5, 1, 0, 5)
+    assert torch.linalg.matrix_norm(A - Z2 @ A[Is4]) / torch.linalg.matrix_norm(A) < 1e-12
+    idx = pg.rocs1(A, 20, 5, 2, 0, 6)
+    assert idx.numel() == 20 and torch.unique(idx).numel() == 20
