@@ -69,7 +69,7 @@ class ClockSampler:
             os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=self.fh, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
@@ -100,6 +100,24 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
+def plain_torch_svd1(torch, A, k, over, num_pass, seed):
+    """The same SVD1(QB1(RF1(RS1(Gaussian, num_pass)))) chain written directly in
+    PyTorch in binary32: cuBLAS SGEMM (TF32 off) for the passes, cuSOLVER QR
+    as the stabilizer after every pass and for the range finder, cuSOLVER SVD
+    of B.  A comparator of what a plain FP32 GPU port gets from the vendor
+    libraries."""
+    l = k + over
+    m, n = A.shape
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    S = torch.randn((n, l), generator=g, device="cuda") / l ** 0.5
+    for p in range(num_pass):
+        S = torch.linalg.qr(A @ S if p % 2 == 0 else A.t() @ S).Q
+    Q = torch.linalg.qr(A @ S).Q
+    B = Q.t() @ A
+    Ub, s, Vh = torch.linalg.svd(B, full_matrices=False)
+    return Q @ Ub[:, :k], s[:k], Vh[:k]
+
+
 def chain(pg, precision="bf16"):
     return pg.SVD1(pg.QB1(pg.RF1(pg.RS1(pg.SkOpGA(), NUM_PASS))), precision=precision)
 
@@ -126,6 +144,11 @@ def run_ours(args):
     svd = chain(pg)
     stream = torch.cuda.current_stream()
 
+    # nvidia-smi samples (50 ms apart) from the warm-up through the timed
+    # region: the timed steps alone are shorter than the sampler's start-up
+    clk = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clk.__enter__()
+    time.sleep(0.5)
     for w in range(args.warmup):
         svd(A, K_RANK, np.nan, OVER, 1000 + w)
     torch.cuda.synchronize()
@@ -134,7 +157,7 @@ def run_ours(args):
     K.STATS.reset()
     K.STATS.timing = True
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+    with clk:
         if dist is not None:
             dist.barrier()
         torch.cuda.synchronize()
@@ -169,15 +192,16 @@ def run_ours(args):
     # end to end: pinned host A in, factors out, through the public API
     A_host = A.cpu().pin_memory()
     h2d = A_host.numel() * 4
+    svd(A_host, K_RANK, np.nan, OVER, 2999)          # (host path warm-up)
     torch.cuda.synchronize()
     t0 = torch.cuda.Event(enable_timing=True)
     t1 = torch.cuda.Event(enable_timing=True)
     d2h = 0
     t0.record(stream)
     for it in range(args.steps):
-        Ad_ = A_host.to("cuda", non_blocking=True)
-        U, sv, Vh = svd(Ad_, K_RANK, np.nan, OVER, 3000 + it)
-        Uh, sh, Vhh = U.cpu(), sv.cpu(), Vh.cpu()
+        # pinned host A in (read over the host link by the bf16 conversion
+        # kernel), host factors out: the public API on host buffers
+        Uh, sh, Vhh = svd(A_host, K_RANK, np.nan, OVER, 3000 + it)
         d2h = (Uh.numel() + sh.numel() + Vhh.numel()) * 4
     t1.record(stream)
     torch.cuda.synchronize()
@@ -215,6 +239,28 @@ def run_ours(args):
     torch.cuda.synchronize()
     plain_ms = p0.elapsed_time(p1) / nplain
     err_plain = float(torch.linalg.matrix_norm(A.double() - (Up.double() * sp.double()) @ Vhp.double()))
+    # the same chain on the vendor libraries in binary32 (TF32 off)
+    tf32 = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    plain_torch_svd1(torch, A, K_RANK, OVER, NUM_PASS, 1)
+    torch.cuda.synchronize()
+    p0.record(stream)
+    for it in range(nplain):
+        Ut, st_, Vht = plain_torch_svd1(torch, A, K_RANK, OVER, NUM_PASS, 4100 + it)
+    p1.record(stream)
+    torch.cuda.synchronize()
+    torch_ms = p0.elapsed_time(p1) / nplain
+    g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    Sx = torch.randn((N_COLS, K_RANK + OVER), device="cuda")
+    g0.record(stream)
+    for _ in range(5):
+        A @ Sx
+    g1.record(stream)
+    torch.cuda.synchronize()
+    sgemm_tflops = 2.0 * M_ROWS * N_COLS * (K_RANK + OVER) * 5 / (g0.elapsed_time(g1) * 1e-3) / 1e12
+    torch.backends.cuda.matmul.allow_tf32 = tf32
+    err_torch = float(torch.linalg.matrix_norm(A.double() - (Ut.double() * st_.double()) @ Vht.double()))
+    del Ut, st_, Vht, Sx
 
     line = {
         "metric": METRIC,
@@ -236,7 +282,14 @@ def run_ours(args):
                    "path": "tcgen05 bf16 passes (fp32 accumulate), tensor-core CholeskyQR stabilizer"},
         "error": {"frob_err": err, "optimal_tail": tail, "ratio": err / tail,
                   "plain_fp32_ratio": err_plain / tail},
-        "plain_fp32_gpu": {"ms_per_step": plain_ms, "speedup": plain_ms / (total_ms / args.steps)},
+        "plain_fp32_gpu": {"ms_per_step": plain_ms, "speedup": plain_ms / (total_ms / args.steps),
+                           "what": "the library's own binary32 chain (SIMT products)",
+                           "pass_gflop": 2.0 * M_ROWS * N_COLS * (K_RANK + OVER) * 6 / 1e9,
+                           "chain_tflops": 2.0 * M_ROWS * N_COLS * (K_RANK + OVER) * 6 / (plain_ms * 1e-3) / 1e12},
+        "plain_fp32_torch": {"ms_per_step": torch_ms, "speedup": torch_ms / (total_ms / args.steps),
+                             "what": "the same chain in PyTorch binary32: cuBLAS SGEMM (TF32 off), cuSOLVER QR "
+                                     "after every pass, cuSOLVER SVD of B",
+                             "sgemm_pass_tflops": sgemm_tflops, "frob_err_ratio": err_torch / tail},
         "e2e": {"value": world * args.steps / (e2e_ms * 1e-3), "unit": "rsvd/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "roofline": {"kernel": "gemm_tc_kernel (RSVD pass)", "bound": "hbm", "achieved": achieved, "peak": hbm,
@@ -249,19 +302,21 @@ def run_ours(args):
     }
     if args.cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(A.cpu().numpy(), budget_s=args.cpu_budget)
-    del A, Ad_, A_host
+    del A, A_host
     torch.cuda.empty_cache()
     if world > 1:  # the side measurements are single-GPU workloads
         print(json.dumps(line))
         return
     line["sketch_apply"] = bench_sketch_apply(torch)
     if args.nystrom:
-        line["nystrom_evd2"] = bench_nystrom(torch, pg)
+        line["nystrom_evd2"] = bench_nystrom(torch, pg, args.cpu_budget if args.cpu_baseline else 0.0)
     if args.learned:
-        line["learned_sketch"] = bench_learned(torch, args.learned_eval)
+        line["learned_sketch"] = bench_learned(torch, args.learned_eval,
+                                               args.cpu_budget if args.cpu_baseline else 0.0)
     if args.ls:
-        line["ls_single"] = bench_ls_single(torch, pg)
-        line["ls_batched"] = bench_ls_batched(torch, pg, args.ls_problems)
+        cb = args.cpu_budget if args.cpu_baseline else 0.0
+        line["ls_single"] = bench_ls_single(torch, pg, cb)
+        line["ls_batched"] = bench_ls_batched(torch, pg, args.ls_problems, cb)
     print(json.dumps(line))
 
 
@@ -320,7 +375,7 @@ def _rbf_problem(N, dim=16, seed=2024):
     return X, 1.0 / (2.0 * h * h), h
 
 
-def bench_nystrom(torch, pg):
+def bench_nystrom(torch, pg, cpu_budget=0.0):
     """Nystrom EVD2 on the 32768 x 32768 Gaussian kernel matrix,
     k = 512, over = 16: K S on the bf16 tensor cores (split hi + lo pair,
     fp32 accumulation), shift / S^T Y / Cholesky / SVD of B in double-float.
@@ -367,8 +422,12 @@ def bench_nystrom(torch, pg):
     with warnings.catch_warnings():
         warnings.simplefilter("ignore")
         _, lam2 = evd(DeviceMatrix.from_bf16(hi, lo), k, np.nan, over, 2)
+        t8192 = _event_ms(torch, lambda: evd(DeviceMatrix.from_bf16(hi, lo), k, np.nan, over, 3), reps=3)
         K64 = torch.exp(-gamma * torch.cdist(X2.double(), X2.double()) ** 2)
         _, lam64 = evd(K64, k, np.nan, over, 2)          # binary64 path, same sketch
+        if cpu_budget > 0:
+            out["cpu_baseline_n8192"] = cpu_nystrom(K64.cpu().numpy(), k, over, cpu_budget)
+            out["cpu_baseline_n8192"]["gpu_bf16_split_ms_n8192"] = t8192
         del K64
     lam2 = lam2.double().cpu().numpy()
     lam64 = lam64.cpu().numpy()
@@ -388,7 +447,7 @@ def bench_nystrom(torch, pg):
     return out
 
 
-def bench_learned(torch, n_eval):
+def bench_learned(torch, n_eval, cpu_budget=0.0):
     """Learned sparse sketch on the 4096 x 4096 family (k = 64, d = 74) with the
     shipped network: held-out range-finder errors against the plain Gaussian
     and plain SJLT sketches of the same size, the guard's fallback rate, and
@@ -412,6 +471,8 @@ def bench_learned(torch, n_eval):
     plain = QB1(RF1(RS1(SkOpGA(), 0), precision="f32"), precision="f32")
     out["qb_ms"] = {"learned_guarded": _event_ms(torch, lambda: guard(A, 74, np.nan, 1), reps=5),
                     "plain_gaussian": _event_ms(torch, lambda: plain(A, 74, np.nan, 1), reps=5)}
+    if cpu_budget > 0:
+        out["cpu_baseline_qb1"] = cpu_qb1(A.double().cpu().numpy(), 74, cpu_budget)
     return out
 
 
@@ -434,7 +495,7 @@ def _ls_single_problem(torch, m=20000, n=200, seed=11):
     return A, b.contiguous()
 
 
-def bench_ls_single(torch, pg):
+def bench_ls_single(torch, pg, cpu_budget=0.0):
     """Sketch-and-precondition LS as the reference runs it (20000 x 200, kappa 1e8):
     A 20000 x 200, kappa 1e8, Gaussian sketch d = 4n, QR preconditioner,
     tolerance 1e-12; plain FP64 GPU path vs the double-float path.
@@ -459,10 +520,12 @@ def bench_ls_single(torch, pg):
                      "pred_err": float(la.norm(An @ (xh - xr)) / la.norm(An @ xr)),
                      "x_err": float(la.norm(xh - xr) / la.norm(xr))}
     out["speedup_df_vs_f64"] = out["df"]["solves_per_s"] / out["f64"]["solves_per_s"]
+    if cpu_budget > 0:
+        out["cpu_baseline"] = cpu_ls_single(An, bn, cpu_budget)
     return out
 
 
-def bench_ls_batched(torch, pg, count):
+def bench_ls_batched(torch, pg, count, cpu_budget=0.0):
     """Batched LS: `count` problems, m log-uniform [2048, 65536],
     n uniform [16, 512], m >= 16 n, kappa log-uniform [1e4, 1e10], noise 1e-8;
     SJLT d = 4n, 8 nonzeros; stop at prediction error ~3e-11.  The batched
@@ -512,6 +575,8 @@ def bench_ls_batched(torch, pg, count):
         "sample": "stratified: the 12 largest m*n, the 12 largest kappa, 24 spread over the rest "
                   f"(largest m*n checked {max(shapes[i][0] * shapes[i][1] for i in idx)}, "
                   f"largest kappa {max(shapes[i][2] for i in idx):.2e}); LAPACK gelsy in binary64 on the host"}
+    if cpu_budget > 0:
+        out["cpu_baseline"] = cpu_ls_batched(probs, shapes, cpu_budget)
     return out
 
 
@@ -557,6 +622,90 @@ def cpu_baseline(A, budget_s=30.0, steps=None):
     return {"value": 1.0 / per, "unit": "rsvd/s", "cores": len(os.sched_getaffinity(0)), "kind": "port",
             "sample": f"{len(times)} full SVD1 runs on the same 16384x8192 matrix (median {per:.2f} s)",
             "blas_threads": os.environ.get("OPENBLAS_NUM_THREADS", "default")}
+
+
+def _cpu_timed(fn, budget_s, max_runs=5):
+    """Median wall time of fn() over up to max_runs runs, stopping after budget_s."""
+    times = []
+    t_start = time.perf_counter()
+    import warnings
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        for i in range(max_runs):
+            t0 = time.perf_counter()
+            fn(i)
+            times.append(time.perf_counter() - t0)
+            if time.perf_counter() - t_start > budget_s:
+                break
+    return float(np.median(times)), len(times)
+
+
+def _cores():
+    return len(os.sched_getaffinity(0))
+
+
+def cpu_ls_single(An, bn, budget_s):
+    """The oracle's SPO(SkOpGA(), 4, 'qr') at tol 1e-12 (Gaussian generation included)."""
+    import oracle
+    m, n = An.shape
+    d = oracle.dim_checks(4, m, n)
+
+    def run(i):
+        S = oracle.gaussian_operator(d, m, np.random.default_rng(100 + i))
+        oracle.spo(An, bn, 0.0, 1e-12, 200, S, "qr", logging=False)
+    per, runs = _cpu_timed(run, budget_s)
+    return {"value": 1.0 / per, "unit": "solves/s", "cores": _cores(), "kind": "port",
+            "sample": f"{runs} full solves of the same 20000x200 problem (median {per:.3f} s)"}
+
+
+def cpu_ls_batched(probs, shapes, budget_s):
+    """The oracle's SPO(SkOpSJ(8), 4, 'qr') at tol 1e-12 on a stratified subset,
+    extrapolated to the whole batch by the problems' element counts."""
+    import oracle
+    idx = _stratified_sample(shapes, 16)
+    idx = sorted(idx, key=lambda i: shapes[i][0] * shapes[i][1])
+    spent, elems, done = 0.0, 0, 0
+    import warnings
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        for i in idx:
+            An, bn = probs[i][0].cpu().numpy(), probs[i][1].cpu().numpy()
+            m, n = An.shape
+            t0 = time.perf_counter()
+            S = oracle.sjlt_operator(oracle.dim_checks(4, m, n), m, np.random.default_rng(200 + i), 8)
+            oracle.spo(An, bn, 0.0, 1e-12, 100, S, "qr", logging=False)
+            spent += time.perf_counter() - t0
+            elems += m * n
+            done += 1
+            if spent > budget_s:
+                break
+    total_elems = sum(m * n for m, n, _ in shapes)
+    est = spent * total_elems / elems
+    return {"value": len(shapes) / est, "unit": "solves/s", "cores": _cores(), "kind": "port",
+            "sample": f"{done} of the {len(shapes)} problems (stratified by size and kappa) in {spent:.1f} s, "
+                      f"extrapolated by element count to {est:.0f} s for the batch"}
+
+
+def cpu_nystrom(K64, k, over, budget_s):
+    """The oracle's EVD2(RS1(SkOpGA, 0)) on the kernel matrix (binary64)."""
+    from oracle import lowrank as olr
+    from oracle import sketching as osk
+    rso = lambda A_, kk, rng: olr.rs1(A_, kk, rng, osk.gaussian_operator, 0)
+    per, runs = _cpu_timed(lambda i: olr.evd2(K64, k, np.nan, over, 300 + i, rso), budget_s, max_runs=3)
+    return {"value": 1e3 * per, "unit": "ms", "cores": _cores(), "kind": "port",
+            "sample": f"{runs} runs at N={K64.shape[0]} (median {per:.2f} s; thin SVD of the sketch, "
+                      "where the reference takes the full one)"}
+
+
+def cpu_qb1(A64, k, budget_s):
+    """The oracle's QB1(RF1(RS1(SkOpGA, 0))) on one matrix of the family (binary64)."""
+    from oracle import lowrank as olr
+    from oracle import sketching as osk
+    rso = lambda A_, kk, rng: olr.rs1(A_, kk, rng, osk.gaussian_operator, 0)
+    rf = lambda A_, kk, tol, rng: olr.rf1(A_, kk, tol, rng, rso)
+    per, runs = _cpu_timed(lambda i: olr.qb1(A64, k, np.nan, 400 + i, rf), budget_s)
+    return {"value": 1e3 * per, "unit": "ms", "cores": _cores(), "kind": "port",
+            "sample": f"{runs} QB1 runs on one 4096x4096 family matrix (median {per * 1e3:.1f} ms)"}
 
 
 def run_reference(args):

@@ -76,9 +76,10 @@ def to_dev(x, dtype=torch.float64):
 
 
 def like_input(t, ref):
-    """Return a numpy array when the user passed numpy, else the tensor."""
+    """Return the result where the input lives: a NumPy array for NumPy input,
+    a host tensor for a host tensor, else the device tensor."""
     if isinstance(ref, torch.Tensor):
-        return t
+        return t if ref.is_cuda else t.detach().cpu()
     return t.detach().cpu().numpy()
 
 
@@ -515,10 +516,21 @@ def convert(x, dtype, transpose=False):
 
 
 def convert_bf16_pair(x, want_y=True, want_t=True):
-    """(bf16(x), bf16(x)^T) from one pass over x (float32/float64)."""
+    """(bf16(x), bf16(x)^T) from one pass over x (float32/float64).
+
+    x may be a CUDA tensor or a pinned (page-locked) host tensor: pinned host
+    memory is mapped into the device's address space, so the kernel reads it
+    directly over the host link and the outputs land in device memory (the
+    host-to-device transfer and the conversion are one pass).
+    """
+    if not x.is_cuda and not x.is_pinned():
+        raise ValueError("convert_bf16_pair: x must be a CUDA tensor or pinned host memory")
+    if not x.is_contiguous():
+        raise ValueError("convert_bf16_pair: x must be contiguous")
     rows, cols = x.shape
-    y = empty_bf16(rows, cols, x.device) if want_y else None
-    yt = empty_bf16(cols, rows, x.device) if want_t else None
+    dev = x.device if x.is_cuda else device()
+    y = empty_bf16(rows, cols, dev) if want_y else None
+    yt = empty_bf16(cols, rows, dev) if want_t else None
     _timed("convert_bf16_pair", 1, call, "rla_convert_bf16_pair", _TORCH_CODE[x.dtype], rows, cols, ptr(x),
            x.stride(0), ptr(y), y.stride(0) if y is not None else 0, ptr(yt),
            yt.stride(0) if yt is not None else 0, stream())

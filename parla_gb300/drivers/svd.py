@@ -51,6 +51,6 @@ class SVD1(SVDecomposer):
         U = Ut.t()
         out_dtype = Qt.dtype
         res = (U, s.to(out_dtype), Vh.to(out_dtype).contiguous())
-        if isinstance(A, (torch.Tensor, opd.DeviceMatrix)):
+        if isinstance(A, opd.DeviceMatrix) or (isinstance(A, torch.Tensor) and A.is_cuda):
             return res
         return tuple(K.like_input(r, A) for r in res)

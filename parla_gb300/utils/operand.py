@@ -113,11 +113,21 @@ class DeviceMatrix:
 
 
 def wrap(A, precision=None):
-    """DeviceMatrix for A (NumPy, tensor or DeviceMatrix)."""
+    """DeviceMatrix for A (NumPy, tensor or DeviceMatrix).
+
+    A pinned binary32 host tensor on the tensor-core path ('bf16') is not
+    copied to the device: the bf16 images are made by one kernel that reads
+    the host memory directly (pinned memory is mapped into the device's
+    address space), so the transfer and the conversion are a single pass and
+    the binary32 A never occupies device memory.
+    """
     if isinstance(A, DeviceMatrix):
         return A
     if isinstance(A, torch.Tensor) and A.is_cuda:
         return DeviceMatrix(A.contiguous(), precision)
+    if (precision == "bf16" and isinstance(A, torch.Tensor) and A.dtype == torch.float32 and A.is_pinned()
+            and A.is_contiguous() and A.dim() == 2):
+        return DeviceMatrix(A, precision)
     want = torch.float32 if precision in ("f32", "bf16") else None
     import numpy as np
     arr = np.asarray(A)

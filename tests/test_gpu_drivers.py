@@ -287,6 +287,14 @@ def test_svd1_bf16_tensor_core_path_within_one_percent(pg):
         errs[prec] = float(torch.linalg.matrix_norm(Ad.double() - (Ug.double() * sg.double()) @ Vhg.double()))
     assert errs["f32"] <= 1.01 * tail
     assert errs["bf16"] <= 1.01 * errs["f32"]
+    # pinned host input: the bf16 images are made straight from host memory,
+    # the factors come back on the host, bit-identical to the device input
+    chain = pg.SVD1(pg.QB1(pg.RF1(pg.RS1(pg.SkOpGA(), 4))), precision="bf16")
+    Ah = torch.from_numpy(A).pin_memory()
+    Uh, sh, Vhh = chain(Ah, k, np.nan, 10, 2)
+    Ud, sd, Vhd = chain(Ad, k, np.nan, 10, 2)
+    assert not Uh.is_cuda and not sh.is_cuda and not Vhh.is_cuda
+    assert torch.equal(Uh, Ud.cpu()) and torch.equal(sh, sd.cpu()) and torch.equal(Vhh, Vhd.cpu())
 
 
 def test_qb1_bf16_orthonormal_basis(pg):
