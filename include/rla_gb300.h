@@ -367,6 +367,45 @@ int rla_lsqr_batched(int dtype, const void* probs, const int* order,
                      int nprob, int64_t nmax, int cluster, int max_ctas,
                      int* next, rla_stream_t stream);
 
+/* One least-squares problem of a batch: min ||A x - b||, A m x n (m >= n)
+ * row-major binary64 with leading dimension lda, b of m entries, x of n
+ * entries receives the solution; all device pointers.  seed keys the
+ * problem's SJLT sketch. */
+typedef struct rla_ls_problem {
+  int64_t m, n, lda;
+  const double* A;
+  const double* b;
+  double* x;
+  uint64_t seed;
+} rla_ls_problem;
+
+/* The whole batched sketch-and-precondition solve in one call: for every
+ * problem of the HOST array probs[nprob], the SJLT sketch (d = min(sf n, m)
+ * rows, min(vec_nnz, d) nonzeros per column, exact fixed-point product),
+ * double-float Householder QR of [S A | S b], R^-1, the presolve start
+ * z0 = (Q^T S b)[:n], and LSQR on A R^-1 in double-float stopped by the
+ * prediction-error rule of rla_lsqr_launch (ptol) or iter_lim.  status
+ * (device int[3 nprob]) receives per problem the LSQR iterations, its stop
+ * code and the grid-barrier status.  Problems run largest first, in
+ * persistent launches (QR: one CTA per problem; LSQR: one thread-block
+ * cluster of 1-8 CTAs per problem by size) and, for a problem much larger
+ * than its share of the device, a full-device cooperative LSQR.  Phase A
+ * (split, sketch, assembly) is spread over the nside caller-owned side
+ * streams (NULL/0: everything on `stream`), forked from and joined back to
+ * `stream` with events.  No allocation and no synchronisation: the call can
+ * be captured in a CUDA graph.  Two workspaces, queried with ws == NULL and
+ * host_ws == NULL: device `ws` (sketches, hi/lo planes, factors, LSQR
+ * vectors, records) and pinned HOST `host_ws`, from which the problem
+ * records are copied to the device inside the call (a captured graph copies
+ * them again from it on every replay, so it must outlive the graph
+ * unchanged).  Replaces a loop of SPO calls,
+ * parla/drivers/least_squares.py:284-369 (SPO.__call__: sketch :303-315,
+ * QR :307-316, presolve :342-351, PcSS2/LSQR :353-362). */
+int rla_spo_batched(int nprob, const rla_ls_problem* probs, int sampling_factor,
+                    int vec_nnz, double ptol, int iter_lim, int* status,
+                    int nside, rla_stream_t* side, void* ws, size_t* ws_bytes,
+                    void* host_ws, size_t* host_ws_bytes, rla_stream_t stream);
+
 /* r = b - A x (m rows) in double-float from the hi/lo planes of A
  * (rla_split_f64): the FP64-class residual of the refinement loop, replacing
  * `A @ x_ske - b` at parla/drivers/least_squares.py:344. */

@@ -19,6 +19,12 @@ STATUS = {
 }
 
 
+class RlaLsProblem(C.Structure):
+    """``rla_ls_problem`` of include/rla_gb300.h (one problem of rla_spo_batched)."""
+    _fields_ = [("m", C.c_int64), ("n", C.c_int64), ("lda", C.c_int64), ("A", C.c_void_p), ("b", C.c_void_p),
+                ("x", C.c_void_p), ("seed", C.c_uint64)]
+
+
 class RlaLibraryMissing(RuntimeError):
     pass
 
@@ -57,6 +63,7 @@ SIGNATURES = {
     "rla_lsqr_launch": [_i32, _i64, _i64, _i64, _p, _p, _p, _i64, _p, _i64, _f64, _p, _p, _i32, _f64, _f64,
                         _f64, _f64, _i32, _i32, _p, _p, _p, _p, _psz, _p],
     "rla_residual_df": [_i64, _i64, _p, _p, _i64, _p, _p, _p, _p],
+    "rla_spo_batched": [_i32, _p, _i32, _i32, _f64, _i32, _p, _i32, _p, _p, _psz, _p, _psz, _p],
     "rla_geqrf_batched": [_i32, _p, _p, _i32, _p, _p],
     "rla_geqrf_hl_batched": [_p, _p, _i32, _i64, _p, _p],
     "rla_trtri_hl_batched": [_p, _i32, _i64, _i64, _p],

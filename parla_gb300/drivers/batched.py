@@ -42,9 +42,14 @@ class BatchedSPO:
 
     def __init__(self, sampling_factor=4, vec_nnz=8, ptol=3e-11, iter_lim=100, precision="mixed", streams=8,
                  tuner=None, max_refine=3, refine_kappa=1e5, strategy="df", big_qr_n=384,
-                 big_lsqr_numel=1 << 23):
+                 big_lsqr_numel=1 << 23, engine="python"):
         if precision not in ("mixed", "f64"):
             raise ValueError(f"unknown precision {precision!r}")
+        if engine not in ("python", "capi"):
+            raise ValueError(f"unknown engine {engine!r}")
+        # 'capi': the whole batch through the single C entry point
+        # rla_spo_batched (the same kernels and plan, orchestrated in C++)
+        self.engine = engine
         self.sf = sampling_factor
         self.nnz = vec_nnz
         self.ptol = ptol
@@ -91,6 +96,13 @@ class BatchedSPO:
             return self._plain(problems, seeds)
         if self.strategy == "refine":
             return self._batched(problems, seeds)
+        if self.engine == "capi":
+            plan = self._capi_plan(problems, seeds)
+            self._capi_launch(plan)
+            torch.cuda.synchronize()
+            self.last_info = self.info_from_plan(plan)
+            self.last_layout = None
+            return plan["xs"]
         plan = self._finish_plan(self._prepare(problems, seeds))
         self._launch(plan)
         torch.cuda.synchronize()
@@ -312,9 +324,48 @@ class BatchedSPO:
         plan["next2"] = torch.zeros(1, dtype=torch.int32, device=dev)
         return plan
 
+    # ---------------------------------------------- the C entry point
+    def _capi_plan(self, problems, seeds):
+        """Records, outputs and both workspaces of one rla_spo_batched call."""
+        import ctypes as C
+        from .. import _lib
+        dev = K.device()
+        nprob = len(problems)
+        recs = (_lib.RlaLsProblem * max(nprob, 1))()
+        xs = []
+        for i, ((A, b), seed) in enumerate(zip(problems, seeds)):
+            m, n = A.shape
+            if A.stride(1) != 1 or not b.is_contiguous():
+                raise ValueError("rla_spo_batched needs row-major A and contiguous b")
+            x = torch.empty(n, dtype=torch.float64, device=dev)
+            recs[i] = _lib.RlaLsProblem(m, n, A.stride(0), A.data_ptr(), b.data_ptr(), x.data_ptr(), seed)
+            xs.append(x)
+        side = [torch.cuda.Stream() for _ in range(self.nstreams)]
+        side_arr = (C.c_void_p * max(len(side), 1))(*[s.cuda_stream for s in side])
+        dq, hq = C.c_size_t(0), C.c_size_t(0)
+        _lib.call("rla_spo_batched", nprob, recs, self.sf, self.nnz, float(self.ptol), int(self.iter_lim), None,
+                  len(side), side_arr, None, C.byref(dq), None, C.byref(hq), K.stream())
+        return dict(recs=recs, xs=xs, nprob=nprob, side=side, side_arr=side_arr,
+                    outs=torch.zeros((nprob, 3), dtype=torch.int32, device=dev),
+                    ws=torch.empty(max(dq.value, 1), dtype=torch.uint8, device=dev),
+                    hws=torch.empty(max(hq.value, 1), dtype=torch.uint8).pin_memory())
+
+    def _capi_launch(self, plan):
+        import ctypes as C
+        from .. import _lib
+        for s in plan["side"]:
+            s.wait_stream(torch.cuda.current_stream())
+        _lib.call("rla_spo_batched", plan["nprob"], plan["recs"], self.sf, self.nnz, float(self.ptol),
+                  int(self.iter_lim), K.ptr(plan["outs"]), len(plan["side"]), plan["side_arr"], K.ptr(plan["ws"]),
+                  C.byref(C.c_size_t(plan["ws"].numel())), C.c_void_p(plan["hws"].data_ptr()),
+                  C.byref(C.c_size_t(plan["hws"].numel())), K.stream())
+        K.STATS.launches += 6 * plan["nprob"] + 4
+
     def plan(self, problems, rng=0):
         rng = np.random.default_rng(rng)
         seeds = [int(s) for s in rng.integers(0, 2 ** 62, size=len(problems))]
+        if self.engine == "capi":
+            return self._capi_plan(problems, seeds)
         return self._finish_plan(self._prepare(problems, seeds))
 
     def capture(self, problems, rng=0):
@@ -324,15 +375,16 @@ class BatchedSPO:
         from the inputs (the sketch seeds are part of the graph).
         """
         plan = self.plan(problems, rng)
-        self._launch(plan)              # warm-up run outside capture
+        launch = self._capi_launch if self.engine == "capi" else self._launch
+        launch(plan)                    # warm-up run outside capture
         torch.cuda.synchronize()
         g = torch.cuda.CUDAGraph()
         cap = torch.cuda.Stream()
         cap.wait_stream(torch.cuda.current_stream())
         with torch.cuda.graph(g, stream=cap):
-            self._launch(plan)
+            launch(plan)
         torch.cuda.synchronize()
-        xs = [it["x"] for it in plan["items"]]
+        xs = plan["xs"] if self.engine == "capi" else [it["x"] for it in plan["items"]]
 
         def replay():
             g.replay()
