@@ -336,6 +336,23 @@ def chol_inv_f32(G, want_r=False, info=None):
     return (Rinv, R) if want_r else Rinv
 
 
+def chol_f32(G, info=None):
+    """Upper Cholesky factor R of an FP32 SPD G (n <= 216), one CTA, without
+    the inverse (``rla_chol_inv_f32`` with Rinv = NULL).  Returns None when n
+    is too large.  ``info`` as in chol_inv_f32."""
+    n = G.shape[0]
+    if n > 216:
+        return None
+    R = torch.empty((n, n), dtype=torch.float32, device=G.device)
+    inf = info if info is not None else torch.zeros(1, dtype=torch.int32, device=G.device)
+    _timed("chol_f32", 1, call, "rla_chol_inv_f32", n, ptr(G), G.stride(0), None, n, ptr(R), n, ptr(inf), stream())
+    if info is None:
+        bad = int(inf.item())
+        if bad:
+            raise _lib.RlaError("rla_chol_inv_f32", 3, f"pivot {bad - 1} not positive")
+    return R
+
+
 def potrf_df_small(G, info=None, want64=False):
     """Upper Cholesky factor of a binary64 SPD matrix (n <= 232) in double-float.
 

@@ -88,14 +88,69 @@ def _svd_from_gram(G):
     return U, s
 
 
+# Smallest accepted pivot of the diagonally scaled Gram on the binary32 route:
+# min_i R_ii^2 / G_ii bounds the scaled condition number from below, and the
+# singular values come out to about eps_32 * kappa(D^-1/2 G D^-1/2) relative.
+SCALED_PIVOT_MIN = 1e-2
+
+
+def _svd_gram_f32(B, trans):
+    """U, s of a square-root factor of the binary32 Gram of B (k <= 216).
+
+    G = B B^T (or B^T B) accumulated in binary32, G = R^T R by the one-CTA
+    binary32 Cholesky, then one-sided Jacobi on R^T.  Cholesky's relative
+    accuracy depends on the condition number of the diagonally scaled Gram
+    D^-1/2 G D^-1/2, not on that of G: the rows of B that a range finder
+    returns are close to scaled singular vectors, so the scaled Gram is well
+    conditioned (about 4 for the 16384 x 8192, i^-1.5 spectrum with l = 210,
+    against 7e6 for G) and binary32 is enough.  The route is taken only when
+    every pivot of the scaled Gram is at least SCALED_PIVOT_MIN; otherwise
+    (and when the Cholesky or Jacobi fail) it returns None, or inside a
+    deferred-check scope raises the flag that sends the driver call down the
+    guarded double-float path.
+    """
+    from .operand import current_checks
+    G = K.syrk(B, trans=trans, mode="f32")   # (trans: B^T B for a tall B)
+    chk = current_checks()
+    if chk is not None:
+        flag = chk.new_flag()
+        R = K.chol_f32(G, info=flag)
+        # (the check reads R only where the Cholesky succeeded; a failed one raised flag)
+        ratio = torch.diagonal(R) ** 2 / torch.diagonal(G).clamp_min(1e-300)
+        chk.add_flag((ratio.min() < SCALED_PIVOT_MIN).to(torch.int32).reshape(1))
+        U, s, inf = K.svd_jacobi(R)
+        chk.add_flag(inf[:1])
+        return U, s
+    try:
+        R = K.chol_f32(G)
+    except RlaError:
+        return None
+    ratio = float((torch.diagonal(R) ** 2 / torch.diagonal(G).clamp_min(1e-300)).min())
+    if not ratio >= SCALED_PIVOT_MIN:
+        return None
+    U, s, inf = K.svd_jacobi(R)
+    if int(inf[0].item()):
+        return None
+    return U, s
+
+
 def small_svd_wide(B):
     """Thin SVD of a wide k x n device matrix B (k << n) through its Gram.
 
-    G = B B^T is accumulated in double-float.  For binary32 B (k <= 232)
-    U and s come from the Cholesky + one-sided Jacobi kernels; otherwise
-    G = U diag(lam) U^T and s = sqrt(lam).  Vh = diag(1/s) U^T B.
-    Returned in descending order.
+    For binary32 B (k <= 216) the binary32 route (``_svd_gram_f32``: Gram,
+    Cholesky and one-sided Jacobi, guarded by the scaled-pivot check) is
+    tried first.  Otherwise G = B B^T is accumulated in double-float; for
+    binary32 B (k <= 232) U and s come from the double-float Cholesky +
+    one-sided Jacobi kernels; otherwise G = U diag(lam) U^T and s = sqrt(lam).
+    Vh = diag(1/s) U^T B.  Returned in descending order.
     """
+    if B.dtype == torch.float32 and B.shape[0] <= 216:
+        res = _svd_gram_f32(B, trans=False)
+        if res is not None:
+            U, s = res
+            inv = torch.where(s > 0, 1.0 / s, torch.zeros_like(s))
+            Vh = K.gemm(U, B, transa=True, mode="f32") * inv[:, None]
+            return U, s, Vh
     B64 = B if B.dtype == torch.float64 else B.to(torch.float64)
     G = K.syrk(B64, mode="df")
     if B.dtype == torch.float32 and B.shape[0] <= JACOBI_MAX:
@@ -114,7 +169,11 @@ def small_svd_wide(B):
 
 
 def small_svd_tall(B):
-    """Thin SVD of a tall n x k device matrix B (k << n) through B^T B."""
+    """Thin SVD of a tall n x k device matrix B (k << n) through B^T B.
+
+    Always the double-float Gram: the tall B of the Nystrom drivers is not a
+    range finder's output, so its scaled Gram need not be well conditioned
+    (the binary32 route of ``small_svd_wide`` would fall back too often)."""
     B64 = B if B.dtype == torch.float64 else B.to(torch.float64)
     G = K.syrk(B64, trans=True, mode="df")
     if B.dtype == torch.float32 and B.shape[1] <= JACOBI_MAX:

@@ -107,3 +107,56 @@ def test_small_svd_wide_uses_jacobi(K, monkeypatch):
     assert float((Bh - Bd.double()).abs().max()) <= 1e-4 * float(Bd.abs().max())
     sl = np.linalg.svd(B.astype(float), compute_uv=False)
     assert np.allclose(s.cpu().numpy(), sl, rtol=1e-5)
+
+
+@pytest.mark.parametrize("n", [1, 2, 17, 64, 129, 210, 216])
+def test_chol_f32_and_inverse(K, n):
+    """rla_chol_inv_f32 with and without the inverse against binary64 Cholesky."""
+    g = torch.Generator(device="cuda").manual_seed(n)
+    Z = torch.randn((n, 2 * n + 3), generator=g, device="cuda", dtype=torch.float64)
+    Gd = Z @ Z.t() / Z.shape[1] + 0.1 * torch.eye(n, device="cuda", dtype=torch.float64)
+    G = Gd.float().contiguous()
+    Rref = torch.linalg.cholesky(Gd, upper=True)
+    R = K.chol_f32(G)
+    assert float((R.double() - Rref).abs().max() / Rref.abs().max()) < 2e-6
+    Rinv, R2 = K.chol_inv_f32(G, want_r=True)
+    assert torch.equal(R, R2)
+    Iref = torch.linalg.inv(Rref)
+    assert float((Rinv.double() - Iref).abs().max() / Iref.abs().max()) < 2e-6
+    assert torch.all(torch.tril(R, -1) == 0) and torch.all(torch.tril(Rinv, -1) == 0)
+
+
+def test_chol_f32_not_spd(K):
+    G = torch.eye(40, device="cuda")
+    G[25, 25] = -1.0
+    info = torch.zeros(1, dtype=torch.int32, device="cuda")
+    K.chol_f32(G, info=info)
+    assert int(info) == 26
+
+
+def test_small_svd_binary32_route_and_fallback(K):
+    """The binary32 Gram route is taken for a range finder's B (well
+    conditioned after diagonal scaling) and its singular values match binary64
+    to 1e-4 relative (the graded-spectrum bar of the Jacobi tests above); a B
+    whose scaled Gram is ill conditioned is refused by the guard and falls
+    back to the double-float route (singular values within 1e-5 s_max)."""
+    from parla_gb300.utils import linalg_wrappers as law
+    g = torch.Generator(device="cuda").manual_seed(5)
+    l, n = 120, 4096
+    V, _ = torch.linalg.qr(torch.randn((n, l), generator=g, device="cuda", dtype=torch.float64))
+    W, _ = torch.linalg.qr(torch.randn((l, l), generator=g, device="cuda", dtype=torch.float64))
+    s = torch.logspace(0, -3.5, l, dtype=torch.float64, device="cuda")
+    Wn = torch.eye(l, dtype=torch.float64, device="cuda") + 0.05 * (W - torch.eye(l, device="cuda", dtype=torch.float64))
+    B = ((Wn * s[None, :]) @ V.t()).float().contiguous()           # rows ~ scaled orthonormal rows
+    res = law._svd_gram_f32(B, trans=False)
+    assert res is not None
+    ref = torch.linalg.svdvals(B.double())
+    U, sv, Vh = law.small_svd_wide(B)
+    assert float(((sv.double() - ref).abs() / ref).max()) < 1e-4
+    # rows that mix strongly: kappa(G) 1e8 that scaling does not remove
+    M, _ = torch.linalg.qr(torch.randn((l, l), generator=g, device="cuda", dtype=torch.float64))
+    Bbad = ((M * torch.logspace(0, -4, l, dtype=torch.float64, device="cuda")[None, :]) @ V.t()).float().contiguous()
+    assert law._svd_gram_f32(Bbad, trans=False) is None
+    U2, sv2, Vh2 = law.small_svd_wide(Bbad)
+    ref2 = torch.linalg.svdvals(Bbad.double())
+    assert float((sv2.double() - ref2).abs().max()) < 1e-5 * float(ref2[0])
