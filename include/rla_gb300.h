@@ -147,6 +147,19 @@ int rla_syrk(int dtype, int trans, int64_t N, int64_t K, double alpha,
              const void* A, int64_t lda, double beta, void* C, int64_t ldc,
              void* ws, size_t* ws_bytes, rla_stream_t stream);
 
+/* Gram of binary32 data with double-float accumulation: G (N x N, binary64,
+ * leading dimension ldg) = A A^T for A (N x K, trans = 0) or A^T A for A
+ * (K x N, trans = 1), row-major A with leading dimension lda.  Each product
+ * of two binary32 numbers is formed exactly (one FMA) and added with a
+ * two-sum, so G carries about 48 bits; split-K partials in `ws` (two-call
+ * query) are summed in a fixed order.  The Gram matrices of the small SVDs
+ * and CholeskyQR on binary32 data (`B @ B.T`, parla/drivers/svd.py:165;
+ * `Q.T @ Q`, parla/utils/linalg_wrappers.py:6-7) without a binary64 copy of
+ * the operand. */
+int rla_gram_f32_df(int trans, int64_t N, int64_t K, const float* A,
+                    int64_t lda, double* G, int64_t ldg, void* ws,
+                    size_t* ws_bytes, rla_stream_t stream);
+
 /* Tensor-core GEMM (tcgen05.mma kind::f16, TMA-fed, FP32 accumulation in
  * TMEM): D (M x N, fp32) = alpha X W^T + beta D with X (M x K) and W (N x K)
  * bf16 row-major (both K-major; ldx, ldw multiples of 8, 16-byte aligned

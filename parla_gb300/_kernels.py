@@ -336,6 +336,21 @@ def chol_inv_f32(G, want_r=False, info=None):
     return (Rinv, R) if want_r else Rinv
 
 
+def gram_f32_df(A, trans=False):
+    """binary64 Gram A A^T (or A^T A with trans) of binary32 A, double-float
+    accumulation (``rla_gram_f32_df``)."""
+    A = A if A.stride(-1) == 1 else A.contiguous()
+    N = A.shape[1] if trans else A.shape[0]
+    K = A.shape[0] if trans else A.shape[1]
+    G = torch.empty((N, N), dtype=torch.float64, device=A.device)
+    head = (int(trans), N, K, ptr(A), A.stride(0), ptr(G), N)
+    need = size_query("rla_gram_f32_df", *head)
+    ws = workspace(need)
+    nb = C.c_size_t(need)
+    _timed("gram_f32_df", 2, call, "rla_gram_f32_df", *head, ptr(ws), C.byref(nb), stream())
+    return G
+
+
 def chol_f32(G, info=None):
     """Upper Cholesky factor R of an FP32 SPD G (n <= 216), one CTA, without
     the inverse (``rla_chol_inv_f32`` with Rinv = NULL).  Returns None when n

@@ -308,3 +308,127 @@ extern "C" int rla_syrk(int dtype, int trans, int64_t N, int64_t K, double alpha
     default: return RLA_ERR_ARG;
   }
 }
+
+// ---------------------------------------------------------------------------
+// Gram of binary32 rows (or columns) with double-float accumulation:
+// G (N x N, binary64) = A A^T for A (N x K) (trans = 0) or A^T A for A (K x N)
+// (trans = 1).  Products of binary32 numbers are exact as p + pe (one FMA),
+// and each is added with a two-sum into a (hi, lo) pair per output; the lazy
+// tail is renormalised once per 32-deep block of K.  64 x 64 output tiles on
+// and above the diagonal, 4 x 4 per thread; split-K partials (binary64) are
+// summed in a fixed order by a second kernel that also mirrors the lower
+// tiles.  About half the instructions of the double-float SYRK on binary64
+// storage, which has to carry the lo halves of both operands.
+namespace rla {
+namespace {
+constexpr int kGrBT = 64, kGrBK = 32, kGrTh = 256;
+
+__device__ __forceinline__ void gram_acc(float& hi, float& lo, float a, float b) {
+  const float p = a * b;
+  const float pe = fmaf(a, b, -p);
+  const float s = hi + p, bb = s - hi;
+  const float e = (hi - (s - bb)) + (p - bb);
+  hi = s;
+  lo += e + pe;
+}
+
+template <bool TRANS>
+__global__ void __launch_bounds__(kGrTh) gram_f32_df_kernel(int64_t N, int64_t K, int64_t kchunk,
+                                                             const float* __restrict__ A, int64_t lda,
+                                                             double* __restrict__ part) {
+  const int ti = blockIdx.y, tj = blockIdx.x;
+  if (ti > tj) return;
+  __shared__ __align__(16) float Ai[kGrBK][kGrBT + 4];
+  __shared__ __align__(16) float Aj[kGrBK][kGrBT + 4];
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  const int64_t k0 = static_cast<int64_t>(blockIdx.z) * kchunk, k1 = min(K, k0 + kchunk);
+  float hi[4][4] = {}, lo[4][4] = {};
+  for (int64_t kb = k0; kb < k1; kb += kGrBK) {
+    for (int e = tid; e < kGrBT * kGrBK; e += kGrTh) {
+      int r, c;
+      if (TRANS) { c = e / kGrBT; r = e % kGrBT; } else { r = e / kGrBK; c = e % kGrBK; }
+      const int64_t k = kb + c, gi = static_cast<int64_t>(ti) * kGrBT + r, gj = static_cast<int64_t>(tj) * kGrBT + r;
+      const bool ok = k < k1;
+      if (TRANS) {
+        Ai[c][r] = (ok && gi < N) ? A[k * lda + gi] : 0.f;
+        Aj[c][r] = (ok && gj < N) ? A[k * lda + gj] : 0.f;
+      } else {
+        Ai[c][r] = (ok && gi < N) ? A[gi * lda + k] : 0.f;
+        Aj[c][r] = (ok && gj < N) ? A[gj * lda + k] : 0.f;
+      }
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int c = 0; c < kGrBK; ++c) {
+      const float4 x = *reinterpret_cast<const float4*>(&Ai[c][ty * 4]);
+      const float4 y = *reinterpret_cast<const float4*>(&Aj[c][tx * 4]);
+      const float xx[4] = {x.x, x.y, x.z, x.w}, yy[4] = {y.x, y.y, y.z, y.w};
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) gram_acc(hi[a][b], lo[a][b], xx[a], yy[b]);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int b = 0; b < 4; ++b) {
+        const float s = hi[a][b] + lo[a][b];
+        lo[a][b] = lo[a][b] - (s - hi[a][b]);
+        hi[a][b] = s;
+      }
+  }
+  double* out = part + static_cast<int64_t>(blockIdx.z) * N * N;
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const int64_t i = static_cast<int64_t>(ti) * kGrBT + ty * 4 + a, j = static_cast<int64_t>(tj) * kGrBT + tx * 4 + b;
+      if (i < N && j < N) out[i * N + j] = static_cast<double>(hi[a][b]) + static_cast<double>(lo[a][b]);
+    }
+}
+
+__global__ void gram_reduce_kernel(int64_t N, int splits, const double* __restrict__ part, double* __restrict__ G,
+                                   int64_t ldg) {
+  const int64_t idx = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= N * N) return;
+  const int64_t i = idx / N, j = idx % N;
+  const bool up = (i / kGrBT) <= (j / kGrBT);  // tile computed directly
+  const int64_t ii = up ? i : j, jj = up ? j : i;
+  double s = 0.0;
+  for (int z = 0; z < splits; ++z) s += part[static_cast<int64_t>(z) * N * N + ii * N + jj];
+  G[i * ldg + j] = s;
+}
+
+inline int gram_splits(int64_t N, int64_t K) {
+  const int64_t tiles = ceil_div(N, kGrBT);
+  const int64_t useful = tiles * (tiles + 1) / 2;
+  const int64_t want = ceil_div(4LL * sm_count(), useful);
+  return static_cast<int>(imax(1, imin(want, imax(1, ceil_div(K, kGrBK)))));
+}
+}  // namespace
+}  // namespace rla
+
+extern "C" int rla_gram_f32_df(int trans, int64_t N, int64_t K, const float* A, int64_t lda, double* G, int64_t ldg,
+                               void* ws, size_t* ws_bytes, rla_stream_t stream) {
+  using namespace rla;
+  if (N < 0 || K < 0 || ldg < N || lda < (trans ? N : K)) return RLA_ERR_ARG;
+  int splits = gram_splits(N, K);
+  const int64_t kchunk = ceil_div(ceil_div(imax(K, 1), splits), kGrBK) * kGrBK;
+  splits = static_cast<int>(imax(1, ceil_div(imax(K, 1), kchunk)));
+  const size_t need = static_cast<size_t>(splits) * N * N * sizeof(double);
+  if (ws == nullptr && ws_bytes != nullptr) { *ws_bytes = need; return RLA_OK; }
+  if (!ws_bytes || *ws_bytes < need || (need && !ws)) return RLA_ERR_WORKSPACE;
+  if (N == 0) return RLA_OK;
+  if (!G || (K > 0 && !A)) return RLA_ERR_ARG;
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  const unsigned tiles = static_cast<unsigned>(ceil_div(N, kGrBT));
+  dim3 grid(tiles, tiles, static_cast<unsigned>(splits));
+  auto* part = static_cast<double*>(ws);
+  if (trans) gram_f32_df_kernel<true><<<grid, kGrTh, 0, st>>>(N, K, kchunk, A, lda, part);
+  else gram_f32_df_kernel<false><<<grid, kGrTh, 0, st>>>(N, K, kchunk, A, lda, part);
+  RLA_LAUNCH_CHECK();
+  gram_reduce_kernel<<<static_cast<unsigned>(ceil_div(N * N, 256)), 256, 0, st>>>(N, splits, part, G, ldg);
+  RLA_LAUNCH_CHECK();
+  return RLA_OK;
+}

@@ -30,8 +30,10 @@ def cholqr(Y, passes=2):
     """CholeskyQR repeated `passes` times; shifted first pass if needed."""
     Q = Y
     for p in range(passes):
-        Q64 = Q if Q.dtype == torch.float64 else Q.to(torch.float64)
-        G = K.syrk(Q64.contiguous(), trans=True, mode="df")
+        if Q.dtype == torch.float32:
+            G = K.gram_f32_df(Q, trans=True)
+        else:
+            G = K.syrk(Q.contiguous(), trans=True, mode="df")
         k = G.shape[0]
         chol = (lambda X: K.potrf_df_small(X, want64=True)[1]) if k <= JACOBI_MAX else \
             (lambda X: K.potrf_upper(X.clone(), mode="df"))
@@ -151,8 +153,7 @@ def small_svd_wide(B):
             inv = torch.where(s > 0, 1.0 / s, torch.zeros_like(s))
             Vh = K.gemm(U, B, transa=True, mode="f32") * inv[:, None]
             return U, s, Vh
-    B64 = B if B.dtype == torch.float64 else B.to(torch.float64)
-    G = K.syrk(B64, mode="df")
+    G = K.gram_f32_df(B) if B.dtype == torch.float32 else K.syrk(B, mode="df")
     if B.dtype == torch.float32 and B.shape[0] <= JACOBI_MAX:
         res = _svd_from_gram(G)
         if res is not None:
@@ -164,6 +165,7 @@ def small_svd_wide(B):
     lam, U = lam.flip(0), U.flip(1).contiguous()
     s = torch.sqrt(torch.clamp(lam, min=0.0))
     inv = torch.where(s > 0, 1.0 / s, torch.zeros_like(s))
+    B64 = B if B.dtype == torch.float64 else B.to(torch.float64)
     Vh = K.gemm(U.contiguous(), B64, transa=True, mode="df") * inv[:, None]
     return U, s, Vh.to(B.dtype) if B.dtype != torch.float64 else Vh
 
@@ -174,8 +176,7 @@ def small_svd_tall(B):
     Always the double-float Gram: the tall B of the Nystrom drivers is not a
     range finder's output, so its scaled Gram need not be well conditioned
     (the binary32 route of ``small_svd_wide`` would fall back too often)."""
-    B64 = B if B.dtype == torch.float64 else B.to(torch.float64)
-    G = K.syrk(B64, trans=True, mode="df")
+    G = K.gram_f32_df(B, trans=True) if B.dtype == torch.float32 else K.syrk(B, trans=True, mode="df")
     if B.dtype == torch.float32 and B.shape[1] <= JACOBI_MAX:
         res = _svd_from_gram(G)
         if res is not None:
@@ -187,6 +188,7 @@ def small_svd_tall(B):
     lam, V = lam.flip(0), V.flip(1).contiguous()
     s = torch.sqrt(torch.clamp(lam, min=0.0))
     inv = torch.where(s > 0, 1.0 / s, torch.zeros_like(s))
+    B64 = B if B.dtype == torch.float64 else B.to(torch.float64)
     U = K.gemm(B64, V.contiguous(), mode="df") * inv[None, :]
     return U.to(B.dtype) if B.dtype != torch.float64 else U, s, V.t().contiguous()
 

@@ -433,3 +433,20 @@ def test_geqrf_hl_batched_backward(K, shapes):
         scale = np.linalg.norm(A)
         assert np.linalg.norm(B[:, :n] - R) / scale <= 1e-13, (m, n)
         assert np.linalg.norm(B[:, n:] - F[:, n:]) / scale <= 1e-13, (m, n)
+
+
+@pytest.mark.parametrize("trans", [False, True])
+@pytest.mark.parametrize("shape", [(210, 8192), (528, 4096), (1, 7), (65, 33), (130, 1)])
+def test_gram_f32_df(K, trans, shape):
+    """rla_gram_f32_df against the binary64 Gram of the same binary32 data:
+    double-float accumulation, so within 1e-13 of max |G| (binary32 data are
+    exact in binary64)."""
+    g = torch.Generator(device="cuda").manual_seed(shape[0] * 7 + shape[1])
+    N, Kd = shape
+    A = torch.randn((Kd, N) if trans else (N, Kd), generator=g, device="cuda")
+    A[:, :1] *= 1e3                        # uneven scales
+    G = K.gram_f32_df(A, trans=trans)
+    A64 = A.double()
+    ref = A64.t() @ A64 if trans else A64 @ A64.t()
+    assert torch.equal(G, G.t())
+    assert float((G - ref).abs().max()) <= 1e-13 * float(ref.abs().max())
