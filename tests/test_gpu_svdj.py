@@ -147,7 +147,7 @@ def test_small_svd_binary32_route_and_fallback(K):
     W, _ = torch.linalg.qr(torch.randn((l, l), generator=g, device="cuda", dtype=torch.float64))
     s = torch.logspace(0, -3.5, l, dtype=torch.float64, device="cuda")
     Wn = torch.eye(l, dtype=torch.float64, device="cuda") + 0.05 * (W - torch.eye(l, device="cuda", dtype=torch.float64))
-    B = ((Wn * s[None, :]) @ V.t()).float().contiguous()           # rows ~ scaled orthonormal rows
+    B = ((s[:, None] * Wn) @ V.t()).float().contiguous()           # rows ~ scaled orthonormal rows
     res = law._svd_gram_f32(B, trans=False)
     assert res is not None
     ref = torch.linalg.svdvals(B.double())
