@@ -516,7 +516,11 @@ def bench_ls_single(torch, pg, cpu_budget=0.0):
         torch.cuda.synchronize()
         dt = (time.perf_counter() - t0) / reps
         xh = x.cpu().numpy()
-        out[prec] = {"solves_per_s": 1.0 / dt, "ms": dt * 1e3, "lsqr_itn": log.itn,
+        # phase split from one logged solve (the logged run synchronises per phase)
+        _, lg = solver(A, b, 0.0, 1e-12, 200, 99, logging=True)
+        phases = {"sketch_ms": 1e3 * lg.time_sketch, "factor_ms": 1e3 * lg.time_factor,
+                  "presolve_ms": 1e3 * lg.time_presolve, "iterate_ms": 1e3 * lg.time_iterate}
+        out[prec] = {"solves_per_s": 1.0 / dt, "ms": dt * 1e3, "lsqr_itn": log.itn, "phases_logged": phases,
                      "pred_err": float(la.norm(An @ (xh - xr)) / la.norm(An @ xr)),
                      "x_err": float(la.norm(xh - xr) / la.norm(xr))}
     out["speedup_df_vs_f64"] = out["df"]["solves_per_s"] / out["f64"]["solves_per_s"]
