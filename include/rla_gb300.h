@@ -65,6 +65,40 @@ int rla_abi_version(void);
 int rla_gaussian_fill(int dtype, int64_t rows, int64_t cols, uint64_t seed,
                       double scale, void* S, int64_t lds, rla_stream_t stream);
 
+/* Grid Gaussian operator: S[i*lds+j] = clip(rint(4 z_ij), -31, 31) as bf16,
+ * z_ij the N(0,1) draw rla_gaussian_fill makes for the same (seed, i, j), so
+ * the operator unit * S (unit = scale / 4) is the Gaussian of that call
+ * rounded to the nearest multiple of scale / 4.  Columns cols..lds-1 are set
+ * to zero (lds a multiple of 8 for rla_sketch_sliced).  The device-drawn
+ * binary64 gaussian_operator (parla/utils/sketching.py:20-31) of the
+ * least-squares drivers; its products are exact through rla_sketch_sliced. */
+int rla_gaussian_grid_bf16(int64_t rows, int64_t cols, uint64_t seed, void* S,
+                           int64_t lds, rla_stream_t stream);
+
+/* Exact sliced sketch on the tensor cores: Y (d x n, binary64) = unit * S X
+ * and, when b != NULL, yb (d) = unit * S b, for S (d x m, bf16 integers of
+ * magnitude <= 31, row stride lds a multiple of 8, 16-byte aligned) and X
+ * (m x n binary64, row-major).  Each column of [X | b] is expanded in
+ * fixed point relative to its power-of-two bound as T digits of q bits
+ * (q T >= 48; rla_sketch_sliced_digits), so every partial sum of the bf16
+ * GEMM S [digits] is an integer below 2^24 and the GEMM is exact; the digit
+ * planes are combined in binary64.  The result equals unit * S X' with X'
+ * within 2^-49 max_k |X_kj| of X column by column.  A column holding NaN or
+ * Inf gives NaN.  Workspace by the two-call query; its first bytes hold the
+ * tensor-core GEMM's error flag (rla_gemm_bf16_tc_status).
+ * RLA_ERR_UNSUPPORTED when m > 270600 (no digit width keeps the sums exact).
+ * Replaces A_ske = S @ A and b_ske = S @ b
+ * (parla/drivers/least_squares.py:303,313) for the Gaussian sketch. */
+int rla_sketch_sliced(int64_t d, int64_t m, int64_t n, const void* S,
+                      int64_t lds, double unit, const double* X, int64_t ldx,
+                      const double* b, double* Y, int64_t ldy, double* yb,
+                      void* ws, size_t* ws_bytes, rla_stream_t stream);
+
+/* Digit width q and count T rla_sketch_sliced uses for m-deep sums (the
+ * largest q with 31 * 2^q * m <= 2^24, at most 8; T = ceil(48 / q)); q = 0
+ * when m is too deep. */
+int rla_sketch_sliced_digits(int64_t m, int* q, int* T);
+
 /* SJLT pattern for a wide d x m operator: for every column j, `nnz` distinct
  * rows rows[j*nnz + t] in [0, d) and signs[j*nnz + t] in {-1, +1}; the value
  * of each nonzero is sign / sqrt(nnz).  Device-side replacement of the

@@ -9,7 +9,7 @@ kernels of ``librla_gb300.so`` (C ABI in ``include/rla_gb300.h``).
 __version__ = "0.1.0"
 
 from .utils.sketching import (gaussian_operator, sjlt_operator, srct_operator, generate_srct,
-                              DeviceOperator, DenseOperator, GaussianOperator, SJLTOperator,
+                              DeviceOperator, DenseOperator, GaussianOperator, GridGaussianOperator, SJLTOperator,
                               SRCTOperator)
 from .comps.sketchers.oblivious import SketchOpGen, SkOpGA, SkOpSJ, SkOpTC
 from .comps.sketchers.aware import RowSketcher, RS1

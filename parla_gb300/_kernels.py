@@ -184,6 +184,44 @@ def gaussian_fill(rows, cols, seed, scale, dtype=torch.float64):
     return S
 
 
+def gaussian_grid_bf16(rows, cols, seed):
+    """Grid Gaussian (bf16 integers |s| <= 31; the operator is scale/4 times
+    this) as a (rows, cols) view with a row stride that is a multiple of 8."""
+    S = empty_bf16(rows, cols, device())
+    _timed("gaussian_grid", 1, call, "rla_gaussian_grid_bf16", rows, cols, C.c_uint64(seed), ptr(S), S.stride(0),
+           stream())
+    return S
+
+
+def sliced_digits(m):
+    """(q, T) of the exact sliced sketch for m-deep sums (q = 0: unsupported)."""
+    q, T = C.c_int(0), C.c_int(0)
+    call("rla_sketch_sliced_digits", m, C.byref(q), C.byref(T))
+    return q.value, T.value
+
+
+def sketch_sliced(S_int, unit, X, b=None):
+    """(unit * S X, unit * S b) exactly up to a 2^-49 column-relative
+    expansion of [X | b] (``rla_sketch_sliced``); X (m x n) binary64, b (m,)
+    or None.  Returns (Y, yb) with yb None when b is None."""
+    d, m = S_int.shape
+    if X is not None:
+        X = X if X.stride(-1) == 1 else X.contiguous()
+        n, ldx = X.shape[1], X.stride(0)
+    else:
+        n, ldx = 0, 0
+    Y = torch.empty((d, n), dtype=torch.float64, device=S_int.device) if n else None
+    yb = torch.empty(d, dtype=torch.float64, device=S_int.device) if b is not None else None
+    bb = b.contiguous() if b is not None else None
+    head = (d, m, n, ptr(S_int), S_int.stride(0), float(unit), ptr(X) if n else None, ldx, ptr(bb),
+            ptr(Y) if n else None, n if n else 1, ptr(yb))
+    need = size_query("rla_sketch_sliced", *head)
+    ws = workspace(need)
+    nb = C.c_size_t(need)
+    _timed("sketch_sliced", 5, call, "rla_sketch_sliced", *head, ptr(ws), C.byref(nb), stream())
+    return Y, yb
+
+
 def sjlt_pattern(d, m, nnz, seed):
     rows = torch.empty(m * nnz, dtype=torch.int32, device=device())
     signs = torch.empty(m * nnz, dtype=torch.int8, device=device())

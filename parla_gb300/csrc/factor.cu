@@ -10,7 +10,11 @@
 //   orgqr  - thin Q from the reflectors
 //   potrf  - upper Cholesky, row-major, right-looking
 //   trtri  - inverse of an upper-triangular matrix, one warp per column
+#include <cooperative_groups.h>
+
 #include "arith.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace rla {
 namespace {
@@ -289,6 +293,251 @@ __global__ void __launch_bounds__(1024) potrf_small_f32_kernel(int n, float* __r
 
 constexpr int kSmallPotrfMax = 238;
 
+
+// ------------------------------------------------------- QR on one cluster
+// Householder QR of one column-major m x (n + nrhs) matrix by one thread-block
+// cluster of CS CTAs (16 where the device allows that size, else 8), the
+// matrix resident in distributed shared memory: CTA r holds rows
+// [r rb, (r + 1) rb) of every column, row-major, as register values (binary64
+// or double-float).  Per column j, two cluster barriers:
+//   A  every CTA has put its partial sum of squares of column j below row j
+//      (and the owner of row j the pivot a_jj) in shared memory; each CTA
+//      sums the CS partials in rank order (the same xor tree in every CTA)
+//      and forms beta, tau and the reflector scale identically;
+//   B  every CTA has put its partial w_c = sum_(own rows) v_i a_ic for the
+//      trailing columns c in shared memory; each CTA sums them in rank order
+//      and updates its own rows, a_ic -= v_i tau w_c.
+// The single partial buffers are safe: a CTA writes the next column's
+// partials only after passing a barrier that every reader of the current
+// ones has reached after reading.  Output as LAPACK geqrf (R on and above
+// the diagonal, v below, tau per column).  Sums run in a fixed order, so
+// results do not depend on scheduling.
+constexpr int kCqThreads = 512;
+
+template <typename V> struct CqOps;
+template <> struct CqOps<double> {
+  __device__ static void mac(double& acc, double x, double y) { acc = fma(x, y, acc); }
+  __device__ static void renorm(double&) {}
+  __device__ static double fms(double a, double x, double y) { return fma(-x, y, a); }
+  __device__ static double add(double a, double b) { return a + b; }
+};
+template <> struct CqOps<df> {
+  // acc += x y: exact leading product, two-sum into hi, lazy tail
+  __device__ static void mac(df& acc, df x, df y) {
+    const float p = x.hi * y.hi;
+    float pe = fmaf(x.hi, y.hi, -p);
+    pe = fmaf(x.hi, y.lo, fmaf(x.lo, y.hi, pe));
+    const float s = acc.hi + p, bb = s - acc.hi;
+    const float e = (acc.hi - (s - bb)) + (p - bb);
+    acc.hi = s;
+    acc.lo += e + pe;
+  }
+  __device__ static void renorm(df& a) { a = quick_two_sum(a.hi, a.lo); }
+  // a - x y with one renormalisation
+  __device__ static df fms(df a, df x, df y) {
+    const float p = x.hi * y.hi;
+    float pe = fmaf(x.hi, y.hi, -p);
+    pe = fmaf(x.hi, y.lo, fmaf(x.lo, y.hi, pe));
+    const df s = two_sum(a.hi, -p);
+    return quick_two_sum(s.hi, s.lo + (a.lo - pe));
+  }
+  __device__ static df add(df a, df b) { return df_add(a, b); }
+};
+
+template <typename V>
+__host__ __device__ inline size_t cq_smem_bytes(int64_t rb, int64_t nc) {
+  // a (rb x nc) + partial w (nc) + summed w (nc) + own reflector (rb) + partial sigma/alpha (2)
+  return sizeof(V) * static_cast<size_t>(rb * nc + 2 * nc + rb + 2);
+}
+
+template <typename V>
+__global__ void __launch_bounds__(kCqThreads, 1)
+geqrf_cluster_kernel(int64_t m, int64_t n, int64_t nrhs, double* __restrict__ A, int64_t lda,
+                     double* __restrict__ tau, int rb) {
+  using R = Ar<V>;
+  using O = CqOps<V>;
+  cg::cluster_group cl = cg::this_cluster();
+  const int rank = static_cast<int>(cl.block_rank()), CS = static_cast<int>(cl.num_blocks());
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int nc = static_cast<int>(n + nrhs);
+  V* a = reinterpret_cast<V*>(smem_raw);  // own rows, row-major rb x nc
+  V* pw = a + static_cast<int64_t>(rb) * nc;
+  V* wv = pw + nc;
+  V* vl = wv + nc;
+  V* pn = vl + rb;
+  __shared__ V s_par[3];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int64_t row0 = static_cast<int64_t>(rank) * rb;
+  for (int64_t e = tid; e < static_cast<int64_t>(rb) * nc; e += blockDim.x) {
+    const int i = static_cast<int>(e % rb), c = static_cast<int>(e / rb);
+    const int64_t ig = row0 + i;
+    a[static_cast<int64_t>(i) * nc + c] = ig < m ? R::ld(A + c * lda + ig) : R::zero();
+  }
+  __syncthreads();
+  // partial sum of squares of column j below row j; the owner of row j also
+  // publishes the pivot
+  auto col_sigma = [&](int64_t j) {
+    if (warp != 0) return;
+    V sg = R::zero();
+    for (int i = lane; i < rb; i += 32) {
+      const int64_t ig = row0 + i;
+      if (ig > j && ig < m) {
+        const V x = a[static_cast<int64_t>(i) * nc + j];
+        sg = R::fma(sg, x, x);
+      }
+    }
+    sg = R::wsum(sg);
+    if (lane == 0) {
+      pn[0] = sg;
+      pn[1] = (j >= row0 && j < row0 + rb) ? a[(j - row0) * nc + j] : R::zero();
+    }
+  };
+  col_sigma(0);
+  for (int64_t j = 0; j < n; ++j) {
+    cl.sync();  // A
+    if (warp == 0) {
+      V sg = R::zero(), al = R::zero();
+      if (lane < CS) {
+        const V* rp = cl.map_shared_rank(pn, lane);
+        sg = rp[0];
+        al = rp[1];
+      }
+      sg = R::wsum(sg);
+      al = R::wsum(al);  // only the owner's term is nonzero
+      if (lane == 0) {
+        V beta, t, sc;
+        if (R::is_zero(sg)) {
+          beta = al; t = R::zero(); sc = R::zero();
+        } else {
+          const V nrm = R::sqrt(R::fma(sg, al, al));
+          beta = R::pos(al) ? R::neg(nrm) : nrm;  // beta = -sign(alpha) ||x||
+          t = R::div(R::sub(beta, al), beta);
+          sc = R::div(R::one(), R::sub(al, beta));
+        }
+        s_par[0] = beta; s_par[1] = t; s_par[2] = sc;
+        if (rank == 0) R::st(tau + j, t);
+      }
+    }
+    __syncthreads();
+    const V beta = s_par[0], t = s_par[1], sc = s_par[2];
+    const int ilo = static_cast<int>(imax(0, imin(rb, j - row0)));  // first own row with index >= j
+    for (int i = tid; i < rb; i += blockDim.x) {
+      const int64_t ig = row0 + i;
+      V v = R::zero();
+      if (ig == j) {
+        v = R::one();
+        a[static_cast<int64_t>(i) * nc + j] = beta;
+      } else if (ig > j && ig < m) {
+        v = R::mul(a[static_cast<int64_t>(i) * nc + j], sc);
+        a[static_cast<int64_t>(i) * nc + j] = v;
+      }
+      vl[i] = v;
+    }
+    __syncthreads();
+    const bool act = !R::is_zero(t);  // identical in every CTA
+    if (act) {
+      for (int64_t c = j + 1 + tid; c < nc; c += blockDim.x) {
+        V acc0 = R::zero(), acc1 = R::zero();
+        int i = ilo;
+        for (; i + 1 < rb; i += 2) {
+          O::mac(acc0, vl[i], a[static_cast<int64_t>(i) * nc + c]);
+          O::mac(acc1, vl[i + 1], a[static_cast<int64_t>(i + 1) * nc + c]);
+        }
+        if (i < rb) O::mac(acc0, vl[i], a[static_cast<int64_t>(i) * nc + c]);
+        O::renorm(acc0);
+        O::renorm(acc1);
+        pw[c] = O::add(acc0, acc1);
+      }
+    }
+    cl.sync();  // B
+    if (act) {
+      for (int64_t c = j + 1 + tid; c < nc; c += blockDim.x) {
+        V sw = R::zero();
+        for (int r = 0; r < CS; ++r) sw = O::add(sw, cl.map_shared_rank(pw, r)[c]);
+        wv[c] = R::mul(t, sw);
+      }
+      __syncthreads();
+      // a_ic -= v_i (tau w_c): with ncu < threads, thread -> column
+      // j+1 + tid % ncu and rows strided by the number of column groups;
+      // wider trailing blocks take a column per thread in turn
+      const int ncu = static_cast<int>(nc - j - 1);
+      if (ncu >= kCqThreads) {
+        for (int64_t c = j + 1 + tid; c < nc; c += blockDim.x) {
+          const V w = wv[c];
+          for (int i = ilo; i < rb; ++i) {
+            V* x = a + static_cast<int64_t>(i) * nc + c;
+            *x = O::fms(*x, vl[i], w);
+          }
+        }
+      } else if (ncu > 0) {
+        const int groups = kCqThreads / ncu;
+        const int g = tid / ncu;
+        if (g < groups) {
+          const int64_t c = j + 1 + tid % ncu;
+          const V w = wv[c];
+          for (int i = ilo + g; i < rb; i += groups) {
+            V* x = a + static_cast<int64_t>(i) * nc + c;
+            *x = O::fms(*x, vl[i], w);
+          }
+        }
+      }
+    }
+    __syncthreads();
+    if (j + 1 < n) col_sigma(j + 1);
+  }
+  cl.sync();  // no CTA leaves while another may still read its shared memory
+  for (int64_t e = tid; e < static_cast<int64_t>(rb) * nc; e += blockDim.x) {
+    const int i = static_cast<int>(e % rb), c = static_cast<int>(e / rb);
+    const int64_t ig = row0 + i;
+    if (ig < m) R::st(A + c * lda + ig, a[static_cast<int64_t>(i) * nc + c]);
+  }
+}
+
+// Launch on one cluster of 16 CTAs (non-portable size), else 8; returns
+// RLA_ERR_UNSUPPORTED when the matrix does not fit the cluster's shared
+// memory (the caller then takes the grid form).
+template <typename V>
+int geqrf_cluster_launch(int64_t m, int64_t n, int64_t nrhs, double* A, int64_t lda, double* tau, cudaStream_t st) {
+  auto kern = geqrf_cluster_kernel<V>;
+  int dev = 0, optin = 0;
+  RLA_CUDA_TRY(cudaGetDevice(&dev));
+  RLA_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  static thread_local int attr_dev = -1;
+  if (attr_dev != dev) {
+    RLA_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - 1024));
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)
+      (void)cudaGetLastError();
+    attr_dev = dev;
+  }
+  const int64_t nc = n + nrhs;
+  for (int cs : {16, 8}) {
+    const int64_t rb = ceil_div(m, cs);
+    const size_t smem = cq_smem_bytes<V>(rb, nc);
+    if (smem + 1024 > static_cast<size_t>(optin)) continue;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(cs);
+    cfg.blockDim = dim3(kCqThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = cs;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int ncl = 0;
+    if (cudaOccupancyMaxActiveClusters(&ncl, kern, &cfg) != cudaSuccess) {
+      (void)cudaGetLastError();
+      continue;
+    }
+    if (ncl < 1) continue;
+    const int rbi = static_cast<int>(rb);
+    RLA_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, m, n, nrhs, A, lda, tau, rbi));
+    return RLA_OK;
+  }
+  return RLA_ERR_UNSUPPORTED;
+}
 }  // namespace
 }  // namespace rla
 
@@ -311,6 +560,12 @@ int rla_geqrf_ctas(int dtype, int64_t m, int64_t n, int64_t nrhs, double* A, int
   if (n == 0) return RLA_OK;
   if (!A || !tau || !ws) return RLA_ERR_ARG;
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  if ((dtype == RLA_DF || dtype == RLA_F64) && (max_ctas == 0 || max_ctas >= 16)) {
+    // one cluster with the matrix in distributed shared memory when it fits
+    const int rc = dtype == RLA_DF ? geqrf_cluster_launch<df>(m, n, nrhs, A, lda, tau, st)
+                                   : geqrf_cluster_launch<double>(m, n, nrhs, A, lda, tau, st);
+    if (rc != RLA_ERR_UNSUPPORTED) return rc;
+  }
   RLA_CUDA_TRY(cudaMemsetAsync(ws, 0, kBarBytes, st));
   GridBar bar = bar_from_ws(ws);
   void* args[] = {&m, &n, &nrhs, &A, &lda, &tau, &bar};

@@ -206,6 +206,160 @@ __global__ void sym_mirror_kernel(int64_t N, Out* __restrict__ C, int64_t ldc, i
   if (i / tile > j / tile) C[i * ldc + j] = C[j * ldc + i];
 }
 
+// ---------------------------------------------------------------- GEMV
+// Products with one output row or column (N == 1 or M == 1) are memory-bound
+// matrix-vector products; a 64 x 64 output tile would use one of its 64 rows
+// or columns.  Two forms, both with a split of K over blockIdx.y (partials
+// summed in a fixed order by splitk_reduce_kernel):
+//   rows - y_r = sum_k X[r, k] v_k, X row-major: one warp per output, lanes
+//          stride along the row (coalesced), xor-tree warp sum;
+//   cols - y_c = sum_k X[k, c] v_k: one thread per output, consecutive
+//          threads read consecutive entries of a row of X.
+constexpr int kGvThreads = 256;
+
+__device__ __forceinline__ float acc_shfl_xor(float v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
+__device__ __forceinline__ double acc_shfl_xor(double v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
+__device__ __forceinline__ df acc_shfl_xor(df v, int o) {
+  return df{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
+}
+__device__ __forceinline__ float acc_combine(float a, float b) { return a + b; }
+__device__ __forceinline__ double acc_combine(double a, double b) { return a + b; }
+__device__ __forceinline__ df acc_combine(df a, df b) { return df_add(a, b); }
+
+template <class P>
+__device__ __forceinline__ void gemv_finish(typename P::Acc acc, int64_t o, int64_t n_out, double alpha, double beta,
+                                            typename P::Out* __restrict__ y, int64_t incy,
+                                            typename P::Part* __restrict__ part) {
+  if (part) {
+    part[static_cast<int64_t>(blockIdx.y) * n_out + o] = P::part(acc);
+  } else {
+    typename P::Out* c = y + o * incy;
+    *c = P::out(acc, alpha, beta, c);
+  }
+}
+
+template <class P>
+__global__ void __launch_bounds__(kGvThreads)
+gemv_rows_kernel(int64_t R, int64_t K, int64_t kchunk, double alpha, const typename P::In* __restrict__ X, int64_t ldx,
+                 const typename P::In* __restrict__ v, int64_t incv, double beta, typename P::Out* __restrict__ y,
+                 int64_t incy, typename P::Part* __restrict__ part) {
+  const int lane = threadIdx.x & 31;
+  const int64_t r = static_cast<int64_t>(blockIdx.x) * (kGvThreads / 32) + (threadIdx.x >> 5);
+  if (r >= R) return;  // whole warps leave together
+  const int64_t kb = static_cast<int64_t>(blockIdx.y) * kchunk, ke = imin(K, kb + kchunk);
+  const typename P::In* xr = X + r * ldx;
+  typename P::Acc acc = P::acc0();
+  int64_t k = kb + lane;
+  int cnt = 0;
+  for (; k + 96 < ke; k += 128) {  // four independent loads per lane in flight
+    typename P::In a[4], b[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      a[u] = xr[k + 32 * u];
+      b[u] = v[(k + 32 * u) * incv];
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) P::madd(acc, P::cvt(a[u]), P::cvt(b[u]));
+    if ((++cnt & 1) == 0) P::renorm(acc);
+  }
+  for (; k < ke; k += 32) P::madd(acc, P::cvt(xr[k]), P::cvt(v[k * incv]));
+  P::renorm(acc);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc = acc_combine(acc, acc_shfl_xor(acc, o));
+  if (lane == 0) gemv_finish<P>(acc, r, R, alpha, beta, y, incy, part);
+}
+
+template <class P>
+__global__ void __launch_bounds__(kGvThreads)
+gemv_cols_kernel(int64_t Cn, int64_t K, int64_t kchunk, double alpha, const typename P::In* __restrict__ X, int64_t ldx,
+                 const typename P::In* __restrict__ v, int64_t incv, double beta, typename P::Out* __restrict__ y,
+                 int64_t incy, typename P::Part* __restrict__ part) {
+  const int64_t c = static_cast<int64_t>(blockIdx.x) * kGvThreads + threadIdx.x;
+  if (c >= Cn) return;
+  const int64_t kb = static_cast<int64_t>(blockIdx.y) * kchunk, ke = imin(K, kb + kchunk);
+  typename P::Acc acc = P::acc0();
+  int64_t k = kb;
+  int cnt = 0;
+  for (; k + 3 < ke; k += 4) {
+    typename P::In a[4], b[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      a[u] = X[(k + u) * ldx + c];
+      b[u] = v[(k + u) * incv];
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) P::madd(acc, P::cvt(a[u]), P::cvt(b[u]));
+    if ((++cnt & 1) == 0) P::renorm(acc);
+  }
+  for (; k < ke; ++k) P::madd(acc, P::cvt(X[k * ldx + c]), P::cvt(v[k * incv]));
+  P::renorm(acc);
+  gemv_finish<P>(acc, c, Cn, alpha, beta, y, incy, part);
+}
+
+template <typename Part, typename Out>
+__global__ void splitk_reduce_kernel(int64_t M, int64_t N, int splits, double alpha, const Part* __restrict__ part,
+                                     double beta, Out* __restrict__ C, int64_t ldc, int sym_tile);
+
+// op(A) op(B) with M == 1 or N == 1 (not a symmetric product).  X is the
+// matrix operand, v the vector one; n_out outputs written to C with stride
+// (N == 1: ldc, M == 1: 1).
+template <class P>
+int gemv_launch(int ta, int tb, int64_t M, int64_t N, int64_t K, double alpha, const void* A, int64_t lda,
+                const void* B, int64_t ldb, double beta, void* C, int64_t ldc, void* ws, size_t* ws_bytes,
+                cudaStream_t st) {
+  using In = typename P::In;
+  using Part = typename P::Part;
+  const bool col_out = (N == 1);
+  const int64_t n_out = col_out ? M : N;
+  bool rows;
+  const In *X, *v;
+  int64_t ldx, incv;
+  if (col_out) {  // y (M) = op(A) b
+    rows = !ta;
+    X = static_cast<const In*>(A); ldx = lda;
+    v = static_cast<const In*>(B); incv = tb ? 1 : ldb;
+  } else {        // y (N) = op(B)^T a
+    rows = tb;
+    X = static_cast<const In*>(B); ldx = ldb;
+    v = static_cast<const In*>(A); incv = ta ? lda : 1;
+  }
+  const int sms = sm_count();
+  int64_t splits;
+  if (rows) splits = imin(ceil_div(32LL * sms, imax(n_out, 1)), imax(1, K / 512));
+  else splits = imin(ceil_div(1024LL * sms, ceil_div(imax(n_out, 1), kGvThreads) * kGvThreads), imax(1, K / 64));
+  splits = imax(1, imin(splits, 64));
+  const size_t need = splits > 1 ? static_cast<size_t>(splits) * n_out * sizeof(Part) : 0;
+  if (ws == nullptr && ws_bytes != nullptr) {  // size query
+    *ws_bytes = need;
+    return RLA_OK;
+  }
+  if (splits > 1) {
+    const size_t have = (ws && ws_bytes) ? *ws_bytes : 0;
+    if (have < need) splits = imax(1, imin(splits, static_cast<int64_t>(have / (static_cast<size_t>(n_out) * sizeof(Part)))));
+  }
+  if (M == 0 || N == 0) return RLA_OK;
+  const int64_t kchunk = imax(1, ceil_div(imax(K, 1), splits));
+  splits = imax(1, ceil_div(imax(K, 1), kchunk));
+  Part* part = splits > 1 ? static_cast<Part*>(ws) : nullptr;
+  auto* y = static_cast<typename P::Out*>(C);
+  const int64_t incy = col_out ? ldc : 1;
+  if (rows) {
+    dim3 grid(static_cast<unsigned>(ceil_div(n_out, kGvThreads / 32)), static_cast<unsigned>(splits));
+    gemv_rows_kernel<P><<<grid, kGvThreads, 0, st>>>(n_out, K, kchunk, alpha, X, ldx, v, incv, beta, y, incy, part);
+  } else {
+    dim3 grid(static_cast<unsigned>(ceil_div(n_out, kGvThreads)), static_cast<unsigned>(splits));
+    gemv_cols_kernel<P><<<grid, kGvThreads, 0, st>>>(n_out, K, kchunk, alpha, X, ldx, v, incv, beta, y, incy, part);
+  }
+  RLA_LAUNCH_CHECK();
+  if (splits > 1) {
+    const int64_t om = col_out ? M : 1, on = col_out ? 1 : N;
+    splitk_reduce_kernel<Part, typename P::Out><<<static_cast<unsigned>(ceil_div(n_out, 256)), 256, 0, st>>>(
+        om, on, static_cast<int>(splits), alpha, part, beta, y, ldc, 0);
+    RLA_LAUNCH_CHECK();
+  }
+  return RLA_OK;
+}
+
 template <class P>
 int gemm_launch(int ta, int tb, int64_t M, int64_t N, int64_t K, double alpha,
                 const void* A, int64_t lda, const void* B, int64_t ldb, double beta,
@@ -213,6 +367,7 @@ int gemm_launch(int ta, int tb, int64_t M, int64_t N, int64_t K, double alpha,
   using In = typename P::In;
   using Out = typename P::Out;
   using Part = typename P::Part;
+  if (!sym && (N == 1 || M == 1)) return gemv_launch<P>(ta, tb, M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, ws, ws_bytes, st);
   const int64_t tiles_m = ceil_div(M, P::BM), tiles_n = ceil_div(N, P::BN);
   const int64_t tiles = sym ? tiles_m * (tiles_m + 1) / 2 : tiles_m * tiles_n;
   int splits = 1;

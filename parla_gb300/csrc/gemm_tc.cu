@@ -31,6 +31,7 @@ constexpr int kTcThreads = 192;
 constexpr int kBM = 128;
 constexpr int kBK = 64;                 // 64 bf16 = one 128-byte swizzle row
 constexpr int kMaxStages = 6;
+constexpr int kStageBudget = 200 * 1024;  // shared memory for the stage buffers
 constexpr long long kWaitLimit = 1LL << 26;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -323,7 +324,7 @@ TcPlan tc_plan(int64_t M, int64_t N, int64_t K, int want_splits) {
   p.tiles_m = ceil_div(M, kBM);
   p.tiles_n = ceil_div(N, p.n_tile);
   const int stage_bytes = (kBM + p.n_tile) * kBK * 2;
-  p.stages = static_cast<int>(imin(kMaxStages, (200 * 1024) / stage_bytes));
+  p.stages = static_cast<int>(imin(kMaxStages, kStageBudget / stage_bytes));
   const int64_t total_kb = ceil_div(K, kBK);
   int splits = want_splits;
   if (splits <= 0) {
@@ -382,15 +383,16 @@ extern "C" int rla_gemm_bf16_tc(int64_t M, int64_t N, int64_t K, const void* X, 
   int dev = 0;
   RLA_CUDA_TRY(cudaGetDevice(&dev));
   {
-    // raise the dynamic shared-memory limit once per device to the largest
-    // plan (n_tile = 256) so later calls need no attribute change
+    // raise the dynamic shared-memory limit once per device to the cap of
+    // every plan (stages * stage bytes <= kStageBudget, plus the alignment
+    // pad), so later calls need no attribute change
     std::lock_guard<std::mutex> lock(g_attr_mu);
     if (dev >= 0 && dev < 64 && !g_attr_set[dev]) {
-      TcPlan big = tc_plan(kBM, 256, kBK, 1);
       RLA_CUDA_TRY(cudaFuncSetAttribute(gemm_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        static_cast<int>(imax(big.smem, pl.smem))));
+                                        kStageBudget + 1024));
       g_attr_set[dev] = true;
     }
+    if (pl.smem > static_cast<size_t>(kStageBudget + 1024)) return RLA_ERR_UNSUPPORTED;
   }
   CUtensorMap mx, mw;
   int rc = make_map(&mx, X, M, K, ldx, pl.bm);

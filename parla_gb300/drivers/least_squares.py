@@ -21,7 +21,7 @@ from .. import _kernels as K
 from ..comps.determiter.logging import SketchAndPrecondLog
 from ..comps.determiter.saddle import PcSS2
 from ..comps.preconditioning import svd_right_precond
-from ..utils.sketching import DenseOperator, DeviceOperator
+from ..utils.sketching import DenseOperator, DeviceOperator, GridGaussianOperator
 
 
 class OverLstsqSolver:
@@ -59,12 +59,24 @@ def _clock(logging):
 
 
 def _apply(S, X, precision):
-    """S @ X on the device; a dense Gaussian runs the double-float GEMM under 'df'."""
+    """S @ X on the device.  Under 'df' a grid Gaussian runs the exact sliced
+    tensor-core product and any other dense operator the double-float GEMM."""
     if not isinstance(S, DeviceOperator):
         raise TypeError("sketch_op_gen must return a parla_gb300 device operator")
+    if precision == "df" and isinstance(S, GridGaussianOperator) and S.sliced_ok(X):
+        if X.dim() == 1:
+            return S.sliced_left(None, X)[1]
+        return S.sliced_left(X)[0]
     if precision == "df" and isinstance(S, DenseOperator):
         return K.gemm(S.S, X, mode="df")
     return S._left(X)
+
+
+def _apply_pair(S, A, b, precision):
+    """(S @ A, S @ b); one sliced product for both under 'df' with a grid Gaussian."""
+    if precision == "df" and isinstance(S, GridGaussianOperator) and S.sliced_ok(A):
+        return S.sliced_left(A, b)
+    return _apply(S, A, precision), _apply(S, b, precision)
 
 
 def _qr_presolve(A_ske, b_ske, n, d, sd, precision):
@@ -119,8 +131,7 @@ class SSO1(OverLstsqSolver):
         log = {"time_sketch": -1.0, "time_solve": -1.0}
         tic = clock()
         S = self.sketch_op_gen(d, m, rng)
-        A_ske = _apply(S, Ad, self.precision)
-        b_ske = _apply(S, bd, self.precision)
+        A_ske, b_ske = _apply_pair(S, Ad, bd, self.precision)
         log["time_sketch"] = clock() - tic
         tic = clock()
         R, z = _qr_presolve(A_ske, b_ske, n, d, np.sqrt(delta), self.precision)
@@ -157,12 +168,14 @@ class SPO(OverLstsqSolver):
 
         tic = clock()
         S = self.sketch_op_gen(d, m, rng)
-        A_ske = _apply(S, Ad, prec)
+        if self.mode == "qr":
+            A_ske, b_ske = _apply_pair(S, Ad, bd, prec)
+        else:
+            A_ske = _apply(S, Ad, prec)
         log.time_sketch = clock() - tic
 
         if self.mode == "qr":
             tic = clock()
-            b_ske = _apply(S, bd, prec)
             R, z_ske = _qr_presolve(A_ske, b_ske, n, d, sd, prec)
             M = K.trtri_upper(R, mode=prec)
             log.time_factor = clock() - tic

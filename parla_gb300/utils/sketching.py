@@ -90,6 +90,41 @@ class GaussianOperator(DenseOperator):
         super().__init__(K.gaussian_fill(n_rows, n_cols, seed, scale, dtype))
 
 
+class GridGaussianOperator(DenseOperator):
+    """Gaussian operator on a grid: scale * N(0, 1) rounded to the nearest
+    multiple of scale/4 (clipped at +-31 scale/4), from the device Philox
+    stream keyed by `seed`.
+
+    The draws are those of ``GaussianOperator(n_rows, n_cols, seed, scale)``
+    before rounding; the rounded distribution is symmetric, bounded and has
+    variance (1 + 1/192) scale^2, a subgaussian embedding like the Gaussian
+    it rounds.  Held as bf16 integers (``S_int``), it is applied to binary64
+    data by the exact sliced tensor-core product (``sliced_left``); ``S``, the
+    binary64 matrix, is made on first use for the other products.
+    """
+
+    def __init__(self, n_rows, n_cols, seed, scale):
+        self.seed, self.scale = seed, scale
+        self.unit = 0.25 * scale
+        self.shape = (n_rows, n_cols)
+        self.S_int = K.gaussian_grid_bf16(n_rows, n_cols, seed)
+        self._S = None
+
+    @property
+    def S(self):
+        if self._S is None:
+            self._S = (self.S_int.to(torch.float64) * self.unit).contiguous()
+        return self._S
+
+    def sliced_ok(self, X):
+        return X.dtype == torch.float64 and K.sliced_digits(self.shape[1])[0] > 0
+
+    def sliced_left(self, X, b=None):
+        """(S X, S b) with binary64 X (m x n) and b (m,) or None, exact up to
+        a 2^-49 column-relative expansion of the operands."""
+        return K.sketch_sliced(self.S_int, self.unit, X, b)
+
+
 class SJLTOperator(DeviceOperator):
     """Sparse sign embedding given by a wide pattern (k x n, nnz per column).
 
@@ -160,13 +195,18 @@ class SRCTOperator(DeviceOperator):
 def gaussian_operator(n_rows, n_cols, rng, normalize=True, seed_compat=False, dtype=torch.float64):
     """Gaussian sketch, entries N(0, 1/min(n_rows, n_cols)) when normalize.
 
-    Mirrors ``parla/utils/sketching.py:20-31``.
+    Mirrors ``parla/utils/sketching.py:20-31``.  ``seed_compat`` draws the
+    reference's NumPy Gaussian; otherwise the draws are made on the device,
+    and a binary64 operator is the grid Gaussian (``GridGaussianOperator``)
+    whose products with binary64 data run exactly on the tensor cores.
     """
     scale = float(np.sqrt(1.0 / min(n_rows, n_cols))) if normalize else 1.0
     if seed_compat:
         gen = np.random.default_rng(rng)
         S = gen.normal(0.0, scale, (n_rows, n_cols)) if normalize else gen.standard_normal((n_rows, n_cols))
         return DenseOperator(K.to_dev(S, dtype))
+    if dtype == torch.float64:
+        return GridGaussianOperator(n_rows, n_cols, _seed_from(rng), scale)
     return GaussianOperator(n_rows, n_cols, _seed_from(rng), scale, dtype)
 
 

@@ -54,3 +54,18 @@ def test_argument_errors_need_no_gpu(lib):
                             None, None, None) == 1
     assert _lib.call_status("rla_sjlt_pattern", 4, 10, 8, 1, None, None, None) == 1  # nnz > d
     assert _lib.call_status("rla_trtri_upper", 0, 3, None, 3, None, 3, None) == 1
+
+
+def test_sliced_digit_plan_needs_no_gpu(lib):
+    """Digit width q (31 * 2^q * m <= 2^24, q <= 8) and count T = ceil(48 / q)
+    of the exact sliced sketch; too deep a sum is refused."""
+    import ctypes as C
+    q, T = C.c_int(-1), C.c_int(-1)
+    for m, want in ((1, (8, 6)), (2114, (8, 6)), (2115, (7, 7)), (20000, (4, 12)), (33825, (4, 12)),
+                    (33826, (3, 16)), (65536, (3, 16)), (270600, (1, 48)), (270601, (0, 0))):
+        assert _lib.call_status("rla_sketch_sliced_digits", m, C.byref(q), C.byref(T)) == 0
+        assert (q.value, T.value) == want, (m, q.value, T.value)
+        if want[0]:
+            assert 31 * 2 ** want[0] * m <= 2 ** 24 and (want[0] == 8 or 31 * 2 ** (want[0] + 1) * m > 2 ** 24)
+    assert _lib.call_status("rla_sketch_sliced", 4, 270601, 2, None, 270608, 1.0, None, 2, None, None, 2, None,
+                            None, C.byref(C.c_size_t(0)), None) == 6

@@ -68,6 +68,32 @@ def test_syrk_symmetric_gram(K, mode, tol, trans, n, k):
         assert np.array_equal(G, G.T)
 
 
+@pytest.mark.parametrize("mode,tol", [("f64", 1e-13), ("df", 1e-12), ("f32", 2e-5)])
+@pytest.mark.parametrize("ta,tb", [(False, False), (True, False), (False, True), (True, True)])
+@pytest.mark.parametrize("shape", [(800, 1, 20000), (20000, 1, 200), (1, 300, 5000), (1, 1, 1000), (7, 1, 3),
+                                   (1, 2000, 64), (3000, 1, 70000)])
+def test_gemv(K, mode, tol, ta, tb, shape):
+    """Products with one output row or column take the matrix-vector kernels
+    (warp per output along rows, thread per output down columns; split K
+    summed in a fixed order), with alpha and beta applied."""
+    M, N, Kd = shape
+    rng = np.random.default_rng(M + 3 * N + Kd)
+    A = rng.standard_normal((Kd, M) if ta else (M, Kd))
+    B = rng.standard_normal((N, Kd) if tb else (Kd, N))
+    C0 = rng.standard_normal((M, N))
+    dt = torch.float32 if mode == "f32" else torch.float64
+    if mode == "f32":
+        A, B, C0 = (x.astype(np.float32).astype(np.float64) for x in (A, B, C0))
+    ref = 1.5 * ((A.T if ta else A) @ (B.T if tb else B)) - 0.25 * C0
+    out = dev(C0, dt)
+    K.gemm(dev(A, dt), dev(B, dt), transa=ta, transb=tb, alpha=1.5, beta=-0.25, out=out, mode=mode)
+    scale = np.sqrt(Kd) if mode == "f32" else 1.0
+    assert rel(out.cpu().numpy(), ref) <= tol * scale
+    again = dev(C0, dt)
+    K.gemm(dev(A, dt), dev(B, dt), transa=ta, transb=tb, alpha=1.5, beta=-0.25, out=again, mode=mode)
+    assert torch.equal(out, again)  # deterministic
+
+
 def test_gemm_alpha_beta(K):
     rng = np.random.default_rng(3)
     A, B, Cm = rng.standard_normal((50, 40)), rng.standard_normal((40, 30)), rng.standard_normal((50, 30))
@@ -230,6 +256,31 @@ def test_srct_apply(K, mode, d, m, n):
     ref = osk.apply_srct(r, e, A, perm)
     Y = K.srct_apply(dev(r), dev(e), dev(perm), dev(A), mode).cpu().numpy()
     assert rel(Y, ref) <= 1e-12
+
+
+@pytest.mark.parametrize("mode", ["f64", "df"])
+@pytest.mark.parametrize("m,n", [(800, 200), (50, 50), (300, 7), (17, 16), (600, 550), (2000, 200), (3000, 300)])
+def test_geqrf_cluster_matches_grid(K, mode, m, n):
+    """The one-cluster QR (matrix in distributed shared memory; the largest
+    shape does not fit and takes the grid form) and the cooperative
+    grid form (forced by a CTA cap below the cluster size), each against
+    LAPACK: R and Q^T b, and Q from the reflectors reproduces A."""
+    rng = np.random.default_rng(m + n)
+    A = rng.standard_normal((m, n)) @ np.diag(np.logspace(0, -8, n))
+    b = rng.standard_normal((m, 2))
+    Qref, Rref = la.qr(A, mode="economic")
+    for cap in (0, 8):
+        T = dev(np.vstack([A.T, b.T]))
+        tau = K.geqrf_colmajor(T, n, mode) if cap == 0 else K.geqrf_colmajor_async(T, n, mode, max_ctas=cap)
+        torch.cuda.synchronize()
+        R = np.triu(T[:n, :n].cpu().numpy().T)
+        assert rel(np.abs(R), np.abs(Rref)) <= 1e-10, cap
+        z = T[n:, :n].cpu().numpy().T
+        assert rel(np.abs(z), np.abs(Qref.T @ b)) <= 1e-10, cap
+        if cap == 0:
+            Q = K.orgqr_colmajor(T, n, tau, mode).cpu().numpy().T
+            assert np.max(np.abs(Q.T @ Q - np.eye(n))) <= 1e-12 * max(1.0, n / 200)
+            assert rel(Q @ R, A) <= 1e-12 * max(1.0, n / 200)
 
 
 @pytest.mark.parametrize("mode", ["f64", "df"])

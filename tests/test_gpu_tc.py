@@ -1,7 +1,9 @@
 """tcgen05 tensor-core GEMM (rla_gemm_bf16_tc) against a float64 product of
 the same bf16-rounded operands.  FP32 accumulation: tolerance 2e-6 * sqrt(K)
 relative to the largest entry.  The shapes include ones whose row tiles are
-shortened below 128 rows to fill the SMs (every output row is checked).
+shortened below 128 rows to fill the SMs (every output row is checked) and
+tile widths whose stage pipeline uses the most shared memory (N = 192: five
+stages of 40 KB).
 """
 import numpy as np
 import pytest
@@ -24,7 +26,8 @@ def _ref(X, W):
 
 @pytest.mark.parametrize("M,N,Kd", [(128, 64, 64), (256, 64, 128), (300, 210, 1000), (1000, 16, 64),
                                     (129, 300, 520), (512, 256, 4096), (64, 48, 8192),
-                                    (5000, 210, 512), (16384, 210, 256), (9001, 100, 640)])
+                                    (5000, 210, 512), (16384, 210, 256), (9001, 100, 640), (3, 192, 2000),
+                                    (200, 176, 512)])
 @pytest.mark.parametrize("out_trans", [False, True])
 def test_gemm_tc_matches_fp64(K, M, N, Kd, out_trans):
     g = torch.Generator(device="cuda").manual_seed(M + N + Kd)
