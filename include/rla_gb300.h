@@ -65,15 +65,19 @@ int rla_abi_version(void);
 int rla_gaussian_fill(int dtype, int64_t rows, int64_t cols, uint64_t seed,
                       double scale, void* S, int64_t lds, rla_stream_t stream);
 
-/* Grid Gaussian operator: S[i*lds+j] = clip(rint(4 z_ij), -31, 31) as bf16,
- * z_ij the N(0,1) draw rla_gaussian_fill makes for the same (seed, i, j), so
- * the operator unit * S (unit = scale / 4) is the Gaussian of that call
- * rounded to the nearest multiple of scale / 4.  Columns cols..lds-1 are set
- * to zero (lds a multiple of 8 for rla_sketch_sliced).  The device-drawn
- * binary64 gaussian_operator (parla/utils/sketching.py:20-31) of the
- * least-squares drivers; its products are exact through rla_sketch_sliced. */
-int rla_gaussian_grid_bf16(int64_t rows, int64_t cols, uint64_t seed, void* S,
-                           int64_t lds, rla_stream_t stream);
+/* Grid Gaussian operator: S[i*lds+j] = unit * clip(rint(4 z_ij), -31, 31),
+ * z_ij the N(0,1) draw rla_gaussian_fill makes for the same (seed, i, j):
+ * with unit = scale / 4 the Gaussian of that call rounded to the nearest
+ * multiple of scale / 4.  dtype RLA_BF16 (with unit = 1: the integers
+ * |s| <= 31 that rla_sketch_sliced takes; lds a multiple of 8), RLA_F32 or
+ * RLA_F64.  Columns cols..lds-1 are set to zero.  When seed_dev is not NULL
+ * the seed is read from that device word when the kernel runs (graph
+ * replays with a new sketch).  The device-drawn binary64 gaussian_operator
+ * (parla/utils/sketching.py:20-31); its products with binary64 data are
+ * exact through rla_sketch_sliced. */
+int rla_gaussian_grid(int dtype, int64_t rows, int64_t cols, uint64_t seed,
+                      const uint64_t* seed_dev, double unit, void* S,
+                      int64_t lds, rla_stream_t stream);
 
 /* Exact sliced sketch on the tensor cores: Y (d x n, binary64) = unit * S X
  * and, when b != NULL, yb (d) = unit * S b, for S (d x m, bf16 integers of

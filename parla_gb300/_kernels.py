@@ -37,11 +37,25 @@ class _Stats:
 STATS = _Stats()
 
 
+def _event():
+    """A timing event; inside a graph capture an external one, whose record
+    node stamps the time on every replay (None where torch has no external
+    events: the call is then not timed)."""
+    if torch.cuda.is_current_stream_capturing():
+        try:
+            return torch.cuda.Event(enable_timing=True, external=True)
+        except TypeError:
+            return None
+    return torch.cuda.Event(enable_timing=True)
+
+
 def _timed(name, n_launch, fn, *args):
     STATS.launches += n_launch
     if not STATS.timing:
         return fn(*args)
-    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s, e = _event(), _event()
+    if s is None or e is None:
+        return fn(*args)
     s.record()
     out = fn(*args)
     e.record()
@@ -184,12 +198,23 @@ def gaussian_fill(rows, cols, seed, scale, dtype=torch.float64):
     return S
 
 
-def gaussian_grid_bf16(rows, cols, seed):
-    """Grid Gaussian (bf16 integers |s| <= 31; the operator is scale/4 times
-    this) as a (rows, cols) view with a row stride that is a multiple of 8."""
-    S = empty_bf16(rows, cols, device())
-    _timed("gaussian_grid", 1, call, "rla_gaussian_grid_bf16", rows, cols, C.c_uint64(seed), ptr(S), S.stride(0),
-           stream())
+def gaussian_grid(rows, cols, seed, unit=1.0, dtype=torch.bfloat16):
+    """Grid Gaussian unit * clip(rint(4 z), -31, 31) (``rla_gaussian_grid``).
+
+    bf16 output is a (rows, cols) view whose row stride is a multiple of 8;
+    ``seed`` is an int, or a one-element int64 device tensor holding the seed
+    bits (read when the kernel runs: a captured graph draws a new sketch per
+    replay)."""
+    if dtype == torch.bfloat16:
+        S = empty_bf16(rows, cols, device())
+    else:
+        S = torch.empty((rows, cols), dtype=dtype, device=device())
+    if isinstance(seed, torch.Tensor):
+        sv, sd = C.c_uint64(0), ptr(seed)
+    else:
+        sv, sd = C.c_uint64(seed), None
+    _timed("gaussian_grid", 1, call, "rla_gaussian_grid", _TORCH_CODE[dtype], rows, cols, sv, sd, float(unit), ptr(S),
+           S.stride(0), stream())
     return S
 
 

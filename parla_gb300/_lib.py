@@ -46,7 +46,7 @@ SIGNATURES = {
     "rla_abi_version": [],
     "rla_gaussian_fill": [_i32, _i64, _i64, _u64, _f64, _p, _i64, _p],
     "rla_sjlt_pattern": [_i64, _i64, _i32, _u64, _p, _p, _p],
-    "rla_gaussian_grid_bf16": [_i64, _i64, _u64, _p, _i64, _p],
+    "rla_gaussian_grid": [_i32, _i64, _i64, _u64, _p, _f64, _p, _i64, _p],
     "rla_sketch_sliced": [_i64, _i64, _i64, _p, _i64, _f64, _p, _i64, _p, _p, _i64, _p, _p, _psz, _p],
     "rla_sketch_sliced_digits": [_i64, C.POINTER(C.c_int), C.POINTER(C.c_int)],
     "rla_sjlt_apply": [_i32, _i64, _i64, _i64, _i32, _p, _p, _f64, _p, _i64, _p, _i64, _p, _psz, _p],

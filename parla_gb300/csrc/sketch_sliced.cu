@@ -75,9 +75,21 @@ __host__ inline SlicedPlan sliced_plan(int64_t d, int64_t m, int64_t n, bool wit
 }
 
 // Grid Gaussian: element (i, j) is lane e % 4 of Philox block e / 4 with
-// e = i * cols + j, the mapping of the Gaussian fill, rounded to 1/4 units.
-__global__ void grid_gaussian_kernel(int64_t rows, int64_t cols, uint64_t seed, __nv_bfloat16* __restrict__ S,
-                                     int64_t lds) {
+// e = i * cols + j, the mapping of the Gaussian fill, rounded to 1/4 units
+// and scaled by `unit`.  The seed is read from device memory when seed_dev is
+// given (a captured graph replays with the seed its host writes there).
+template <typename T>
+__device__ __forceinline__ T grid_value(float v, double unit);
+template <> __device__ __forceinline__ __nv_bfloat16 grid_value(float v, double unit) {
+  return __float2bfloat16_rn(static_cast<float>(unit) * v);
+}
+template <> __device__ __forceinline__ float grid_value(float v, double unit) { return static_cast<float>(unit * v); }
+template <> __device__ __forceinline__ double grid_value(float v, double unit) { return unit * v; }
+
+template <typename T>
+__global__ void grid_gaussian_kernel(int64_t rows, int64_t cols, uint64_t seed_arg, const uint64_t* __restrict__ seed_dev,
+                                     double unit, T* __restrict__ S, int64_t lds) {
+  const uint64_t seed = seed_dev != nullptr ? *seed_dev : seed_arg;
   const int64_t total = rows * cols, nblk = ceil_div(total, 4);
   const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
   for (int64_t q = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; q < nblk; q += stride) {
@@ -88,13 +100,13 @@ __global__ void grid_gaussian_kernel(int64_t rows, int64_t cols, uint64_t seed, 
       const int64_t e = q * 4 + t;
       if (e < total) {
         const float v = fminf(fmaxf(rintf(4.f * zz[t]), -static_cast<float>(kGridMax)), static_cast<float>(kGridMax));
-        S[(e / cols) * lds + e % cols] = __float2bfloat16_rn(v);
+        S[(e / cols) * lds + e % cols] = grid_value<T>(v, unit);
       }
     }
   }
   const int64_t pad = lds - cols, ptot = rows * pad;  // zero the row padding
   for (int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; e < ptot; e += stride)
-    S[(e / pad) * lds + cols + e % pad] = __float2bfloat16_rn(0.f);
+    S[(e / pad) * lds + cols + e % pad] = grid_value<T>(0.f, unit);
 }
 
 // Column maxima of |[X | b]| as the bit patterns of non-negative binary64
@@ -217,15 +229,23 @@ __global__ void combine_kernel(int64_t d, int64_t n, int with_b, const float* __
 
 using namespace rla;
 
-extern "C" int rla_gaussian_grid_bf16(int64_t rows, int64_t cols, uint64_t seed, void* S, int64_t lds,
-                                      rla_stream_t stream) {
+extern "C" int rla_gaussian_grid(int dtype, int64_t rows, int64_t cols, uint64_t seed, const uint64_t* seed_dev,
+                                 double unit, void* S, int64_t lds, rla_stream_t stream) {
   if (rows < 0 || cols < 0 || lds < cols) return RLA_ERR_ARG;
+  if (dtype != RLA_BF16 && dtype != RLA_F32 && dtype != RLA_F64) return RLA_ERR_ARG;
   if (rows == 0 || lds == 0) return RLA_OK;
   if (!S) return RLA_ERR_ARG;
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   const int64_t work = imax(ceil_div(rows * cols, 4), rows * (lds - cols));
   const unsigned blocks = static_cast<unsigned>(imax(1, imin(ceil_div(work, 256), 32LL * sm_count())));
-  grid_gaussian_kernel<<<blocks, 256, 0, st>>>(rows, cols, seed, static_cast<__nv_bfloat16*>(S), lds);
+  if (dtype == RLA_BF16)
+    grid_gaussian_kernel<__nv_bfloat16><<<blocks, 256, 0, st>>>(rows, cols, seed, seed_dev, unit,
+                                                                static_cast<__nv_bfloat16*>(S), lds);
+  else if (dtype == RLA_F32)
+    grid_gaussian_kernel<float><<<blocks, 256, 0, st>>>(rows, cols, seed, seed_dev, unit, static_cast<float*>(S), lds);
+  else
+    grid_gaussian_kernel<double><<<blocks, 256, 0, st>>>(rows, cols, seed, seed_dev, unit, static_cast<double*>(S),
+                                                         lds);
   RLA_LAUNCH_CHECK();
   return RLA_OK;
 }

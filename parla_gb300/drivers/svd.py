@@ -37,20 +37,91 @@ class SVD1(SVDecomposer):
             rng.bit_generator.state = state  # redo on the guarded path
         return self._run(A, Am, k, tol, over, rng)
 
-    def _run(self, A, Am, k, tol, over, rng):
+    def _run(self, A, Am, k, tol, over, rng, graph=False):
         Q, B = self.qb(Am, k + over, tol, rng)
         Ub, s, Vh = law.small_svd_wide(B)
         if over > 0:
             c = min(k, s.numel())
             Ub, s, Vh = Ub[:, :c], s[:c], Vh[:c]
-        keep = ~(s < 10 * np.finfo(float).eps)
-        if not bool(torch.all(keep)):
-            Ub, s, Vh = Ub[:, keep], s[keep], Vh[keep]
+        if not graph:  # (a captured call checks this after the replay)
+            keep = ~(s < 10 * np.finfo(float).eps)
+            if not bool(torch.all(keep)):
+                Ub, s, Vh = Ub[:, keep], s[keep], Vh[keep]
         Qt = opd.panel_t(Q)
         Ut = K.gemm(Ub.to(Qt.dtype).contiguous(), Qt, transa=True)   # (Q Ub)^T
         U = Ut.t()
         out_dtype = Qt.dtype
         res = (U, s.to(out_dtype), Vh.to(out_dtype).contiguous())
-        if isinstance(A, opd.DeviceMatrix) or (isinstance(A, torch.Tensor) and A.is_cuda):
+        if graph or isinstance(A, opd.DeviceMatrix) or (isinstance(A, torch.Tensor) and A.is_cuda):
             return res
         return tuple(K.like_input(r, A) for r in res)
+
+    def capture(self, A, k, tol, over, rng, warm=True):
+        """One call captured as a CUDA graph (``SVDReplay``); tensor-core chain
+        only.  ``warm``: run the call eagerly once first (set False when the
+        caller has already made an eager call with these shapes)."""
+        return SVDReplay(self, A, k, tol, over, rng, warm)
+
+
+class SVDReplay:
+    """An SVD1 call on the bf16 tensor-core chain captured as one CUDA graph.
+
+    ``replay(rng=None)`` (or calling the object) recomputes
+    ``SVD1(A, k, tol, over, rng)`` for the current contents of A: every kernel
+    of the call runs again (the bf16 images of A, each pass, each stabilizer,
+    the small SVD, U = Q Ub), drawing the sketch an eager call with `rng`
+    would draw (the capture's `rng` when None), in one graph launch instead
+    of about sixty.  A may be a device tensor or a pinned binary32 host tensor
+    (read over the host link by the conversion kernel).  One synchronisation
+    per replay reads the deferred pivot flags and checks that no singular
+    value fell below 10 eps; if either fails, the call is repeated eagerly
+    (guarded path, data-dependent truncation) and its results returned.  The
+    returned tensors are the graph's outputs and are overwritten by the next
+    replay; for a host A they are pinned host tensors the graph fills.
+    """
+
+    def __init__(self, svd, A, k, tol, over, rng, warm=True):
+        from ..utils import sketching as usk
+        self.svd, self.A, self.args = svd, A, (k, tol, over)
+        self.rng = rng
+        if not opd.wrap(A, svd.precision).tc:
+            raise NotImplementedError("graph capture is provided for the bf16 tensor-core chain")
+        self.host = not (isinstance(A, torch.Tensor) and A.is_cuda)
+        if warm:
+            svd(A, k, tol, over, rng)                   # warm-up: attributes, maps, allocator
+        torch.cuda.synchronize()
+        # host outputs (U m x k, s, Vh k x n) are allocated before the capture
+        m, n = A.shape
+        hout = tuple(torch.empty(sh, dtype=torch.float32).pin_memory() for sh in ((m, k), (k,), (k, n))) \
+            if self.host else None
+        self.slots = usk.SeedSlots()
+        self.graph = torch.cuda.CUDAGraph()
+        eps10 = 10 * np.finfo(float).eps
+        with opd.deferred_checks() as chk, usk.recording(self.slots):
+            with torch.cuda.graph(self.graph):
+                gen = np.random.default_rng(rng)
+                Am = opd.wrap(A, svd.precision)         # inside: the bf16 images are part of the graph
+                U, s, Vh = svd._run(A, Am, k, tol, over, gen, graph=True)
+                bad = (s < eps10).any()
+                for f in chk.flags:
+                    bad = bad | (f != 0).any()
+                self.bad = bad.to(torch.int32).reshape(1)
+                if self.host:
+                    self.out = hout
+                    for h, t in zip(self.out, (U, s, Vh)):
+                        h.copy_(t, non_blocking=True)
+                else:
+                    self.out = (U, s, Vh)
+        self.bad_host = torch.zeros(1, dtype=torch.int32).pin_memory()
+
+    def replay(self, rng=None):
+        self.slots.set_from(self.rng if rng is None else rng)
+        self.graph.replay()
+        self.bad_host.copy_(self.bad, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+        if int(self.bad_host[0]):
+            k, tol, over = self.args
+            return self.svd(self.A, k, tol, over, self.rng if rng is None else rng)
+        return self.out
+
+    __call__ = replay

@@ -15,6 +15,7 @@ Two ways to draw the randomness:
 * ``seed_compat=False`` (default) takes one 64-bit seed from ``rng`` and
   draws on the device (Philox4x32-10): no host work and no PCIe traffic.
 """
+import threading
 import warnings
 
 import numpy as np
@@ -22,9 +23,61 @@ import torch
 
 from .. import _kernels as K
 
+_tls = threading.local()
+
+
+class SeedSlots:
+    """Device seed words for a captured CUDA graph.
+
+    While ``recording(slots)`` is active, every device draw of a seed still
+    consumes the caller's Generator exactly as an eager call does, but hands
+    the operator a one-word device tensor instead of the integer; the graph
+    captures a copy into that word from a pinned host word, so a replay draws
+    the sketch of whatever seed the host wrote there (``set_from``).  Slots
+    are allocated up front: nothing is allocated on the host while capturing.
+    """
+
+    def __init__(self, count=4):
+        self.host = [torch.zeros(1, dtype=torch.int64).pin_memory() for _ in range(count)]
+        self.dev = [torch.zeros(1, dtype=torch.int64, device=K.device()) for _ in range(count)]
+        self.used = 0
+
+    def take(self, seed):
+        if self.used >= len(self.host):
+            raise RuntimeError("more seed draws than SeedSlots were allocated for the capture")
+        h, d = self.host[self.used], self.dev[self.used]
+        self.used += 1
+        h[0] = seed - (1 << 64) if seed >= (1 << 63) else seed
+        d.copy_(h, non_blocking=True)
+        return d
+
+    def set_from(self, rng):
+        """Write the seeds an eager call with `rng` would draw, in order."""
+        gen = np.random.default_rng(rng)
+        for h in self.host[:self.used]:
+            h[0] = int(gen.integers(0, 2 ** 63 - 1))
+
+
+class recording:
+    """Context manager: device seed draws of this thread go through `slots`."""
+
+    def __init__(self, slots):
+        self.slots = slots
+
+    def __enter__(self):
+        self.prev = getattr(_tls, "slots", None)
+        _tls.slots = self.slots
+        return self.slots
+
+    def __exit__(self, *exc):
+        _tls.slots = self.prev
+        return False
+
 
 def _seed_from(rng):
-    return int(np.random.default_rng(rng).integers(0, 2 ** 63 - 1))
+    seed = int(np.random.default_rng(rng).integers(0, 2 ** 63 - 1))
+    slots = getattr(_tls, "slots", None)
+    return seed if slots is None else slots.take(seed)
 
 
 class DeviceOperator:
@@ -86,6 +139,8 @@ class GaussianOperator(DenseOperator):
     """N(0, scale^2) entries from the device Philox stream keyed by `seed`."""
 
     def __init__(self, n_rows, n_cols, seed, scale, dtype=torch.float64):
+        if isinstance(seed, torch.Tensor):
+            raise NotImplementedError("graph capture draws the binary64 device Gaussian (the grid operator) only")
         self.seed, self.scale = seed, scale
         super().__init__(K.gaussian_fill(n_rows, n_cols, seed, scale, dtype))
 
@@ -107,14 +162,26 @@ class GridGaussianOperator(DenseOperator):
         self.seed, self.scale = seed, scale
         self.unit = 0.25 * scale
         self.shape = (n_rows, n_cols)
-        self.S_int = K.gaussian_grid_bf16(n_rows, n_cols, seed)
+        self._S_int = None
         self._S = None
+
+    @property
+    def S_int(self):
+        if self._S_int is None:
+            self._S_int = K.gaussian_grid(self.shape[0], self.shape[1], self.seed)
+        return self._S_int
 
     @property
     def S(self):
         if self._S is None:
-            self._S = (self.S_int.to(torch.float64) * self.unit).contiguous()
+            self._S = self.dense_matrix(torch.float64)
         return self._S
+
+    def dense_matrix(self, dtype=torch.float64):
+        """The operator in `dtype` (redrawn from the seed, no conversion pass)."""
+        if dtype == torch.float64 and self._S is not None:
+            return self._S
+        return K.gaussian_grid(self.shape[0], self.shape[1], self.seed, self.unit, dtype)
 
     def sliced_ok(self, X):
         return X.dtype == torch.float64 and K.sliced_digits(self.shape[1])[0] > 0
@@ -238,7 +305,10 @@ def sjlt_operator(n_rows, n_cols, rng, vec_nnz=8, seed_compat=False):
         signs_d = K.to_dev(signs, torch.int8)
     else:
         nnz = min(n, vec_nnz)
-        rows_d, signs_d = K.sjlt_pattern(k, n, nnz, _seed_from(gen))
+        seed = _seed_from(gen)
+        if isinstance(seed, torch.Tensor):
+            raise NotImplementedError("graph capture draws the binary64 device Gaussian (the grid operator) only")
+        rows_d, signs_d = K.sjlt_pattern(k, n, nnz, seed)
     return SJLTOperator(rows_d, signs_d, nnz, k, n, tall=tall)
 
 

@@ -1,5 +1,5 @@
 """The exact sliced sketch on the tensor cores (``rla_sketch_sliced``) and the
-grid Gaussian operator (``rla_gaussian_grid_bf16``).
+grid Gaussian operator (``rla_gaussian_grid``).
 
 - The grid Gaussian is the device Gaussian of the same seed rounded to
   quarters, bit for bit, with zero row padding.
@@ -47,13 +47,21 @@ def _full(S):
 @pytest.mark.parametrize("rows,cols", [(37, 101), (300, 1001), (8, 8)])
 def test_grid_gaussian_is_rounded_fill(K, rows, cols):
     seed = 4242 + rows
-    S = K.gaussian_grid_bf16(rows, cols, seed)
+    S = K.gaussian_grid(rows, cols, seed)
     z = K.gaussian_fill(rows, cols, seed, 1.0, torch.float32).cpu().numpy()
     ref = np.clip(np.rint(4.0 * z), -31, 31)
     got = S.to(torch.float32).cpu().numpy()
     assert np.array_equal(got, ref)
     pad = _full(S)[:, cols:].to(torch.float32).cpu().numpy()
     assert not pad.size or not pad.any()
+    unit = 0.3                                     # scaled in binary64, then rounded to the output type
+    ref64 = unit * ref.astype(np.float64)
+    S64 = K.gaussian_grid(rows, cols, seed, unit, torch.float64).cpu().numpy()
+    assert np.array_equal(S64, ref64)
+    S32 = K.gaussian_grid(rows, cols, seed, unit, torch.float32).cpu().numpy()
+    assert np.array_equal(S32, ref64.astype(np.float32))
+    sd = torch.tensor([seed], dtype=torch.int64, device="cuda")      # seed read from device memory
+    assert torch.equal(K.gaussian_grid(rows, cols, sd), S)
 
 
 def _bound(Si, unit, X, b):
@@ -78,7 +86,7 @@ def test_sketch_sliced_matches_exact_operator(K, d, m, n, with_b):
         X[:, 2] *= 2.0 ** -1070                          # subnormal column
         X[:, 3] = np.where(rng.random(m) < 0.01, 1e200, 1e-200) * rng.standard_normal(m)  # wide range
     b = rng.standard_normal(m) * 1e5 if with_b else None
-    S = K.gaussian_grid_bf16(d, m, 77 + d)
+    S = K.gaussian_grid(d, m, 77 + d)
     unit = 0.25 / np.sqrt(d)
     Xd = torch.from_numpy(X).cuda() if n else None
     bd = torch.from_numpy(b).cuda() if with_b else None
@@ -101,7 +109,7 @@ def test_sketch_sliced_nonfinite_column(K):
     X = rng.standard_normal((500, 4))
     X[17, 2] = np.nan
     X[3, 0] = np.inf
-    S = K.gaussian_grid_bf16(9, 500, 1)
+    S = K.gaussian_grid(9, 500, 1)
     Y, _ = K.sketch_sliced(S, 0.1, torch.from_numpy(X).cuda())
     Y = Y.cpu().numpy()
     assert np.all(np.isnan(Y[:, [0, 2]])) and np.all(np.isfinite(Y[:, [1, 3]]))
