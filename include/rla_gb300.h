@@ -198,6 +198,20 @@ int rla_gram_f32_df(int trans, int64_t N, int64_t K, const float* A,
                     int64_t lda, double* G, int64_t ldg, void* ws,
                     size_t* ws_bytes, rla_stream_t stream);
 
+/* Y (c x M) = W^T X for a small binary32 W (l x c, row-major) and a binary32
+ * panel X (l x M, row-major); with tri != 0, W is upper triangular (c <= l;
+ * entries below the diagonal are not read and only the lower triangle of
+ * W^T is multiplied).  Yb, when not NULL, receives a bf16 copy of Y (leading
+ * dimension ldyb).  The products of the randomized SVD whose inner dimension
+ * is the sketch size: the R^-1 application of CholeskyQR on transposed
+ * panels, Q^T = R^-T Y^T (`Q = Y R^-1`, parla/utils/linalg_wrappers.py:6-7,
+ * as the stabilizer of parla/comps/sketchers/aware.py:124-184 uses it),
+ * Vh = U^T B and U = Q Ub (parla/drivers/svd.py:164-172). */
+int rla_gemm_tn_panel_f32(int tri, int64_t c, int64_t l, int64_t M,
+                          const float* W, int64_t ldw, const float* X,
+                          int64_t ldx, float* Y, int64_t ldy, void* Yb,
+                          int64_t ldyb, rla_stream_t stream);
+
 /* Tensor-core GEMM (tcgen05.mma kind::f16, TMA-fed, FP32 accumulation in
  * TMEM): D (M x N, fp32) = alpha X W^T + beta D with X (M x K) and W (N x K)
  * bf16 row-major (both K-major; ldx, ldw multiples of 8, 16-byte aligned

@@ -399,6 +399,22 @@ def chol_inv_f32(G, want_r=False, info=None):
     return (Rinv, R) if want_r else Rinv
 
 
+def gemm_tn_panel(W, X, tri=False, want_bf16=False):
+    """Y = W^T X for a small binary32 W (l x c) and a binary32 panel X (l x M)
+    (``rla_gemm_tn_panel_f32``); ``tri``: W is upper triangular.  With
+    ``want_bf16`` also a bf16 copy of Y.  Returns Y, or (Y, Yb)."""
+    l, M = X.shape
+    c = W.shape[1]
+    assert W.shape[0] == l and W.dtype == torch.float32 and X.dtype == torch.float32
+    W = W if W.stride(1) == 1 else W.contiguous()
+    X = X if X.stride(1) == 1 else X.contiguous()
+    Y = torch.empty((c, M), dtype=torch.float32, device=X.device)
+    Yb = empty_bf16(c, M, X.device) if want_bf16 else None
+    _timed("gemm_panel", 1, call, "rla_gemm_tn_panel_f32", int(tri), c, l, M, ptr(W), W.stride(0), ptr(X), X.stride(0),
+           ptr(Y), Y.stride(0), ptr(Yb), Yb.stride(0) if Yb is not None else 0, stream())
+    return (Y, Yb) if want_bf16 else Y
+
+
 def gram_f32_df(A, trans=False):
     """binary64 Gram A A^T (or A^T A with trans) of binary32 A, double-float
     accumulation (``rla_gram_f32_df``)."""

@@ -10,15 +10,17 @@
 //   diagonal block - [D | I] (16 x 32) eliminated by ALL threads, one block
 //                    barrier per pivot, in unscaled symmetric form
 //                    (a_rc -= a_kr a_kc / a_kk), rows scaled by 1/sqrt(d_r)
-//                    once at the end: D -> R_d, I -> R_d^-T.  (One warp doing
-//                    this alone while the others wait at a barrier made the
-//                    kernel barrier-bound.)
+//                    once at the end: D -> R_d, I -> R_d^-T.  (A one-warp
+//                    elimination in registers measured twice as slow per
+//                    panel: its serial shuffle/divide chain is exposed.)
 //   panel rows     - P = R_d^-T [rows jb..jb+15 of a] for the columns
-//                    outside the block, one thread per column;
+//                    outside the block, one thread per column with the 16
+//                    outputs as independent accumulators;
 //   trailing       - a_ij -= sum_k P_ki P_kj for rows i below the panel and
 //                    columns j >= i (and j < panel end for the L part), on
-//                    4 x 4 register tiles with float4 loads; the tiles of a
-//                    panel are one flat list over all threads (balanced).
+//                    4 x 4 register tiles with float4 loads and float4
+//                    read-modify-writes; the tiles of a panel are one flat
+//                    list over all threads (balanced).
 #include "common.cuh"
 
 namespace rla {
@@ -31,11 +33,14 @@ constexpr int kW2 = 2 * kNB + 1;  // row stride of the [D | I] block
 
 __host__ __device__ __forceinline__ int ci_ld(int n) { return (n + 3) & ~3; }
 
+// panel buffer: kNB rows of ld, and at least the kNB x kW2 [D | I] block
+__host__ __device__ __forceinline__ int ci_pcols(int n) { return ci_ld(n) > 36 ? ci_ld(n) : 36; }
+
 __host__ __device__ inline size_t ci_smem_bytes(int n) {
   const size_t ld = static_cast<size_t>(ci_ld(n));
-  // a (n x ld), panel rows P (kNB x ld), R_d^-T (kNB x (kNB + 1)), diag of L
-  // (n), tile-row prefix (64), [D | I] block (kNB x kW2)
-  return (static_cast<size_t>(n) * ld + kNB * ld + kNB * (kNB + 1) + n + 64 + kNB * kW2) * sizeof(float);
+  // a (n x ld), panel rows P (kNB x max(ld, 36)), R_d^-T (kNB x kNB), diag
+  // of L (n), tile-row prefix (64)
+  return (static_cast<size_t>(n) * ld + static_cast<size_t>(kNB) * ci_pcols(n) + kNB * kNB + n + 64) * sizeof(float);
 }
 
 template <bool INV>
@@ -46,10 +51,10 @@ chol_inv_kernel(int n, const float* __restrict__ G, int64_t ldg, float* __restri
   const int LD = ci_ld(n);
   float* a = smem;                   // upper: G -> R;  strictly lower: L = R^-T (INV)
   float* P = a + n * LD;             // panel rows, kNB x LD
-  float* Dv = P + kNB * LD;          // R_d^-T of the current block, kNB x (kNB + 1)
-  float* dl = Dv + kNB * (kNB + 1);  // diagonal of L
+  float* Dv = P + kNB * ci_pcols(n);  // R_d^-T of the current block, kNB x kNB (zero above the diagonal)
+  float* dl = Dv + kNB * kNB;        // diagonal of L
   int* tstart = reinterpret_cast<int*>(dl + n);
-  float* Db = dl + n + 64;           // [D | I] block, kNB x kW2
+  float* Db = P;                     // the [D | I] block (kNB x kW2) while eliminated, before P is formed
   __shared__ int s_bad;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = kCiThreads >> 5;
 
@@ -96,29 +101,37 @@ chol_inv_kernel(int n, const float* __restrict__ G, int64_t ldg, float* __restri
         const float lv = Db[r * kW2 + kNB + c] * isd;
         if (INV && c < r) a[(jb + r) * LD + jb + c] = lv;
         if (c == r) dl[jb + r] = lv;
-        Dv[r * (kNB + 1) + c] = c <= r ? lv : 0.f;
+        Dv[r * kNB + c] = c <= r ? lv : 0.f;
       } else {
-        Dv[r * (kNB + 1) + c] = 0.f;
+        Dv[r * kNB + c] = 0.f;
       }
     }
     __syncthreads();
     // ---- panel rows: P = R_d^-T [rows jb..t0 of a]: L part (c < jb) and upper part (c >= t0) ----
     for (int c = (INV ? 0 : t0) + tid; c < LD; c += kCiThreads) {
       if (c >= jb && c < t0) {
-        for (int k = 0; k < kNB; ++k) P[k * LD + c] = (k < nb) ? Dv[k * (kNB + 1) + (c - jb)] : 0.f;
+        for (int k = 0; k < kNB; ++k) P[k * LD + c] = Dv[k * kNB + (c - jb)];
         continue;
       }
       float u[kNB];
 #pragma unroll
       for (int q = 0; q < kNB; ++q) u[q] = (q < nb && c < n) ? a[(jb + q) * LD + c] : 0.f;
-#pragma unroll 1
-      for (int k = 0; k < kNB; ++k) {
-        float acc = 0.f;
-        const float* dk = Dv + k * (kNB + 1);
+      // Dv is lower triangular: output k takes q = 0..k, in that order; four
+      // outputs at a time (four independent chains)
 #pragma unroll
-        for (int q = 0; q < kNB; ++q) acc = fmaf(dk[q], u[q], acc);  // Dv is zero above the diagonal
-        P[k * LD + c] = acc;
-        if (k < nb && c < n) a[(jb + k) * LD + c] = acc;
+      for (int kb = 0; kb < kNB; kb += 4) {
+        float acc[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+        for (int q = 0; q < kb + 4; ++q)
+#pragma unroll
+          for (int t = 0; t < 4; ++t)
+            if (q <= kb + t) acc[t] = fmaf(Dv[(kb + t) * kNB + q], u[q], acc[t]);
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+          const int k = kb + t;
+          P[k * LD + c] = acc[t];
+          if (k < nb && c < n) a[(jb + k) * LD + c] = acc[t];
+        }
       }
     }
     // tile rows of 4 trailing rows: L-part tiles (columns < t0) then upper tiles
@@ -164,12 +177,19 @@ chol_inv_kernel(int n, const float* __restrict__ G, int64_t ldg, float* __restri
             for (int z = 0; z < 4; ++z) acc[q][z] = fmaf(xx[q], yy[z], acc[q][z]);
         }
 #pragma unroll
-        for (int q = 0; q < 4; ++q)
+        for (int q = 0; q < 4; ++q) {
+          const int r = r0 + q;
+          if (r >= n) continue;
+          float4* dst = reinterpret_cast<float4*>(a + r * LD + c0);  // c0 + 3 < LD, 16-byte aligned
+          float4 w = *dst;
+          float ww[4] = {w.x, w.y, w.z, w.w};
 #pragma unroll
           for (int z = 0; z < 4; ++z) {
-            const int r = r0 + q, c = c0 + z;
-            if (r < n && c < n && ((INV && c < t0) || c >= r)) a[r * LD + c] -= acc[q][z];
+            const int c = c0 + z;
+            if (c < n && ((INV && c < t0) || c >= r)) ww[z] -= acc[q][z];
           }
+          *dst = make_float4(ww[0], ww[1], ww[2], ww[3]);
+        }
       }
     }
     __syncthreads();

@@ -9,6 +9,8 @@
 // Small outputs use split-K: each z-slice writes a partial tile into the
 // workspace and a second kernel sums the slices in a fixed order, so results
 // are deterministic.
+#include <cuda_bf16.h>
+
 #include "common.cuh"
 
 namespace rla {
@@ -584,6 +586,119 @@ extern "C" int rla_gram_f32_df(int trans, int64_t N, int64_t K, const float* A, 
   else gram_f32_df_kernel<false><<<grid, kGrTh, 0, st>>>(N, K, kchunk, A, lda, part);
   RLA_LAUNCH_CHECK();
   gram_reduce_kernel<<<static_cast<unsigned>(ceil_div(N * N, 256)), 256, 0, st>>>(N, splits, part, G, ldg);
+  RLA_LAUNCH_CHECK();
+  return RLA_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Y (c x M) = W^T X for a small W (l x c, row-major) and a panel X (l x M,
+// row-major): the products of the randomized SVD whose inner dimension is
+// the sketch size l -- the R^-1 application of CholeskyQR on transposed
+// panels (Q^T = R^-T Y^T, W = R^-1 upper triangular), Vh = U^T B and
+// (Q Ub)^T = Ub^T Q^T.  A CTA computes a 64-row band of Y over a 128-column
+// strip.  With `tri` (W upper triangular, c <= l) band [i0, i0 + 64) needs
+// only k < i0 + 64, so the bands are separate CTAs with their own K length
+// (about 60 % of the multiply-adds of the full product at l = 210).  K runs
+// in chunks of 16 staged in shared memory, the next chunk prefetched into
+// registers while the current one is multiplied; each thread holds a 4 x 8
+// tile (one float4 of W^T and two of X per k).  Optionally a bf16 copy of Y
+// is stored from the same registers.
+namespace rla {
+namespace {
+constexpr int kTpBM = 64, kTpBN = 128, kTpBK = 16, kTpThreads = 256;
+
+__global__ void __launch_bounds__(kTpThreads)
+gemm_tn_panel_kernel(int tri, int cdim, int l, int64_t M, const float* __restrict__ R, int64_t ldr,
+                     const float* __restrict__ X, int64_t ldx, float* __restrict__ Y, int64_t ldy,
+                     __nv_bfloat16* __restrict__ Yb, int64_t ldyb) {
+  __shared__ __align__(16) float Ls[kTpBK][kTpBM];  // Ls[kk][i] = W[k0 + kk][i0 + i] (tri: 0 below the diagonal)
+  __shared__ __align__(16) float Xs[kTpBK][kTpBN];
+  const int tid = threadIdx.x;
+  const int ty = tid >> 4, tx = tid & 15;  // rows 4 ty .. 4 ty + 3, columns 8 tx .. 8 tx + 7 of the tile
+  const int i0 = blockIdx.y * kTpBM;
+  const int64_t j0 = static_cast<int64_t>(blockIdx.x) * kTpBN;
+  const int kend = tri ? min(l, i0 + kTpBM) : l;  // triangular W: W^T (i, k) = 0 for k > i
+  // staging assignment: Ls 16 x 64 (4 per thread), Xs 16 x 128 (8 per thread)
+  float rl[4], rx[8];
+  auto load = [&](int k0) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int e = tid + u * kTpThreads, kk = e >> 6, i = e & 63, k = k0 + kk, gi = i0 + i;
+      rl[u] = (k < kend && gi < cdim && (!tri || gi >= k)) ? R[static_cast<int64_t>(k) * ldr + gi] : 0.f;
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int e = tid + u * kTpThreads, kk = e >> 7, c = e & 127, k = k0 + kk;
+      const int64_t j = j0 + c;
+      rx[u] = (k < kend && j < M) ? X[static_cast<int64_t>(k) * ldx + j] : 0.f;
+    }
+  };
+  auto stash = [&]() {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int e = tid + u * kTpThreads;
+      Ls[e >> 6][e & 63] = rl[u];
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int e = tid + u * kTpThreads;
+      Xs[e >> 7][e & 127] = rx[u];
+    }
+  };
+  float acc[4][8];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int c = 0; c < 8; ++c) acc[a][c] = 0.f;
+  if (kend > 0) load(0);
+  for (int k0 = 0; k0 < kend; k0 += kTpBK) {
+    __syncthreads();
+    stash();
+    __syncthreads();
+    if (k0 + kTpBK < kend) load(k0 + kTpBK);
+#pragma unroll
+    for (int kk = 0; kk < kTpBK; ++kk) {
+      const float4 lv = *reinterpret_cast<const float4*>(&Ls[kk][4 * ty]);
+      const float4 x0 = *reinterpret_cast<const float4*>(&Xs[kk][8 * tx]);
+      const float4 x1 = *reinterpret_cast<const float4*>(&Xs[kk][8 * tx + 4]);
+      const float la[4] = {lv.x, lv.y, lv.z, lv.w};
+      const float xv[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int c = 0; c < 8; ++c) acc[a][c] = fmaf(la[a], xv[c], acc[a][c]);
+    }
+  }
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+    const int i = i0 + 4 * ty + a;
+    if (i >= cdim) continue;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      const int64_t j = j0 + 8 * tx + c;
+      if (j < M) {
+        Y[static_cast<int64_t>(i) * ldy + j] = acc[a][c];
+        if (Yb) Yb[static_cast<int64_t>(i) * ldyb + j] = __float2bfloat16_rn(acc[a][c]);
+      }
+    }
+  }
+}
+}  // namespace
+}  // namespace rla
+
+extern "C" int rla_gemm_tn_panel_f32(int tri, int64_t c, int64_t l, int64_t M, const float* W, int64_t ldw,
+                                     const float* X, int64_t ldx, float* Y, int64_t ldy, void* Yb, int64_t ldyb,
+                                     rla_stream_t stream) {
+  using namespace rla;
+  if (c < 0 || l < 0 || M < 0 || ldw < c || ldx < M || ldy < M || (Yb && ldyb < M) || (tri && c > l))
+    return RLA_ERR_ARG;
+  if (c > (1 << 20) || l > (1 << 20)) return RLA_ERR_UNSUPPORTED;
+  if (c == 0 || M == 0) return RLA_OK;
+  if (!Y || (l > 0 && (!W || !X))) return RLA_ERR_ARG;
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  dim3 grid(static_cast<unsigned>(ceil_div(M, kTpBN)), static_cast<unsigned>(ceil_div(c, kTpBM)));
+  gemm_tn_panel_kernel<<<grid, kTpThreads, 0, st>>>(tri ? 1 : 0, static_cast<int>(c), static_cast<int>(l), M, W, ldw,
+                                                    X, ldx, Y, ldy, static_cast<__nv_bfloat16*>(Yb), ldyb);
   RLA_LAUNCH_CHECK();
   return RLA_OK;
 }

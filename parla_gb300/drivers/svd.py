@@ -48,7 +48,10 @@ class SVD1(SVDecomposer):
             if not bool(torch.all(keep)):
                 Ub, s, Vh = Ub[:, keep], s[keep], Vh[keep]
         Qt = opd.panel_t(Q)
-        Ut = K.gemm(Ub.to(Qt.dtype).contiguous(), Qt, transa=True)   # (Q Ub)^T
+        if Qt.dtype == torch.float32:
+            Ut = K.gemm_tn_panel(Ub.to(torch.float32), Qt)             # (Q Ub)^T = Ub^T Q^T
+        else:
+            Ut = K.gemm(Ub.to(Qt.dtype).contiguous(), Qt, transa=True)
         U = Ut.t()
         out_dtype = Qt.dtype
         res = (U, s.to(out_dtype), Vh.to(out_dtype).contiguous())

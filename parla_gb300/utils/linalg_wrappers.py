@@ -151,7 +151,7 @@ def small_svd_wide(B):
         if res is not None:
             U, s = res
             inv = torch.where(s > 0, 1.0 / s, torch.zeros_like(s))
-            Vh = K.gemm(U, B, transa=True, mode="f32") * inv[:, None]
+            Vh = K.gemm_tn_panel(U, B) * inv[:, None]
             return U, s, Vh
     G = K.gram_f32_df(B) if B.dtype == torch.float32 else K.syrk(B, mode="df")
     if B.dtype == torch.float32 and B.shape[0] <= JACOBI_MAX:
@@ -243,7 +243,7 @@ def orth_tc(Y, passes=1):
         else:
             G = K.syrk(Qt, mode="f32")
         Rinv = _chol_inv_f32(G)
-        Qt = K.gemm(Rinv, Qt, transa=True, mode="f32")
+        Qt = K.gemm_tn_panel(Rinv, Qt, tri=True)
     return Qt.t()
 
 

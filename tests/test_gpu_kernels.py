@@ -94,6 +94,29 @@ def test_gemv(K, mode, tol, ta, tb, shape):
     assert torch.equal(out, again)  # deterministic
 
 
+@pytest.mark.parametrize("tri", [True, False])
+@pytest.mark.parametrize("l,c,M", [(1, 1, 5), (17, 17, 63), (210, 210, 16384), (256, 256, 1000), (100, 100, 64),
+                                   (210, 200, 8192), (300, 70, 777), (64, 130, 129)])
+def test_gemm_tn_panel(K, tri, l, c, M):
+    """Y = W^T X for a small W and a wide panel (the randomized SVD's
+    sketch-size products); with tri, W is upper triangular and the entries
+    below its diagonal are garbage that must not be read; the bf16 copy."""
+    if tri and c > l:
+        pytest.skip("a triangular W is square-topped (c <= l)")
+    rng = np.random.default_rng(l + c + M)
+    W = rng.standard_normal((l, c)).astype(np.float32)
+    if tri:
+        W = np.triu(W)
+        Wg = W + np.tril(np.full((l, c), np.nan, dtype=np.float32), -1)
+    else:
+        Wg = W
+    X = rng.standard_normal((l, M)).astype(np.float32)
+    Y, Yb = K.gemm_tn_panel(dev(Wg), dev(X), tri=tri, want_bf16=True)
+    ref = W.astype(np.float64).T @ X.astype(np.float64)
+    assert rel(Y.cpu().numpy(), ref) <= 2e-6 * np.sqrt(l)
+    assert torch.equal(Yb, Y.to(torch.bfloat16))
+
+
 def test_gemm_alpha_beta(K):
     rng = np.random.default_rng(3)
     A, B, Cm = rng.standard_normal((50, 40)), rng.standard_normal((40, 30)), rng.standard_normal((50, 30))
