@@ -202,7 +202,9 @@ int rla_gram_f32_df(int trans, int64_t N, int64_t K, const float* A,
  * panel X (l x M, row-major); with tri != 0, W is upper triangular (c <= l;
  * entries below the diagonal are not read and only the lower triangle of
  * W^T is multiplied).  Yb, when not NULL, receives a bf16 copy of Y (leading
- * dimension ldyb).  The products of the randomized SVD whose inner dimension
+ * dimension ldyb).  X and Y rows are read and written as float4: 16-byte
+ * aligned bases and ldx, ldy multiples of 4 (RLA_ERR_UNSUPPORTED otherwise).
+ * The products of the randomized SVD whose inner dimension
  * is the sketch size: the R^-1 application of CholeskyQR on transposed
  * panels, Q^T = R^-T Y^T (`Q = Y R^-1`, parla/utils/linalg_wrappers.py:6-7,
  * as the stabilizer of parla/comps/sketchers/aware.py:124-184 uses it),

@@ -402,12 +402,17 @@ def chol_inv_f32(G, want_r=False, info=None):
 def gemm_tn_panel(W, X, tri=False, want_bf16=False):
     """Y = W^T X for a small binary32 W (l x c) and a binary32 panel X (l x M)
     (``rla_gemm_tn_panel_f32``); ``tri``: W is upper triangular.  With
-    ``want_bf16`` also a bf16 copy of Y.  Returns Y, or (Y, Yb)."""
+    ``want_bf16`` also a bf16 copy of Y.  Returns Y, or (Y, Yb).  Rows of X
+    that are not 16-byte aligned (M or its stride not a multiple of 4) take
+    the general GEMM."""
     l, M = X.shape
     c = W.shape[1]
     assert W.shape[0] == l and W.dtype == torch.float32 and X.dtype == torch.float32
     W = W if W.stride(1) == 1 else W.contiguous()
     X = X if X.stride(1) == 1 else X.contiguous()
+    if M % 4 or X.stride(0) % 4 or X.data_ptr() % 16:
+        Y = gemm((torch.triu(W) if tri else W).contiguous(), X.contiguous(), transa=True, mode="f32")
+        return (Y, convert(Y, torch.bfloat16)) if want_bf16 else Y
     Y = torch.empty((c, M), dtype=torch.float32, device=X.device)
     Yb = empty_bf16(c, M, X.device) if want_bf16 else None
     _timed("gemm_panel", 1, call, "rla_gemm_tn_panel_f32", int(tri), c, l, M, ptr(W), W.stride(0), ptr(X), X.stride(0),

@@ -595,90 +595,122 @@ extern "C" int rla_gram_f32_df(int trans, int64_t N, int64_t K, const float* A, 
 // row-major): the products of the randomized SVD whose inner dimension is
 // the sketch size l -- the R^-1 application of CholeskyQR on transposed
 // panels (Q^T = R^-T Y^T, W = R^-1 upper triangular), Vh = U^T B and
-// (Q Ub)^T = Ub^T Q^T.  A CTA computes a 64-row band of Y over a 128-column
+// (Q Ub)^T = Ub^T Q^T.  A CTA computes a 64-row band of Y over a 256-column
 // strip.  With `tri` (W upper triangular, c <= l) band [i0, i0 + 64) needs
 // only k < i0 + 64, so the bands are separate CTAs with their own K length
 // (about 60 % of the multiply-adds of the full product at l = 210).  K runs
-// in chunks of 16 staged in shared memory, the next chunk prefetched into
-// registers while the current one is multiplied; each thread holds a 4 x 8
-// tile (one float4 of W^T and two of X per k).  Optionally a bf16 copy of Y
-// is stored from the same registers.
+// in chunks of 16 staged in shared memory by asynchronous copies (the next
+// chunk lands while the current one is multiplied); each thread holds an
+// 8 x 8 tile (two float4 of W^T and two of X per k, 64 multiply-adds).  X and Y
+// rows are accessed as float4 (16-byte aligned, leading dimensions multiples
+// of 4).  Optionally a bf16 copy of Y is stored from the same registers.
 namespace rla {
 namespace {
-constexpr int kTpBM = 64, kTpBN = 128, kTpBK = 16, kTpThreads = 256;
+constexpr int kTpBM = 64, kTpBN = 256, kTpBK = 16, kTpThreads = 256;
 
-__global__ void __launch_bounds__(kTpThreads)
+__device__ __forceinline__ void cp_async4(float* dst, const float* src, bool valid) {
+  const uint32_t d = static_cast<uint32_t>(__cvta_generic_to_shared(dst));
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(d), "l"(src), "r"(valid ? 4 : 0) : "memory");
+}
+__device__ __forceinline__ void cp_async16(float* dst, const float* src, bool valid) {
+  const uint32_t d = static_cast<uint32_t>(__cvta_generic_to_shared(dst));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(d), "l"(src), "r"(valid ? 16 : 0) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+// Thread (ty, tx) = (tid / 32, tid % 32): rows 8 ty .. 8 ty + 7 of the band
+// (a warp shares its rows: the W^T reads are broadcasts) and columns
+// 4 tx .. 4 tx + 3 and 128 + 4 tx .. 128 + 4 tx + 3 of the strip (a warp
+// reads 512 contiguous bytes per float4 load: no bank conflicts).  Chunks
+// are staged by cp.async into two shared-memory buffers: the copy of chunk
+// c + 1 runs while chunk c is multiplied.  Out-of-range entries (and W
+// below its diagonal when triangular) are zero-filled by the copy.
+__global__ void __launch_bounds__(kTpThreads, 2)
 gemm_tn_panel_kernel(int tri, int cdim, int l, int64_t M, const float* __restrict__ R, int64_t ldr,
                      const float* __restrict__ X, int64_t ldx, float* __restrict__ Y, int64_t ldy,
                      __nv_bfloat16* __restrict__ Yb, int64_t ldyb) {
-  __shared__ __align__(16) float Ls[kTpBK][kTpBM];  // Ls[kk][i] = W[k0 + kk][i0 + i] (tri: 0 below the diagonal)
-  __shared__ __align__(16) float Xs[kTpBK][kTpBN];
-  const int tid = threadIdx.x;
-  const int ty = tid >> 4, tx = tid & 15;  // rows 4 ty .. 4 ty + 3, columns 8 tx .. 8 tx + 7 of the tile
+  __shared__ __align__(16) float Ls[2][kTpBK][kTpBM];  // Ls[b][kk][i] = W[k0 + kk][i0 + i]
+  __shared__ __align__(16) float Xs[2][kTpBK][kTpBN];
+  const int tid = threadIdx.x, ty = tid >> 5, tx = tid & 31;
   const int i0 = blockIdx.y * kTpBM;
   const int64_t j0 = static_cast<int64_t>(blockIdx.x) * kTpBN;
   const int kend = tri ? min(l, i0 + kTpBM) : l;  // triangular W: W^T (i, k) = 0 for k > i
-  // staging assignment: Ls 16 x 64 (4 per thread), Xs 16 x 128 (8 per thread)
-  float rl[4], rx[8];
-  auto load = [&](int k0) {
+  const bool full = j0 + kTpBN <= M;               // whole float4 groups in range
+  auto issue = [&](int k0, int b) {
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       const int e = tid + u * kTpThreads, kk = e >> 6, i = e & 63, k = k0 + kk, gi = i0 + i;
-      rl[u] = (k < kend && gi < cdim && (!tri || gi >= k)) ? R[static_cast<int64_t>(k) * ldr + gi] : 0.f;
+      const bool ok = k < kend && gi < cdim && (!tri || gi >= k);
+      cp_async4(&Ls[b][kk][i], ok ? R + static_cast<int64_t>(k) * ldr + gi : R, ok);
     }
-#pragma unroll
-    for (int u = 0; u < 8; ++u) {
-      const int e = tid + u * kTpThreads, kk = e >> 7, c = e & 127, k = k0 + kk;
-      const int64_t j = j0 + c;
-      rx[u] = (k < kend && j < M) ? X[static_cast<int64_t>(k) * ldx + j] : 0.f;
-    }
-  };
-  auto stash = [&]() {
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
-      const int e = tid + u * kTpThreads;
-      Ls[e >> 6][e & 63] = rl[u];
-    }
+      const int e = tid + u * kTpThreads, kk = e >> 6, c4 = (e & 63) * 4, k = k0 + kk;
+      const int64_t j = j0 + c4;
+      if (full) {
+        const bool ok = k < kend;
+        cp_async16(&Xs[b][kk][c4], ok ? X + static_cast<int64_t>(k) * ldx + j : X, ok);
+      } else {
 #pragma unroll
-    for (int u = 0; u < 8; ++u) {
-      const int e = tid + u * kTpThreads;
-      Xs[e >> 7][e & 127] = rx[u];
+        for (int z = 0; z < 4; ++z) {
+          const bool ok = k < kend && j + z < M;
+          cp_async4(&Xs[b][kk][c4 + z], ok ? X + static_cast<int64_t>(k) * ldx + j + z : X, ok);
+        }
+      }
     }
+    cp_async_commit();
   };
-  float acc[4][8];
+  float acc[8][8];
 #pragma unroll
-  for (int a = 0; a < 4; ++a)
+  for (int a = 0; a < 8; ++a)
 #pragma unroll
     for (int c = 0; c < 8; ++c) acc[a][c] = 0.f;
-  if (kend > 0) load(0);
-  for (int k0 = 0; k0 < kend; k0 += kTpBK) {
+  if (kend > 0) issue(0, 0);
+  int b = 0;
+  for (int k0 = 0; k0 < kend; k0 += kTpBK, b ^= 1) {
+    if (k0 + kTpBK < kend) {
+      issue(k0 + kTpBK, b ^ 1);
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
     __syncthreads();
-    stash();
-    __syncthreads();
-    if (k0 + kTpBK < kend) load(k0 + kTpBK);
 #pragma unroll
     for (int kk = 0; kk < kTpBK; ++kk) {
-      const float4 lv = *reinterpret_cast<const float4*>(&Ls[kk][4 * ty]);
-      const float4 x0 = *reinterpret_cast<const float4*>(&Xs[kk][8 * tx]);
-      const float4 x1 = *reinterpret_cast<const float4*>(&Xs[kk][8 * tx + 4]);
-      const float la[4] = {lv.x, lv.y, lv.z, lv.w};
+      const float4 l0 = *reinterpret_cast<const float4*>(&Ls[b][kk][8 * ty]);
+      const float4 l1 = *reinterpret_cast<const float4*>(&Ls[b][kk][8 * ty + 4]);
+      const float4 x0 = *reinterpret_cast<const float4*>(&Xs[b][kk][4 * tx]);
+      const float4 x1 = *reinterpret_cast<const float4*>(&Xs[b][kk][128 + 4 * tx]);
+      const float la[8] = {l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, l1.z, l1.w};
       const float xv[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
 #pragma unroll
-      for (int a = 0; a < 4; ++a)
+      for (int a = 0; a < 8; ++a)
 #pragma unroll
         for (int c = 0; c < 8; ++c) acc[a][c] = fmaf(la[a], xv[c], acc[a][c]);
     }
+    __syncthreads();  // buffer b is refilled two chunks on
   }
 #pragma unroll
-  for (int a = 0; a < 4; ++a) {
-    const int i = i0 + 4 * ty + a;
+  for (int a = 0; a < 8; ++a) {
+    const int i = i0 + 8 * ty + a;
     if (i >= cdim) continue;
 #pragma unroll
-    for (int c = 0; c < 8; ++c) {
-      const int64_t j = j0 + 8 * tx + c;
-      if (j < M) {
-        Y[static_cast<int64_t>(i) * ldy + j] = acc[a][c];
-        if (Yb) Yb[static_cast<int64_t>(i) * ldyb + j] = __float2bfloat16_rn(acc[a][c]);
+    for (int h = 0; h < 2; ++h) {
+      const int64_t j = j0 + 128 * h + 4 * tx;
+      const float* v = &acc[a][4 * h];
+      if (full) {
+        *reinterpret_cast<float4*>(Y + static_cast<int64_t>(i) * ldy + j) = make_float4(v[0], v[1], v[2], v[3]);
+      } else {
+#pragma unroll
+        for (int z = 0; z < 4; ++z)
+          if (j + z < M) Y[static_cast<int64_t>(i) * ldy + j + z] = v[z];
+      }
+      if (Yb) {
+#pragma unroll
+        for (int z = 0; z < 4; ++z)
+          if (j + z < M) Yb[static_cast<int64_t>(i) * ldyb + j + z] = __float2bfloat16_rn(v[z]);
       }
     }
   }
@@ -695,6 +727,9 @@ extern "C" int rla_gemm_tn_panel_f32(int tri, int64_t c, int64_t l, int64_t M, c
   if (c > (1 << 20) || l > (1 << 20)) return RLA_ERR_UNSUPPORTED;
   if (c == 0 || M == 0) return RLA_OK;
   if (!Y || (l > 0 && (!W || !X))) return RLA_ERR_ARG;
+  // float4 rows of X and Y: 16-byte aligned bases, leading dimensions multiples of 4
+  if ((reinterpret_cast<uintptr_t>(X) & 15) || (reinterpret_cast<uintptr_t>(Y) & 15) || (ldx % 4) || (ldy % 4))
+    return RLA_ERR_UNSUPPORTED;
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   dim3 grid(static_cast<unsigned>(ceil_div(M, kTpBN)), static_cast<unsigned>(ceil_div(c, kTpBM)));
   gemm_tn_panel_kernel<<<grid, kTpThreads, 0, st>>>(tri ? 1 : 0, static_cast<int>(c), static_cast<int>(l), M, W, ldw,

@@ -95,12 +95,14 @@ def test_gemv(K, mode, tol, ta, tb, shape):
 
 
 @pytest.mark.parametrize("tri", [True, False])
-@pytest.mark.parametrize("l,c,M", [(1, 1, 5), (17, 17, 63), (210, 210, 16384), (256, 256, 1000), (100, 100, 64),
-                                   (210, 200, 8192), (300, 70, 777), (64, 130, 129)])
+@pytest.mark.parametrize("l,c,M", [(1, 1, 8), (17, 17, 64), (210, 210, 16384), (256, 256, 1000), (100, 100, 64),
+                                   (210, 200, 8192), (300, 70, 780), (64, 130, 132), (17, 17, 63), (30, 20, 777)])
 def test_gemm_tn_panel(K, tri, l, c, M):
     """Y = W^T X for a small W and a wide panel (the randomized SVD's
     sketch-size products); with tri, W is upper triangular and the entries
-    below its diagonal are garbage that must not be read; the bf16 copy."""
+    below its diagonal are garbage that must not be read; the bf16 copy.
+    Whole and partial 256-column strips; M not a multiple of 4 takes the
+    general GEMM."""
     if tri and c > l:
         pytest.skip("a triangular W is square-topped (c <= l)")
     rng = np.random.default_rng(l + c + M)
