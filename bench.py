@@ -413,6 +413,26 @@ def bench_sketch_apply(torch):
     byts = m2 * n2 * 4 + m2 * d2 * 4 + n2 * 8 * 12
     out["learned_right"] = {"shape": "A (16384 x 4096 f32) @ S^T (learned values, 74 rows)", "ms": ms,
                             "gbs": byts / ms / 1e6, "frac": byts / ms / 1e6 / hbm}
+    del A
+    # SRCT at the single-LS shape: the FFT-based DCT (gather-transpose, per-column
+    # shared-memory FFT) against the explicit 800 x 20000 operator.  Algorithmic
+    # bytes: A read once, the sketch written once, e and perm read once.
+    import numpy as _np
+    from oracle import sketching as _osk
+    m3, n3, d3 = 20000, 200, 800
+    r_, e_, p_ = _osk.generate_srct(d3, m3, _np.random.default_rng(7))
+    r_d, e_d, p_d = (torch.from_numpy(_np.asarray(x)).cuda() for x in (r_, e_, p_))
+    A = torch.randn((m3, n3), device="cuda", dtype=torch.float64)
+    byts = m3 * n3 * 8 + d3 * n3 * 8 + m3 * 16
+    for mode in ("df", "f64"):
+        ms = _event_ms(torch, lambda: K.srct_apply(r_d, e_d, p_d, A, mode))
+        out[f"srct_{mode}"] = {"shape": "S (800 x 20000 SRCT) @ A (20000 x 200 f64)", "ms": ms,
+                               "gbs": byts / ms / 1e6, "frac": byts / ms / 1e6 / hbm,
+                               "arith": "double-float" if mode == "df" else "binary64"}
+    C_ = torch.zeros((d3, m3), dtype=torch.float64, device="cuda")
+    ms = _event_ms(torch, lambda: K.gemm(C_, A, mode="df"))
+    out["srct_explicit_operator_df"] = {"ms": ms, "what": "the 800 x 20000 x 200 double-float product the "
+                                                          "explicit-operator path runs (without building it)"}
     return out
 
 

@@ -153,12 +153,28 @@ int rla_sjlt_apply_noalloc(int dtype, int64_t d, int64_t m, int64_t n, int nnz,
 
 /* SRCT: Y (d x n) = (DCT-II_ortho(diag(e) A[perm, :]))[r, :], m = rows of A.
  * r: d distinct row indices, e: m signed scales, perm: permutation of [0,m)
- * (NULL for identity).  FP64 storage; dtype RLA_F64.  Replaces apply_srct's
- * forward branch, parla/utils/sketching.py:148-161 (SkOpTC). */
+ * (NULL for identity).  FP64 storage; dtype RLA_F64 (binary64 arithmetic)
+ * or RLA_DF (double-float).  For even m whose half N = m/2 <= 12800 has no
+ * prime factor above 7, a fast transform: the columns gathered (signs,
+ * permutation) and transposed, then one CTA per column runs a length-N
+ * complex FFT in shared memory (Makhoul's reordering of the real DCT-II)
+ * and evaluates the d kept outputs; otherwise the explicit d x m operator
+ * times the gathered A.  Replaces apply_srct's forward branch,
+ * parla/utils/sketching.py:148-161 (SkOpTC). */
 int rla_srct_apply(int dtype, int64_t d, int64_t m, int64_t n, const int64_t* r,
                    const double* e, const int64_t* perm, const double* A,
                    int64_t lda, double* Y, int64_t ldy, void* ws,
                    size_t* ws_bytes, rla_stream_t stream);
+
+/* Adjoint SRCT: X (m x n) = P^T diag(e) IDCT_ortho(scatter_r(Y)) for Y
+ * (d x n) (the explicit DCT rows, a transposed product, then the signed
+ * scatter).  Replaces apply_srct's adjoint branch,
+ * parla/utils/sketching.py:162-176, which the tall operator (the transpose
+ * of the wide one, :197-200) applies from the left. */
+int rla_srct_adjoint(int dtype, int64_t d, int64_t m, int64_t n,
+                     const int64_t* r, const double* e, const int64_t* perm,
+                     const double* Y, int64_t ldy, double* X, int64_t ldx,
+                     void* ws, size_t* ws_bytes, rla_stream_t stream);
 
 /* --------------------------------------------------------------- GEMM */
 

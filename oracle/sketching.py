@@ -117,11 +117,19 @@ def apply_srct(r, e, mat, perm=None, forward=True):
 def srct_apply_dense(n_rows, n_cols, rng):
     """Return (r, e, perm, apply) for an SRCT operator of shape (n_rows, n_cols).
 
-    Mirrors ``srct_operator`` (``parla/utils/sketching.py:179-201``) for the
-    wide case used by the least-squares drivers (n_cols >= n_rows).
+    Mirrors ``srct_operator`` (``parla/utils/sketching.py:179-201``): the
+    wide operator applies the forward transform; the tall one
+    (n_cols < n_rows) is the transpose of the wide (n_cols x n_rows)
+    operator, so ``apply`` (S @ mat) runs the adjoint.
     """
     gen = np.random.default_rng(rng)
-    if n_cols < n_rows:
-        raise ValueError("oracle SRCT covers the wide (n_cols >= n_rows) case")
     r, e, perm = generate_srct(n_rows, n_cols, gen)
+    if n_cols < n_rows:
+        return r, e, perm, (lambda mat: apply_srct(r, e, mat, perm, forward=False))
     return r, e, perm, (lambda mat: apply_srct(r, e, mat, perm))
+
+
+def srct_matrix(n_rows, n_cols, rng):
+    """The SRCT operator of shape (n_rows, n_cols) as a dense matrix."""
+    *_, apply = srct_apply_dense(n_rows, n_cols, rng)
+    return apply(np.eye(n_cols))

@@ -279,6 +279,9 @@ def sjlt_apply_right(rows, signs, nnz, k, A, scale):
 
 
 def srct_apply(r, e, perm, A, mode="f64"):
+    """Y (d x n) = S A for the wide SRCT (r, e, perm) of length m = A.shape[0]
+    (``rla_srct_apply``: an FFT-based DCT for even m whose half has prime
+    factors 2, 3, 5, 7 only, up to m = 25600; the explicit operator otherwise)."""
     vec = A.dim() == 1
     A2 = A.reshape(-1, 1) if vec else A
     m, n = A2.shape
@@ -288,8 +291,22 @@ def srct_apply(r, e, perm, A, mode="f64"):
     need = size_query("rla_srct_apply", *head)
     ws = workspace(need)
     nb = C.c_size_t(need)
-    _timed("srct_apply", 4, call, "rla_srct_apply", *head, ptr(ws), C.byref(nb), stream())
+    _timed("srct_apply", 3, call, "rla_srct_apply", *head, ptr(ws), C.byref(nb), stream())
     return Y.reshape(-1) if vec else Y
+
+
+def srct_adjoint(r, e, perm, Y, m, mode="f64"):
+    """X (m x n) = S^T Y for the wide SRCT (r, e, perm) and Y (d x n) (``rla_srct_adjoint``)."""
+    vec = Y.dim() == 1
+    Y2 = Y.reshape(-1, 1) if vec else Y
+    d, n = Y2.shape
+    X = torch.empty((m, n), dtype=torch.float64, device=Y2.device)
+    head = (MODES[mode], d, m, n, ptr(r), ptr(e), ptr(perm), ptr(Y2), _ld(Y2), ptr(X), n)
+    need = size_query("rla_srct_adjoint", *head)
+    ws = workspace(need)
+    nb = C.c_size_t(need)
+    _timed("srct_adjoint", 3, call, "rla_srct_adjoint", *head, ptr(ws), C.byref(nb), stream())
+    return X.reshape(-1) if vec else X
 
 
 # ---------------------------------------------------------- factorizations

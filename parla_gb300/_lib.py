@@ -53,6 +53,7 @@ SIGNATURES = {
     "rla_sjlt_apply_noalloc": [_i32, _i64, _i64, _i64, _i32, _p, _p, _f64, _p, _i64, _p, _i64, _p],
     "rla_sjlt_apply_right": [_i32, _i64, _i64, _i64, _i32, _p, _p, _f64, _p, _i64, _p, _i64, _p],
     "rla_srct_apply": [_i32, _i64, _i64, _i64, _p, _p, _p, _p, _i64, _p, _i64, _p, _psz, _p],
+    "rla_srct_adjoint": [_i32, _i64, _i64, _i64, _p, _p, _p, _p, _i64, _p, _i64, _p, _psz, _p],
     "rla_gemm": [_i32, _i32, _i32, _i64, _i64, _i64, _f64, _p, _i64, _p, _i64, _f64, _p, _i64, _p, _psz, _p],
     "rla_syrk": [_i32, _i32, _i64, _i64, _f64, _p, _i64, _f64, _p, _i64, _p, _psz, _p],
     "rla_gram_f32_df": [_i32, _i64, _i64, _p, _i64, _p, _i64, _p, _psz, _p],

@@ -81,9 +81,13 @@ def _seed_from(rng):
 
 
 class DeviceOperator:
-    """Base class: a linear operator whose products run on the GPU."""
+    """Base class: a linear operator whose products run on the GPU.
+
+    ``ndarray @ op`` defers to ``op.__rmatmul__`` (NumPy's operators return
+    NotImplemented for an object that sets ``__array_ufunc__ = None``)."""
 
     shape = (0, 0)
+    __array_ufunc__ = None
 
     def _left(self, X):
         raise NotImplementedError
@@ -240,22 +244,57 @@ class SJLTOperator(DeviceOperator):
 
 
 class SRCTOperator(DeviceOperator):
-    """Subsampled randomized DCT-II: S X = (DCT_ortho(diag(e) X[perm]))[r]."""
+    """Subsampled randomized DCT-II (``parla/utils/sketching.py:118-201``).
 
-    def __init__(self, r, e, perm, n_rows, n_cols, mode="f64"):
+    The wide transform W (k x big, k = len(r)) is
+    W X = (DCT_ortho(diag(e) X[perm]))[r] and its adjoint
+    W^T Y = P^T diag(e) IDCT_ortho(scatter_r(Y)).  ``tall=False``: the
+    operator is W (S @ X = W X); ``tall=True``: the operator is W^T, as the
+    reference builds the tall operator as the transpose of the wide one
+    (S @ X = W^T X, X @ S = (W X^T)^T: a right sketch A @ S runs the fast
+    forward transform on A^T).
+    """
+
+    def __init__(self, r, e, perm, n_rows, n_cols, mode="f64", tall=False):
         self.r = K.to_dev(r, torch.int64)
         self.e = K.to_dev(e, torch.float64)
         self.perm = K.to_dev(perm, torch.int64) if perm is not None else None
         self.shape = (n_rows, n_cols)
         self.mode = mode
+        self.tall = tall
+        self.big = int(np.asarray(e).size)
         self.sketch_data = (r, e, perm)
 
-    def _left(self, X):
+    def _fwd(self, X):  # W X, X (big x c)
         Xd = X if X.dtype == torch.float64 else X.to(torch.float64)
-        return K.srct_apply(self.r, self.e, self.perm, Xd, self.mode)
+        return K.srct_apply(self.r, self.e, self.perm, Xd.contiguous(), self.mode)
+
+    def _adj(self, Y):  # W^T Y, Y (k x c)
+        Yd = Y if Y.dtype == torch.float64 else Y.to(torch.float64)
+        return K.srct_adjoint(self.r, self.e, self.perm, Yd.contiguous(), self.big, self.mode)
+
+    def _left(self, X):
+        return self._adj(X) if self.tall else self._fwd(X)
 
     def _right(self, X):
-        raise NotImplementedError("SRCT is applied from the left (S @ A)")
+        out = self._fwd(X.t()) if self.tall else self._adj(X.t())   # X W^T = (W X^T)^T; X W = (W^T X^T)^T
+        return out.t().to(X.dtype).contiguous()
+
+    def t_matvec(self, v):
+        """S' v: W v for the tall operator, W^T v for the wide one."""
+        return self._fwd(v) if self.tall else self._adj(v)
+
+    def dense_matrix(self, dtype=torch.float64):
+        """The operator as an explicit device matrix."""
+        k = self.r.numel()
+        if self.tall:
+            M = self._adj(torch.eye(k, dtype=torch.float64, device=K.device()))
+        else:
+            M = self._fwd(torch.eye(self.big, dtype=torch.float64, device=K.device()))
+        return M if dtype == torch.float64 else M.to(dtype)
+
+    def dense(self):
+        return self.dense_matrix()
 
 
 # ----------------------------------------------------------- constructors
@@ -323,9 +362,9 @@ def generate_srct(n_rows, n_cols, rng):
 
 
 def srct_operator(n_rows, n_cols, rng, mode="f64"):
-    """SRCT sketch (``parla/utils/sketching.py:179-201``), wide orientation."""
-    if n_cols < n_rows:
-        raise NotImplementedError("SRCT is provided for the wide (sketch-from-the-left) case")
+    """SRCT sketch (``parla/utils/sketching.py:179-201``): the wide operator,
+    or for n_cols < n_rows the transpose of the wide (n_cols x n_rows) one,
+    with the reference's draws in both cases."""
     gen = rng if isinstance(rng, np.random.Generator) else np.random.default_rng(rng)
     r, e, perm = generate_srct(n_rows, n_cols, gen)
-    return SRCTOperator(r, e, perm, n_rows, n_cols, mode)
+    return SRCTOperator(r, e, perm, n_rows, n_cols, mode, tall=n_cols < n_rows)

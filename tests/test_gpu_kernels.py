@@ -273,14 +273,52 @@ def test_sjlt_apply_right(K):
 
 
 @pytest.mark.parametrize("mode", ["f64", "df"])
-@pytest.mark.parametrize("d,m,n", [(16, 100, 5), (80, 2000, 20)])
+@pytest.mark.parametrize("d,m,n", [(16, 100, 5), (80, 2000, 20), (800, 20000, 200), (64, 2 * 3 * 5 * 7 * 12, 9),
+                                   (10, 99, 3), (8, 176, 4), (1, 2, 3), (40, 2 * 12544, 2), (7, 8, 1)])
 def test_srct_apply(K, mode, d, m, n):
-    gen = np.random.default_rng(16)
+    """Against the oracle's transform (SciPy DCT): the FFT path (even m with
+    N = m/2 of factors 2, 3, 5, 7 up to 12800: 100, 2000, 20000, 2520, 2,
+    25088, 8) and the explicit-operator path (odd m, N = 88 = 8 x 11)."""
+    gen = np.random.default_rng(16 + m)
     r, e, perm = osk.generate_srct(d, m, gen)
     A = np.random.default_rng(1).standard_normal((m, n))
+    A[::13] *= 1e6                                    # wide dynamic range
     ref = osk.apply_srct(r, e, A, perm)
     Y = K.srct_apply(dev(r), dev(e), dev(perm), dev(A), mode).cpu().numpy()
     assert rel(Y, ref) <= 1e-12
+    y = K.srct_apply(dev(r), dev(e), dev(perm), dev(A[:, 0]), mode).cpu().numpy()   # a vector
+    assert rel(y, ref[:, 0]) <= 1e-12
+
+
+@pytest.mark.parametrize("mode", ["f64", "df"])
+@pytest.mark.parametrize("d,m,n", [(16, 100, 5), (80, 2000, 20), (10, 99, 1)])
+def test_srct_adjoint(K, mode, d, m, n):
+    gen = np.random.default_rng(7 + m)
+    r, e, perm = osk.generate_srct(d, m, gen)
+    Y = np.random.default_rng(2).standard_normal((d, n))
+    ref = osk.apply_srct(r, e, Y, perm, forward=False)
+    X = K.srct_adjoint(dev(r), dev(e), dev(perm), dev(Y), m, mode).cpu().numpy()
+    assert rel(X, ref) <= 1e-12
+
+
+@pytest.mark.parametrize("shape", [(2000, 40), (40, 2000), (300, 299), (99, 10)])
+def test_srct_operator_orientations(K, shape):
+    """The SRCT operator of the reference's draws in both orientations
+    (tall: the transpose of the wide one): S @ X, X @ S and S' v against the
+    oracle's dense matrix."""
+    import parla_gb300 as pg
+    n_rows, n_cols = shape
+    S = pg.SkOpTC()(n_rows, n_cols, np.random.default_rng(3))
+    Sd = osk.srct_matrix(n_rows, n_cols, np.random.default_rng(3))
+    assert Sd.shape == (n_rows, n_cols)
+    rng = np.random.default_rng(4)
+    X = rng.standard_normal((n_cols, 3))
+    Z = rng.standard_normal((5, n_rows))
+    v = rng.standard_normal(n_rows)
+    assert rel(np.asarray(S @ X), Sd @ X) <= 1e-12
+    assert rel(np.asarray(Z @ S), Z @ Sd) <= 1e-12
+    assert rel(S.t_matvec(dev(v)).cpu().numpy(), Sd.T @ v) <= 1e-12
+    assert rel(S.dense_matrix().cpu().numpy(), Sd) <= 1e-12
 
 
 @pytest.mark.parametrize("mode", ["f64", "df"])
@@ -528,3 +566,16 @@ def test_gram_f32_df(K, trans, shape):
     assert torch.equal(G, G.t())
     d = torch.sqrt(torch.diagonal(ref))
     assert bool(torch.all((G - ref).abs() <= 1e-12 * torch.outer(d, d) + 1e-300))
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_srct_right_sketch_in_qb(K, precision):
+    """The tall SRCT as RS1's right sketch (A @ S runs the fast transform on
+    A^T): QB1 recovers an exactly rank-20 matrix."""
+    import parla_gb300 as pg
+    rng = np.random.default_rng(12)
+    A = rng.standard_normal((600, 20)) @ rng.standard_normal((20, 400))
+    qb = pg.QB1(pg.RF1(pg.RS1(pg.SkOpTC(), 2)), precision=precision)
+    Q, B = qb(A, 30, np.nan, 5)
+    err = np.linalg.norm(A - np.asarray(Q) @ np.asarray(B)) / np.linalg.norm(A)
+    assert err <= (1e-10 if precision == "f64" else 1e-5), err
