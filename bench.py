@@ -14,6 +14,7 @@ the reference driver chain, pinned against the reference's own outputs) on
 the host cores, on the same matrix.
 """
 import argparse
+import math
 import json
 import os
 import subprocess
@@ -616,7 +617,8 @@ def bench_ls_batched(torch, pg, count, cpu_budget=0.0):
     out = {"workload": f"{count} LS problems, SJLT d=4n nnz=8, target rel. prediction error 1e-10",
            "problems": count, "total_A_GB": sum(A.numel() * 8 for A, _ in probs) / 1e9}
     solver = pg.BatchedSPO(precision="mixed", streams=16)
-    replay = solver.capture(probs, rng=5)
+    layout, cand = solver.tune_layout(probs, rng=5)      # every candidate LSQR layout timed on this batch
+    replay = solver.capture(probs, rng=5)                 # captured with the tuned layout
     replay()
     torch.cuda.synchronize()
     s_, e_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -628,7 +630,19 @@ def bench_ls_batched(torch, pg, count, cpu_budget=0.0):
     info = solver.info_from_plan(replay.plan)
     out["batched"] = {"solves_per_s": count / dt, "ms": dt * 1e3,
                       "lsqr_itn_mean": float(np.mean([i["itn"] for i in info])),
-                      "barrier_errors": int(sum(i["err"] != 0 for i in info))}
+                      "barrier_errors": int(sum(i["err"] != 0 for i in info)),
+                      "strategy_mix": {s_: sum(i["strategy"] == s_ for i in info) for s_ in ("df",)},
+                      "layout": {"tuned": layout, "classes": [[int(c[1]), int(c[2]), int(c[3]), int(c[4])]
+                                                              for c in replay.plan["ls_classes"]],
+                                 "class_fields": "problems, widest n, cluster CTAs, CTA budget",
+                                 "candidates_ms": {f"epc=2^{int(math.log2(k[0]))},gmax={k[1]}": v
+                                                   for k, v in cand.items()}}}
+    solver.phase_times = {}
+    solver._launch(replay.plan)
+    out["batched"]["phases_ms_eager"] = dict(solver.phase_times)
+    solver.phase_times = None
+    lsq_bytes = sum(A.numel() * 8 * i["itn"] for (A, _), i in zip(probs, info))
+    out["batched"]["lsqr_phase_gbs"] = lsq_bytes / (out["batched"]["phases_ms_eager"]["lsqr"] * 1e-3) / 1e9
     plain = pg.BatchedSPO(precision="f64")
     plain(probs[:2], rng=1)
     torch.cuda.synchronize()

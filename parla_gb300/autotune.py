@@ -1,14 +1,18 @@
-"""Project autotuner: per-shape launch configurations chosen by measurement.
+"""Project autotuner: launch configurations chosen by measurement.
 
-The batched least-squares solver runs one cooperative QR and one cooperative
-LSQR per problem, several problems at once on separate streams.  How many
-CTAs each problem gets trades latency (more CTAs) against barrier overhead
-and concurrency (fewer CTAs).  ``Tuner`` measures candidate CTA counts on a
-synthetic problem of each size bucket (log2 of rows and columns), keeps the
-one with the least CTA-seconds whose time stays within ``slack`` of the
-fastest, and caches the choice in a JSON file (``$PARLA_GB300_TUNE`` or
-``~/.cache/parla_gb300/tune.json``).  Without measurements it falls back to
-a cost model.
+Two kinds of entries share one table, cached in a JSON file
+(``$PARLA_GB300_TUNE`` or ``~/.cache/parla_gb300/tune.json``):
+
+* ``qr:<bucket>`` / ``lsqr:<bucket>`` -- the CTA count of a single
+  cooperative QR or LSQR launch (the per-problem solves of the non-graph
+  batched path, ``BatchedSPO(strategy='refine')``): ``tune`` measures the
+  candidates (4, 16, 64) on a synthetic problem of each size bucket (log2 of
+  rows and columns) and keeps the one with the least CTA-seconds within
+  ``slack`` of the fastest; without a measurement a cost model answers.
+* ``layout:<batch signature>`` -- the LSQR launch layout of the
+  graph-captured batched solver (the cluster-size rule of its persistent
+  launches), stored by ``BatchedSPO.tune_layout`` after timing every
+  candidate on the batch itself, read back by ``lookup``.
 """
 import json
 import math
@@ -51,6 +55,15 @@ class Tuner:
         if kind == "lsqr":
             return int(min(128, max(2, 2 ** round(math.log2(max(m * n * 8 / 2e6, 1))))))
         return int(min(128, max(2, 2 ** round(math.log2(max(n / 16, 1))))))
+
+    def put(self, key, value):
+        with self._lock:
+            self.table[key] = value
+
+    def lookup(self, key):
+        """The stored entry for `key`, or None."""
+        with self._lock:
+            return self.table.get(key)
 
     def get(self, kind, m, n):
         key = f"{kind}:{_bucket(m, n)}"

@@ -64,6 +64,9 @@ class BatchedSPO:
         self.big_lsqr_numel = big_lsqr_numel
         self.last_info = None
         self.last_layout = None
+        # phase_times: when a dict, eager launches record CUDA events at the
+        # phase boundaries and fill it with milliseconds per phase
+        self.phase_times = None
 
     # ---------------------------------------------------------------- helpers
     def _sketch_qr(self, A, b, seed, mode, ctas):
@@ -103,7 +106,7 @@ class BatchedSPO:
             self.last_info = self.info_from_plan(plan)
             self.last_layout = None
             return plan["xs"]
-        plan = self._finish_plan(self._prepare(problems, seeds))
+        plan = self._finish_plan(self._prepare(problems, seeds), self.tuner.lookup(self.layout_key(problems)))
         self._launch(plan)
         torch.cuda.synchronize()
         self.last_info = self.info_from_plan(plan)
@@ -168,6 +171,16 @@ class BatchedSPO:
         items, problems = plan["items"], plan["problems"]
         dev = K.device()
         main = torch.cuda.current_stream()
+        timing = self.phase_times is not None and not torch.cuda.is_current_stream_capturing()
+        marks = []
+
+        def mark(name):
+            if timing:
+                ev = torch.cuda.Event(enable_timing=True)
+                ev.record(main)
+                marks.append((name, ev))
+
+        mark("start")
         streams = [torch.cuda.Stream() for _ in range(self.nstreams)]
         for s in streams:
             s.wait_stream(main)
@@ -190,10 +203,12 @@ class BatchedSPO:
                           K.ptr(it["Tlo"]), it["d"], K.stream())
         for s in streams:
             main.wait_stream(s)
+        mark("split_sketch")
         # phase B: every QR in one persistent launch (one CTA per problem,
         # double-float arithmetic on the hi/lo planes)
         _lib.call("rla_geqrf_hl_batched", K.ptr(plan["qr_dev"]), K.ptr(plan["order_dev"]), plan["nprob"],
                   plan["dmax"], K.ptr(plan["next"]), K.stream())
+        mark("qr")
         # phase C: every R^-1 in one launch (one warp per column), and the
         # presolve start z0 = (Q^T S b)[:n] (after every QR)
         _lib.call("rla_trtri_hl_batched", K.ptr(plan["tri_dev"]), plan["nprob"], plan["tri_cols"], plan["nmax"],
@@ -207,6 +222,7 @@ class BatchedSPO:
                 torch.add(it["Thi"][n, :n].double(), it["Tlo"][n, :n].double(), out=it["z"])
         for s in streams:
             main.wait_stream(s)
+        mark("trtri_presolve")
         # phase D: the largest LSQRs as full-device cooperative launches, all
         # the others in one persistent launch
         for i in plan["ls_big"]:
@@ -231,17 +247,33 @@ class BatchedSPO:
         for i in plan["ls_big"]:
             it = items[i]
             K.gemm(it["Rinv"], it["z"], out=it["x"].view(-1, 1), mode="df")
+        mark("lsqr")
+        if timing:
+            torch.cuda.synchronize()
+            self.phase_times.clear()
+            for (_, e0), (name, e1) in zip(marks[:-1], marks[1:]):
+                self.phase_times[name] = e0.elapsed_time(e1)
         K.STATS.launches += 6 * plan["nprob"] + 2
 
-    def _finish_plan(self, plan):
-        """Descriptor arrays that need R^-1 buffers: built after allocation."""
+    # LSQR launch layout: a problem of e elements gets a cluster of the
+    # smallest G (power of two, at most gmax) with e <= G epc
+    DEFAULT_LAYOUT = {"epc": 1 << 21, "gmax": 8}
+    LAYOUTS = tuple({"epc": e, "gmax": g} for g in (8, 4) for e in (1 << 20, 1 << 21, 1 << 22))
+
+    def _finish_plan(self, plan, layout=None):
+        """Descriptor arrays that need R^-1 buffers: built after allocation.
+        ``layout``: the LSQR cluster rule (``DEFAULT_LAYOUT``, or the tuned
+        one for this batch)."""
         import ctypes as C
         from .. import _lib
         lib = _lib.load()
+        layout = dict(layout or self.DEFAULT_LAYOUT)
+        plan["layout"] = layout
         items = plan["items"]
         buf = (C.c_char * len(plan["ls_host"])).from_buffer(plan["ls_host"])
         for i, (it, (A, b)) in enumerate(zip(items, plan["problems"])):
-            it["Rinv"] = torch.empty((it["n"], it["n"]), dtype=torch.float64, device=K.device())
+            if "Rinv" not in it:
+                it["Rinv"] = torch.empty((it["n"], it["n"]), dtype=torch.float64, device=K.device())
             rec = C.addressof(buf) + i * plan["ls_rec"]
             _lib.call("rla_lsqr_record", C.c_void_p(rec), it["m"], it["n"], it["n"], None, K.ptr(it["hi"]),
                       K.ptr(it["lo"]), it["n"], K.ptr(it["Rinv"]), it["n"], 0.0, K.ptr(b), K.ptr(it["z"]), 1,
@@ -304,7 +336,7 @@ class BatchedSPO:
         def cluster_of(i):
             e = items[i]["m"] * items[i]["n"]
             g = 1
-            while g < 8 and e > g * (1 << 21):
+            while g < layout["gmax"] and e > g * layout["epc"]:
                 g *= 2
             return g
 
@@ -361,19 +393,59 @@ class BatchedSPO:
                   C.byref(C.c_size_t(plan["hws"].numel())), K.stream())
         K.STATS.launches += 6 * plan["nprob"] + 4
 
-    def plan(self, problems, rng=0):
+    @staticmethod
+    def layout_key(problems):
+        """Batch signature for the tuned layout: count and the log2 histogram of
+        element counts (the quantity the cluster rule reads)."""
+        hist = {}
+        for A, _ in problems:
+            e = int(round(math.log2(max(A.numel(), 1))))
+            hist[e] = hist.get(e, 0) + 1
+        return "layout:%d:%s" % (len(problems), ",".join(f"{k}x{v}" for k, v in sorted(hist.items())))
+
+    def tune_layout(self, problems, rng=0, reps=1):
+        """Time every candidate LSQR layout (``LAYOUTS``) on this batch (each a
+        full solve), keep the fastest in the Tuner's table under the batch
+        signature and return (layout, {layout: ms})."""
+        rng = np.random.default_rng(rng)
+        seeds = [int(s) for s in rng.integers(0, 2 ** 62, size=len(problems))]
+        base = self._prepare(problems, seeds)
+        times = {}
+        for lay in self.LAYOUTS:
+            plan = self._finish_plan(dict(base), lay)
+            self._launch(plan)
+            torch.cuda.synchronize()
+            s_, e_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s_.record()
+            for _ in range(reps):
+                self._launch(plan)
+            e_.record()
+            torch.cuda.synchronize()
+            times[(lay["epc"], lay["gmax"])] = s_.elapsed_time(e_) / reps
+        best = min(times, key=times.get)
+        choice = {"epc": best[0], "gmax": best[1]}
+        self.tuner.put(self.layout_key(problems), choice)
+        return choice, times
+
+    def plan(self, problems, rng=0, layout=None):
         rng = np.random.default_rng(rng)
         seeds = [int(s) for s in rng.integers(0, 2 ** 62, size=len(problems))]
         if self.engine == "capi":
             return self._capi_plan(problems, seeds)
-        return self._finish_plan(self._prepare(problems, seeds))
+        if layout is None:
+            layout = self.tuner.lookup(self.layout_key(problems))
+        return self._finish_plan(self._prepare(problems, seeds), layout)
 
-    def capture(self, problems, rng=0):
+    def capture(self, problems, rng=0, tune=False):
         """Record the whole batch as one CUDA graph; returns replay() -> solutions.
 
         Every replay recomputes all sketches, QRs, inverses and LSQR solves
-        from the inputs (the sketch seeds are part of the graph).
+        from the inputs (the sketch seeds are part of the graph).  The LSQR
+        layout is the Tuner's for this batch signature when it has one; with
+        ``tune`` the candidates are timed first (``tune_layout``).
         """
+        if tune and self.engine != "capi" and self.tuner.lookup(self.layout_key(problems)) is None:
+            self.tune_layout(problems, rng)
         plan = self.plan(problems, rng)
         launch = self._capi_launch if self.engine == "capi" else self._launch
         launch(plan)                    # warm-up run outside capture

@@ -135,3 +135,23 @@ def test_batched_hard_problems(pg, hard_batch, route):
         err = _pred_err(A, x.cpu().numpy(), b)
         assert err <= 1e-10, (name, info, err)
         assert info["err"] == 0
+
+
+def test_tuned_layout_on_the_graph_path(pg, batch, tmp_path):
+    """tune_layout times every candidate LSQR layout on the batch, stores the
+    fastest under the batch signature; a capture then uses it, and the
+    replayed solutions meet the 1e-10 gate."""
+    probs, refs, shapes = batch
+    tuner = pg.Tuner(path=str(tmp_path / "tune.json"))
+    solver = pg.BatchedSPO(precision="mixed", tuner=tuner, streams=4)
+    choice, times = solver.tune_layout(probs, rng=3)
+    assert choice in [dict(l) for l in solver.LAYOUTS]
+    assert len(times) == len(solver.LAYOUTS) and all(t > 0 for t in times.values())
+    assert tuner.lookup(solver.layout_key(probs)) == choice
+    replay = solver.capture(probs, rng=3)
+    assert replay.plan["layout"] == choice
+    xs = replay()
+    torch.cuda.synchronize()
+    for (A, b), x, xr in zip(probs, xs, refs):
+        An = A.cpu().numpy()
+        assert la.norm(An @ (x.cpu().numpy() - xr)) / la.norm(An @ xr) <= 1e-10
