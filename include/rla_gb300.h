@@ -245,6 +245,16 @@ int rla_gemm_bf16_tc(int64_t M, int64_t N, int64_t K, const void* X,
                      int splits, void* ws, size_t* ws_bytes,
                      rla_stream_t stream);
 
+/* rla_gemm_bf16_tc with an optional bf16 copy of the output: Db (same
+ * layout as D, leading dimension lddb) receives bf16(D) when not NULL (the
+ * operand image the next tensor-core product of the randomized SVD reads,
+ * stored from the same registers instead of a separate conversion pass). */
+int rla_gemm_bf16_tc_ex(int64_t M, int64_t N, int64_t K, const void* X,
+                        int64_t ldx, const void* W, int64_t ldw, float* D,
+                        int64_t ldd, int out_trans, float alpha, float beta,
+                        void* Db, int64_t lddb, int splits, void* ws,
+                        size_t* ws_bytes, rla_stream_t stream);
+
 /* Reads the device error flag (0 or RLA_ERR_TIMEOUT) left in `ws` by the
  * last rla_gemm_bf16_tc on that workspace; synchronises `stream`. */
 int rla_gemm_bf16_tc_status(const void* ws, int* status, rla_stream_t stream);

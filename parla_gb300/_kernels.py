@@ -161,11 +161,11 @@ def gemm(A, B, transa=False, transb=False, alpha=1.0, beta=0.0, out=None, mode=N
     return out
 
 
-def gemm_tc(X, W, out=None, out_trans=False, alpha=1.0, beta=0.0, splits=0, check=False):
+def gemm_tc(X, W, out=None, out_trans=False, alpha=1.0, beta=0.0, splits=0, check=False, want_bf16=False):
     """fp32 D = alpha X W^T (+ beta D) on the tensor cores; X, W bf16 row-major.
 
-    Returns D (M x N) or, with out_trans, D^T (N x M).
-    """
+    Returns D (M x N) or, with out_trans, D^T (N x M); with ``want_bf16``
+    (D, Db) where Db is the bf16 image of D stored by the same kernel."""
     assert X.dtype == torch.bfloat16 and W.dtype == torch.bfloat16
     assert X.stride(1) == 1 and W.stride(1) == 1
     M, Kx = X.shape
@@ -175,20 +175,22 @@ def gemm_tc(X, W, out=None, out_trans=False, alpha=1.0, beta=0.0, splits=0, chec
     if out is None:
         out = torch.empty((N, M) if out_trans else (M, N), dtype=torch.float32, device=X.device)
         beta = 0.0
+    Db = empty_bf16(*out.shape, X.device) if want_bf16 else None
     head = (M, N, Kx, ptr(X), X.stride(0), ptr(W), W.stride(0), ptr(out), out.stride(0), int(out_trans),
-            C.c_float(alpha), C.c_float(beta), int(splits))
-    need = size_query("rla_gemm_bf16_tc", *head)
+            C.c_float(alpha), C.c_float(beta))
+    tail = (ptr(Db), Db.stride(0) if Db is not None else 0, int(splits))
+    need = size_query("rla_gemm_bf16_tc_ex", *head, *tail)
     ws = workspace(need)
     nb = C.c_size_t(need)
     if STATS.timing:
         STATS.meta.append((M, N, Kx))
-    _timed("gemm_tc", 2, call, "rla_gemm_bf16_tc", *head, ptr(ws), C.byref(nb), stream())
+    _timed("gemm_tc", 2, call, "rla_gemm_bf16_tc_ex", *head, *tail, ptr(ws), C.byref(nb), stream())
     if check:
         st = C.c_int(0)
         call("rla_gemm_bf16_tc_status", ptr(ws), C.byref(st), stream())
         if st.value:
             raise _lib.RlaError("rla_gemm_bf16_tc", st.value, "device wait timed out")
-    return out
+    return (out, Db) if want_bf16 else out
 
 
 # ------------------------------------------------------------- sketches

@@ -61,6 +61,8 @@ SIGNATURES = {
     "rla_gemm_bf16_tc": [_i64, _i64, _i64, _p, _i64, _p, _i64, _p, _i64, _i32, C.c_float, C.c_float, _i32,
                          _p, _psz, _p],
     "rla_gemm_bf16_tc_status": [_p, C.POINTER(C.c_int), _p],
+    "rla_gemm_bf16_tc_ex": [_i64, _i64, _i64, _p, _i64, _p, _i64, _p, _i64, _i32, C.c_float, C.c_float, _p, _i64,
+                            _i32, _p, _psz, _p],
     "rla_geqrf": [_i32, _i64, _i64, _i64, _p, _i64, _p, _p, _psz, _p],
     "rla_geqrf_ctas": [_i32, _i64, _i64, _i64, _p, _i64, _p, _i32, _p, _psz, _p],
     "rla_geqp3": [_i32, _i64, _i64, _i64, _i64, _p, _i64, _p, _p, _p, _psz, _p],

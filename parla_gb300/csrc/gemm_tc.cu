@@ -134,6 +134,8 @@ struct TcParams {
   float alpha, beta;
   float* D;
   int64_t ldd;
+  __nv_bfloat16* Db;  // optional bf16 copy of the output (same layout, leading dimension lddb)
+  int64_t lddb;
   float* part;       // split-K partials [z][N][M] (transposed layout) or null
   int* err;
 };
@@ -253,6 +255,7 @@ gemm_tc_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_constant
                 float r = p.alpha * v[t];
                 if (p.beta != 0.f) r = fmaf(p.beta, *dst, r);
                 *dst = r;
+                if (p.Db) (p.out_trans ? p.Db[col * p.lddb + row] : p.Db[row * p.lddb + col]) = __float2bfloat16_rn(r);
               }
             }
           }
@@ -270,7 +273,8 @@ gemm_tc_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_constant
 
 // D (or D^T) = alpha * sum_z part[z] + beta * D, fixed summation order.
 __global__ void tc_splitk_reduce(int64_t M, int64_t N, int splits, const float* __restrict__ part, float alpha,
-                                 float beta, float* __restrict__ D, int64_t ldd, int out_trans) {
+                                 float beta, float* __restrict__ D, int64_t ldd, int out_trans,
+                                 __nv_bfloat16* __restrict__ Db, int64_t lddb) {
   int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (e >= M * N) return;
   int64_t col = e / M, row = e % M;  // part layout [z][col][row]
@@ -280,6 +284,7 @@ __global__ void tc_splitk_reduce(int64_t M, int64_t N, int splits, const float* 
   float r = alpha * s;
   if (beta != 0.f) r = fmaf(beta, *dst, r);
   *dst = r;
+  if (Db) (out_trans ? Db[col * lddb + row] : Db[row * lddb + col]) = __float2bfloat16_rn(r);
 }
 
 // ------------------------------------------------------------------ host
@@ -366,9 +371,22 @@ bool g_attr_set[64] = {};  // per device: dynamic smem limit raised
 
 using namespace rla;
 
+extern "C" int rla_gemm_bf16_tc_ex(int64_t M, int64_t N, int64_t K, const void* X, int64_t ldx, const void* W,
+                                   int64_t ldw, float* D, int64_t ldd, int out_trans, float alpha, float beta,
+                                   void* Db, int64_t lddb, int splits, void* ws, size_t* ws_bytes,
+                                   rla_stream_t stream);
+
 extern "C" int rla_gemm_bf16_tc(int64_t M, int64_t N, int64_t K, const void* X, int64_t ldx, const void* W,
                                 int64_t ldw, float* D, int64_t ldd, int out_trans, float alpha, float beta,
                                 int splits, void* ws, size_t* ws_bytes, rla_stream_t stream) {
+  return rla_gemm_bf16_tc_ex(M, N, K, X, ldx, W, ldw, D, ldd, out_trans, alpha, beta, nullptr, 0, splits, ws,
+                             ws_bytes, stream);
+}
+
+extern "C" int rla_gemm_bf16_tc_ex(int64_t M, int64_t N, int64_t K, const void* X, int64_t ldx, const void* W,
+                                   int64_t ldw, float* D, int64_t ldd, int out_trans, float alpha, float beta,
+                                   void* Db, int64_t lddb, int splits, void* ws, size_t* ws_bytes,
+                                   rla_stream_t stream) {
   if (M < 0 || N < 0 || K < 0 || splits < 0) return RLA_ERR_ARG;
   TcPlan pl = tc_plan(imax(M, 1), imax(N, 1), imax(K, 1), splits);
   if (ws == nullptr && ws_bytes != nullptr) { *ws_bytes = pl.ws; return RLA_OK; }
@@ -379,6 +397,7 @@ extern "C" int rla_gemm_bf16_tc(int64_t M, int64_t N, int64_t K, const void* X, 
       ldx < K || ldw < K)
     return RLA_ERR_ARG;
   if (out_trans ? (ldd < M) : (ldd < N)) return RLA_ERR_ARG;
+  if (Db && (out_trans ? (lddb < M) : (lddb < N))) return RLA_ERR_ARG;
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   int dev = 0;
   RLA_CUDA_TRY(cudaGetDevice(&dev));
@@ -404,13 +423,14 @@ extern "C" int rla_gemm_bf16_tc(int64_t M, int64_t N, int64_t K, const void* X, 
   TcParams p{};
   p.M = M; p.N = N; p.K = K; p.bm = pl.bm; p.n_tile = pl.n_tile; p.stages = pl.stages; p.kblocks_per_split = pl.kbps;
   p.out_trans = out_trans; p.alpha = alpha; p.beta = beta; p.D = D; p.ldd = ldd; p.err = err;
+  p.Db = static_cast<__nv_bfloat16*>(Db); p.lddb = lddb;
   p.part = pl.splits > 1 ? reinterpret_cast<float*>(static_cast<char*>(ws) + 256) : nullptr;
   dim3 grid(static_cast<unsigned>(pl.tiles_m), static_cast<unsigned>(pl.tiles_n), static_cast<unsigned>(pl.splits));
   gemm_tc_kernel<<<grid, kTcThreads, pl.smem, st>>>(mx, mw, p);
   RLA_LAUNCH_CHECK();
   if (pl.splits > 1) {
-    tc_splitk_reduce<<<static_cast<unsigned>(ceil_div(M * N, 256)), 256, 0, st>>>(M, N, pl.splits, p.part, alpha,
-                                                                                  beta, D, ldd, out_trans);
+    tc_splitk_reduce<<<static_cast<unsigned>(ceil_div(M * N, 256)), 256, 0, st>>>(
+        M, N, pl.splits, p.part, alpha, beta, D, ldd, out_trans, p.Db, lddb);
     RLA_LAUNCH_CHECK();
   }
   return RLA_OK;

@@ -231,20 +231,26 @@ def orth_tc(Y, passes=1):
     use an fp32 Gram and bring the columns to fp32 orthonormality, which the
     final range-finder basis needs.  Returns an (m x l) view of l x m storage.
     """
-    from .operand import panel_t
+    from .operand import bf16_image, panel_t
     Qt = panel_t(Y)
     if Qt.dtype != torch.float32:
         Qt = Qt.to(torch.float32)
-    l = Qt.shape[0]
+    Qb = None
     for p in range(passes):
         if p == 0:
-            Yb = K.convert(Qt, torch.bfloat16)
+            Yb = bf16_image(Y) if Y.dtype == torch.float32 else K.convert(Qt, torch.bfloat16)
             G = K.gemm_tc(Yb, Yb)
         else:
             G = K.syrk(Qt, mode="f32")
         Rinv = _chol_inv_f32(G)
-        Qt = K.gemm_tn_panel(Rinv, Qt, tri=True)
-    return Qt.t()
+        if p == passes - 1:  # the next tensor-core product reads Q's bf16 image
+            Qt, Qb = K.gemm_tn_panel(Rinv, Qt, tri=True, want_bf16=True)
+        else:
+            Qt = K.gemm_tn_panel(Rinv, Qt, tri=True)
+    Q = Qt.t()
+    if Qb is not None:
+        Q._rla_bf16 = Qb
+    return Q
 
 
 # ----------------------------------------------------------------------------

@@ -141,6 +141,24 @@ def panel_t(S):
     return St if St.is_contiguous() else St.contiguous()
 
 
+def bf16_image(S):
+    """bf16 image of panel_t(S) (l x rows), made once: the kernel that
+    produced S may have stored it alongside (``_rla_bf16``, bitwise the same
+    round-to-nearest conversion); panels are not modified in place after."""
+    Wt = getattr(S, "_rla_bf16", None)
+    if Wt is not None:
+        return Wt
+    return K.convert(panel_t(S), torch.bfloat16)
+
+
+def _with_image(D, Db):
+    """(rows x l) view of the l x rows result D, carrying Db, the bf16 image
+    of D stored by the same kernel."""
+    Y = D.t()
+    Y._rla_bf16 = Db
+    return Y
+
+
 def tc_times(Am, S):
     """A @ S on the tensor cores; returns an (m x l) view of l x m storage.
 
@@ -148,11 +166,11 @@ def tc_times(Am, S):
     way and hi S_hi + hi S_lo + lo S_hi are accumulated in fp32 (about 16
     significant bits)."""
     Ab, _ = Am.bf16_pair()
-    St = panel_t(S)
-    Wt = K.convert(St, torch.bfloat16)
+    Wt = bf16_image(S)
     lo = getattr(Am, "lo", None)
     if lo is None:
-        return K.gemm_tc(Ab, Wt, out_trans=True).t()
+        return _with_image(*K.gemm_tc(Ab, Wt, out_trans=True, want_bf16=True))
+    St = panel_t(S)
     St32 = St if St.dtype == torch.float32 else St.to(torch.float32)
     Wl = K.convert((St32 - Wt.float()).contiguous(), torch.bfloat16)
     out = K.gemm_tc(Ab, Wt, out_trans=True)
@@ -164,5 +182,4 @@ def tc_times(Am, S):
 def tc_times_t(Am, S):
     """A.T @ S on the tensor cores; returns an (n x l) view of l x n storage."""
     _, Abt = Am.bf16_pair()
-    Wt = K.convert(panel_t(S), torch.bfloat16)
-    return K.gemm_tc(Abt, Wt, out_trans=True).t()
+    return _with_image(*K.gemm_tc(Abt, bf16_image(S), out_trans=True, want_bf16=True))
