@@ -210,23 +210,39 @@ def run_ours(args):
     torch.cuda.synchronize()
     eager_ms = t0.elapsed_time(t1) / args.steps
 
-    # end to end: pinned host A in, factors out, through the public API (a
-    # captured call on the host buffer: the bf16 conversion kernel reads A
-    # over the host link, the graph copies U, s, Vh back into pinned memory)
+    # end to end: pinned host A in, factors out, through the public API.
+    # `value`: SVD1.stream over the steps' host matrices (two pinned host
+    # copies of A, alternating): every step copies its 537 MB in (copy
+    # engine) and U, s, Vh out; the copy of step i + 1 runs during the
+    # computation of step i.  The clock runs from before the first copy to
+    # the host holding the last step's factors (pipeline fill and drain
+    # included).  `graph_host_value`: one captured call per step on the host
+    # buffer itself (the bf16 conversion kernel reads A over the host link,
+    # no overlap between steps).
     A_host = A.cpu().pin_memory()
+    A_host2 = A_host.clone().pin_memory()
     h2d = A_host.numel() * 4
+    sv = svd.stream((M_ROWS, N_COLS), K_RANK, np.nan, OVER, 2999)
+    for _ in sv.map([(A_host, 2990 + w) for w in range(args.warmup)]):
+        pass
+    torch.cuda.synchronize()
+    d2h = 0
+    items = [((A_host, A_host2)[it % 2], 3000 + it) for it in range(args.steps)]
+    t_e2e = time.perf_counter()
+    for Uh, sh, Vhh in sv.map(items):
+        d2h = (Uh.numel() + sh.numel() + Vhh.numel()) * 4
+    e2e_ms = (time.perf_counter() - t_e2e) * 1e3
+    del sv
     rep_h = svd.capture(A_host, K_RANK, np.nan, OVER, 2999)
     for w in range(args.warmup):
         rep_h(2990 + w)
     torch.cuda.synchronize()
-    d2h = 0
     t0.record(stream)
     for it in range(args.steps):
-        Uh, sh, Vhh = rep_h(3000 + it)
-        d2h = (Uh.numel() + sh.numel() + Vhh.numel()) * 4
+        rep_h(3000 + it)
     t1.record(stream)
     torch.cuda.synchronize()
-    e2e_ms = t0.elapsed_time(t1)
+    e2e_graph_host_ms = t0.elapsed_time(t1) / args.steps
     t0.record(stream)
     for it in range(args.steps):
         svd(A_host, K_RANK, np.nan, OVER, 3500 + it)
@@ -336,7 +352,12 @@ def run_ours(args):
                              "sgemm_pass_tflops": sgemm_tflops, "frob_err_ratio": err_torch / tail},
         "e2e": {"value": world * args.steps / (e2e_ms * 1e-3), "unit": "rsvd/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "eager_value": 1e3 / e2e_eager_ms,
-                "how": "graph replay of SVD1 on a pinned host A (SVD1.capture); eager_value: plain svd() calls"},
+                "graph_host_value": 1e3 / e2e_graph_host_ms,
+                "how": "SVD1.stream over the steps' pinned host matrices: each step copies A in and U, s, Vh out, "
+                       "the copy of the next step overlapping this step's graph replay; wall clock from the first "
+                       "copy to the last step's factors on the host.  graph_host_value: one captured call per step "
+                       "on the host buffer (conversion kernel reading A over the host link, no overlap); "
+                       "eager_value: plain svd() calls on the host buffer"},
         "eager": {"ms_per_step": eager_ms, "value": 1e3 / eager_ms,
                   "what": "the same SVD1 calls without graph capture (one host launch per kernel)"},
         "roofline": {"kernel": dom, "bound": "hbm", "achieved": dom_gbs, "peak": hbm, "unit": "GB/s",
@@ -643,6 +664,30 @@ def bench_ls_batched(torch, pg, count, cpu_budget=0.0):
     solver.phase_times = None
     lsq_bytes = sum(A.numel() * 8 * i["itn"] for (A, _), i in zip(probs, info))
     out["batched"]["lsqr_phase_gbs"] = lsq_bytes / (out["batched"]["phases_ms_eager"]["lsqr"] * 1e-3) / 1e9
+    # the batched bar: the same plan and graph with binary64 LSQR on A (the
+    # precision of the dominant phase without the batching confound)
+    solver64 = pg.BatchedSPO(precision="f64_batched", streams=16)
+    lay64, _ = solver64.tune_layout(probs, rng=5)
+    rep64 = solver64.capture(probs, rng=5)
+    rep64()
+    torch.cuda.synchronize()
+    s_.record()
+    xb = rep64()
+    e_.record()
+    torch.cuda.synchronize()
+    dtb = s_.elapsed_time(e_) / 1e3
+    info64 = solver64.info_from_plan(rep64.plan)
+    solver64.phase_times = {}
+    solver64._launch(rep64.plan)
+    ph64 = dict(solver64.phase_times)
+    lsq64 = sum(A.numel() * 8 * i["itn"] for (A, _), i in zip(probs, info64))
+    out["batched_fp64"] = {"solves_per_s": count / dtb, "ms": dtb * 1e3, "layout": lay64,
+                           "lsqr_itn_mean": float(np.mean([i["itn"] for i in info64])),
+                           "barrier_errors": int(sum(i["err"] != 0 for i in info64)),
+                           "phases_ms_eager": ph64, "lsqr_phase_gbs": lsq64 / (ph64["lsqr"] * 1e-3) / 1e9,
+                           "what": "the batched plan and CUDA graph with binary64 LSQR on A (no hi/lo split); "
+                                   "the exact sketch and the double-float sketch QR are the mixed path's"}
+    del rep64, solver64
     plain = pg.BatchedSPO(precision="f64")
     plain(probs[:2], rng=1)
     torch.cuda.synchronize()
@@ -652,17 +697,20 @@ def bench_ls_batched(torch, pg, count, cpu_budget=0.0):
     dtp = time.perf_counter() - t0
     out["plain_fp64"] = {"solves_per_s": count / dtp, "ms": dtp * 1e3}
     out["speedup"] = out["batched"]["solves_per_s"] / out["plain_fp64"]["solves_per_s"]
+    out["speedup_vs_batched_fp64"] = out["batched"]["solves_per_s"] / out["batched_fp64"]["solves_per_s"]
     idx = _stratified_sample(shapes, 48)
-    worst, worst_p, errs = 0.0, 0.0, []
+    worst, worst_p, worst_b, errs = 0.0, 0.0, 0.0, []
     for i in idx:
         An = probs[i][0].cpu().numpy()
         xr = la.lstsq(An, probs[i][1].cpu().numpy(), lapack_driver="gelsy")[0]
         e = float(la.norm(An @ (xs[i].cpu().numpy() - xr)) / la.norm(An @ xr))
         worst = max(worst, e)
         worst_p = max(worst_p, float(la.norm(An @ (xp[i].cpu().numpy() - xr)) / la.norm(An @ xr)))
+        worst_b = max(worst_b, float(la.norm(An @ (xb[i].cpu().numpy() - xr)) / la.norm(An @ xr)))
         errs.append(e)
     out["pred_err_sampled"] = {
-        "batched": worst, "plain_fp64": worst_p, "problems_checked": len(idx), "median_batched": float(np.median(errs)),
+        "batched": worst, "plain_fp64": worst_p, "batched_fp64": worst_b, "problems_checked": len(idx),
+        "median_batched": float(np.median(errs)),
         "sample": "stratified: the 12 largest m*n, the 12 largest kappa, 24 spread over the rest "
                   f"(largest m*n checked {max(shapes[i][0] * shapes[i][1] for i in idx)}, "
                   f"largest kappa {max(shapes[i][2] for i in idx):.2e}); LAPACK gelsy in binary64 on the host"}
@@ -865,6 +913,44 @@ def run_case(args):
             K.chol_inv_f32(G32)
             R = K.potrf_df_small(G)
             K.svd_jacobi(R)
+    elif args.case == "spo":
+        # three double-float sketch-and-precondition solves, A 20000 x 200 (kappa 1e8),
+        # Gaussian sketch d = 4n, QR preconditioner, tolerance 1e-12
+        import parla_gb300 as pg
+        A, b = _ls_single_problem(torch)
+        solver = pg.SPO(pg.SkOpGA(), 4, "qr", "df")
+        for r in range(3):
+            solver(A, b, 0.0, 1e-12, 200, 1 + r, logging=False)
+    elif args.case == "srct":
+        # the SRCT sketch 800 x 20000 applied to A 20000 x 200, double-float then binary64
+        import parla_gb300 as pg
+        A = torch.randn((20000, 200), generator=g, device="cuda", dtype=torch.float64)
+        S = pg.srct_operator(800, 20000, 5)
+        for mode in ("df", "f64", "df"):
+            K.srct_apply(S.r, S.e, S.perm, A, mode)
+    elif args.case == "panel":
+        # the RSVD's sketch-size products: R^-1 applied to the 210 x 16384 panel
+        # (upper triangular) and U^T B for the final factor
+        C = torch.randn((K_RANK + OVER, K_RANK + OVER), generator=g, device="cuda")
+        R = torch.triu(C).contiguous()
+        X = torch.randn((K_RANK + OVER, M_ROWS), generator=g, device="cuda")
+        for _ in range(3):
+            K.gemm_tn_panel(R, X, tri=True, want_bf16=True)
+            K.gemm_tn_panel(C, X)
+    elif args.case == "batched":
+        # two eager launches of the batched solver's plan: 48 problems of the
+        # batched workload's distribution (SJLT d = 4n, double-float LSQR),
+        # every LSQR in the persistent cluster launches (as nearly all of the
+        # 1024-problem batch's are)
+        import parla_gb300 as pg
+        from parla_gb300.drivers.batched import batch_shapes, make_problem
+        shapes = batch_shapes(48, 7)
+        probs = [make_problem(m, n, kap, 1e-8, 1000 + i)[:2] for i, (m, n, kap) in enumerate(shapes)]
+        solver = pg.BatchedSPO(precision="mixed", streams=16, big_lsqr_numel=1 << 40)
+        plan = solver.plan(probs, rng=5)
+        solver._launch(plan)
+        torch.cuda.synchronize()
+        solver._launch(plan)
     elif args.case == "learned":
         # one training step and one sketch of the learned SJLT, 8 matrices of 4096 columns
         from parla_gb300.learned.sketch import SJLTPattern
@@ -887,7 +973,8 @@ def run_case(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--case", default=None, choices=["tc_pass", "sjlt", "sjlt32", "lsqr", "small", "learned"],
+    ap.add_argument("--case", default=None, choices=["tc_pass", "sjlt", "sjlt32", "lsqr", "small", "learned",
+                                                     "spo", "srct", "panel", "batched"],
                     help="run one small kernel case for a profiler capture and exit")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)

@@ -184,7 +184,9 @@ def gemm_tc(X, W, out=None, out_trans=False, alpha=1.0, beta=0.0, splits=0, chec
     nb = C.c_size_t(need)
     if STATS.timing:
         STATS.meta.append((M, N, Kx))
-    _timed("gemm_tc", 2, call, "rla_gemm_bf16_tc_ex", *head, *tail, ptr(ws), C.byref(nb), stream())
+    # (the workspace holds a 256-byte status block, plus the split-K slices
+    # when the product is split: then a reduce kernel follows)
+    _timed("gemm_tc", 2 if need > 256 else 1, call, "rla_gemm_bf16_tc_ex", *head, *tail, ptr(ws), C.byref(nb), stream())
     if check:
         st = C.c_int(0)
         call("rla_gemm_bf16_tc_status", ptr(ws), C.byref(st), stream())

@@ -16,6 +16,20 @@
 namespace rla {
 namespace {
 
+// Asynchronous global -> shared copies (cp.async, Ampere and later): the
+// source size 0 form zero-fills the destination.
+__device__ __forceinline__ void cp_async4(float* dst, const float* src, bool valid) {
+  const uint32_t d = static_cast<uint32_t>(__cvta_generic_to_shared(dst));
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(d), "l"(src), "r"(valid ? 4 : 0) : "memory");
+}
+__device__ __forceinline__ void cp_async16(float* dst, const float* src, bool valid) {
+  const uint32_t d = static_cast<uint32_t>(__cvta_generic_to_shared(dst));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(d), "l"(src), "r"(valid ? 16 : 0) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
 struct PolF32 {
   using In = float; using Sm = float; using Acc = float; using Part = float; using Out = float;
   static constexpr int BM = 128, BN = 128, BK = 8, TM = 8, TN = 8;
@@ -448,6 +462,162 @@ extern "C" int rla_gemm(int dtype, int transa, int transb, int64_t M, int64_t N,
 // or A^T (A is K x N, trans = 1): only the tiles on and above the diagonal
 // are computed; the lower tiles are copied from them (with beta != 0, C must
 // be symmetric on entry).
+namespace rla {
+namespace {
+// Binary32 Gram of a few long rows, G = A A^T for A (N x K), N <= 248, K
+// large (the l x n matrix B and the l x m final basis of the randomized SVD).
+// The 128 x 128 output tiles of the general kernel leave most SMs idle at
+// N ~ 200; here each CTA takes a slice of K (about K / #SMs columns), stages
+// it transposed in shared memory 32 columns at a time (cp.async, double
+// buffered), and computes the whole upper triangle of 8 x 8 tiles over it,
+// one or two tiles per thread (tiles enumerated row by row, so neighbouring
+// threads share the row operand).  The slices' partials (binary32) are
+// summed in slice order in binary64 by the reduce kernel, which mirrors the
+// tiles below the diagonal.
+constexpr int kGwKS = 32, kGwTh = 256, kGwMaxN = 248;
+
+__host__ __device__ inline int gw_tiles(int64_t N) { return static_cast<int>((N + 7) / 8); }
+__host__ __device__ inline int gw_ld(int64_t N) { return gw_tiles(N) * 8 + 4; }
+
+__global__ void __launch_bounds__(kGwTh, 1) gram_rows_f32_kernel(int N, int64_t K, int64_t kchunk,
+                                                                 const float* __restrict__ A, int64_t lda,
+                                                                 float* __restrict__ part) {
+  extern __shared__ __align__(16) float As[];  // [2][kGwKS][NP]: column c of buffer b at As + (b kGwKS + c) NP
+  const int nt = gw_tiles(N), NP = gw_ld(N), P = nt * (nt + 1) / 2;
+  const int tid = threadIdx.x;
+  int ti[2], tj[2];
+  bool on[2];
+#pragma unroll
+  for (int s = 0; s < 2; ++s) {
+    int p = tid + s * kGwTh, r = 0;
+    on[s] = p < P;
+    while (on[s] && p >= nt - r) { p -= nt - r; ++r; }
+    ti[s] = r;
+    tj[s] = r + p;
+  }
+  float acc[2][8][8];
+#pragma unroll
+  for (int s = 0; s < 2; ++s)
+#pragma unroll
+    for (int a = 0; a < 8; ++a)
+#pragma unroll
+      for (int b = 0; b < 8; ++b) acc[s][a][b] = 0.f;
+  const int64_t k0 = static_cast<int64_t>(blockIdx.x) * kchunk, k1 = min(K, k0 + kchunk);
+  const int rows = nt * 8;
+  // chunk q of the slice -> buffer q & 1; lanes copy 32 consecutive columns of
+  // a row (128 bytes), the rows past N and the columns past k1 zero-filled
+  auto stage = [&](int64_t kb, int buf) {
+    float* dst = As + buf * kGwKS * NP;
+    for (int e = tid; e < rows * kGwKS; e += kGwTh) {
+      const int r = e / kGwKS, c = e % kGwKS;
+      const int64_t k = kb + c;
+      const bool ok = r < N && k < k1;
+      cp_async4(dst + c * NP + r, ok ? A + static_cast<int64_t>(r) * lda + k : A, ok);
+    }
+    cp_async_commit();
+  };
+  if (k0 < k1) stage(k0, 0);
+  int buf = 0;
+  for (int64_t kb = k0; kb < k1; kb += kGwKS, buf ^= 1) {
+    if (kb + kGwKS < k1) {
+      stage(kb + kGwKS, buf ^ 1);  // lands while this chunk is multiplied
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
+    __syncthreads();
+#pragma unroll 2
+    for (int c = 0; c < kGwKS; ++c) {
+      const float* col = As + (buf * kGwKS + c) * NP;
+#pragma unroll
+      for (int s = 0; s < 2; ++s) {
+        if (!on[s]) continue;
+        const float4 a0 = *reinterpret_cast<const float4*>(col + ti[s] * 8);
+        const float4 a1 = *reinterpret_cast<const float4*>(col + ti[s] * 8 + 4);
+        const float4 b0 = *reinterpret_cast<const float4*>(col + tj[s] * 8);
+        const float4 b1 = *reinterpret_cast<const float4*>(col + tj[s] * 8 + 4);
+        const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+        const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+        for (int a = 0; a < 8; ++a)
+#pragma unroll
+          for (int b = 0; b < 8; ++b) acc[s][a][b] = fmaf(av[a], bv[b], acc[s][a][b]);
+      }
+    }
+    __syncthreads();
+  }
+  float* out = part + static_cast<int64_t>(blockIdx.x) * N * N;
+#pragma unroll
+  for (int s = 0; s < 2; ++s) {
+    if (!on[s]) continue;
+#pragma unroll
+    for (int a = 0; a < 8; ++a) {
+      const int i = ti[s] * 8 + a;
+      if (i >= N) continue;
+#pragma unroll
+      for (int b = 0; b < 8; ++b) {
+        const int j = tj[s] * 8 + b;
+        if (j < N) out[static_cast<int64_t>(i) * N + j] = acc[s][a][b];
+      }
+    }
+  }
+}
+
+// C = alpha * sum_z part[z] + beta * C in slice order (binary64), entries of
+// tiles below the diagonal read from the mirror entry.  The loads of a group
+// of 32 slices are issued before their adds.
+__global__ void gram_rows_reduce_kernel(int N, int splits, double alpha, const float* __restrict__ part, double beta,
+                                        float* __restrict__ C, int64_t ldc) {
+  const int64_t idx = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (idx >= static_cast<int64_t>(N) * N) return;
+  const int i = static_cast<int>(idx / N), j = static_cast<int>(idx % N);
+  const bool mir = (i >> 3) > (j >> 3);
+  const int64_t off = mir ? static_cast<int64_t>(j) * N + i : static_cast<int64_t>(i) * N + j;
+  const int64_t stride = static_cast<int64_t>(N) * N;
+  constexpr int kU = 32;
+  double s = 0.0;
+  for (int z0 = 0; z0 < splits; z0 += kU) {
+    float v[kU];
+#pragma unroll
+    for (int u = 0; u < kU; ++u) v[u] = z0 + u < splits ? __ldcg(part + (z0 + u) * stride + off) : 0.f;
+#pragma unroll
+    for (int u = 0; u < kU; ++u) s += static_cast<double>(v[u]);
+  }
+  double r = alpha * s;
+  if (beta != 0.0) r += beta * static_cast<double>(C[static_cast<int64_t>(i) * ldc + j]);
+  C[static_cast<int64_t>(i) * ldc + j] = static_cast<float>(r);
+}
+
+inline int64_t gram_rows_kchunk(int64_t K) {
+  return imax(2 * kGwKS, ceil_div(ceil_div(imax(K, 1), sm_count()), kGwKS) * kGwKS);
+}
+
+int gram_rows_launch(int64_t N, int64_t K, double alpha, const float* A, int64_t lda, double beta, float* C,
+                     int64_t ldc, void* ws, size_t* ws_bytes, cudaStream_t st) {
+  const int64_t kchunk = gram_rows_kchunk(K);
+  const int splits = static_cast<int>(imax(1, ceil_div(imax(K, 1), kchunk)));
+  const size_t need = static_cast<size_t>(splits) * N * N * sizeof(float);
+  if (ws == nullptr && ws_bytes != nullptr) { *ws_bytes = need; return RLA_OK; }
+  if (!ws || !ws_bytes || *ws_bytes < need) return RLA_ERR_WORKSPACE;
+  if (N == 0) return RLA_OK;
+  const size_t smem = 2 * static_cast<size_t>(kGwKS) * gw_ld(N) * sizeof(float);
+  // one attribute for the largest N, set by the first call (thread-safe static)
+  static const cudaError_t attr = cudaFuncSetAttribute(
+      gram_rows_f32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+      static_cast<int>(2 * kGwKS * gw_ld(kGwMaxN) * sizeof(float)));
+  RLA_CUDA_TRY(attr);
+  auto* part = static_cast<float*>(ws);
+  gram_rows_f32_kernel<<<static_cast<unsigned>(splits), kGwTh, smem, st>>>(static_cast<int>(N), K, kchunk, A, lda,
+                                                                           part);
+  RLA_LAUNCH_CHECK();
+  gram_rows_reduce_kernel<<<static_cast<unsigned>(ceil_div(N * N, 256)), 256, 0, st>>>(static_cast<int>(N), splits,
+                                                                                      alpha, part, beta, C, ldc);
+  RLA_LAUNCH_CHECK();
+  return RLA_OK;
+}
+}  // namespace
+}  // namespace rla
+
 extern "C" int rla_syrk(int dtype, int trans, int64_t N, int64_t K, double alpha, const void* A, int64_t lda,
                         double beta, void* C, int64_t ldc, void* ws, size_t* ws_bytes, rla_stream_t stream) {
   if (N < 0 || K < 0) return RLA_ERR_ARG;
@@ -458,6 +628,11 @@ extern "C" int rla_syrk(int dtype, int trans, int64_t N, int64_t K, double alpha
   }
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   const int ta = trans ? 1 : 0, tb = trans ? 0 : 1;
+  // a few long binary32 rows: the slice-per-CTA Gram
+  if (dtype == RLA_F32 && !trans && N > 0 && N <= rla::kGwMaxN && K >= 1024 && lda >= K && ldc >= N &&
+      (query || (ws != nullptr && ws_bytes != nullptr)))
+    return rla::gram_rows_launch(N, K, alpha, static_cast<const float*>(A), lda, beta, static_cast<float*>(C), ldc,
+                                 ws, ws_bytes, st);
   switch (dtype) {
     case RLA_F32: return rla::gemm_launch<rla::PolF32>(ta, tb, N, N, K, alpha, A, lda, A, lda, beta, C, ldc, ws, ws_bytes, st, 1);
     case RLA_F64: return rla::gemm_launch<rla::PolF64>(ta, tb, N, N, K, alpha, A, lda, A, lda, beta, C, ldc, ws, ws_bytes, st, 1);
@@ -608,17 +783,6 @@ namespace rla {
 namespace {
 constexpr int kTpBM = 64, kTpBN = 256, kTpBK = 16, kTpThreads = 256;
 
-__device__ __forceinline__ void cp_async4(float* dst, const float* src, bool valid) {
-  const uint32_t d = static_cast<uint32_t>(__cvta_generic_to_shared(dst));
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(d), "l"(src), "r"(valid ? 4 : 0) : "memory");
-}
-__device__ __forceinline__ void cp_async16(float* dst, const float* src, bool valid) {
-  const uint32_t d = static_cast<uint32_t>(__cvta_generic_to_shared(dst));
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(d), "l"(src), "r"(valid ? 16 : 0) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
 // Thread (ty, tx) = (tid / 32, tid % 32): rows 8 ty .. 8 ty + 7 of the band
 // (a warp shares its rows: the W^T reads are broadcasts) and columns

@@ -25,7 +25,10 @@ problems fill the SMs that large ones leave free; grids come from the
 autotuner.  ``precision='f64'`` is the plain FP64 GPU path: binary64 kernels,
 full-device grids, one problem at a time (the bar the batched path is
 measured against); both use the same stopping rule, so they stop at the
-same accuracy.
+same accuracy.  ``precision='f64_batched'`` is the batched plan and graph
+with the LSQR in binary64 on A itself (no hi/lo split; the exact sketch and
+the double-float QR of the sketch are shared with 'mixed'): the bar that
+separates the precision of the dominant phase from the batching.
 """
 import math
 
@@ -43,7 +46,7 @@ class BatchedSPO:
     def __init__(self, sampling_factor=4, vec_nnz=8, ptol=3e-11, iter_lim=100, precision="mixed", streams=8,
                  tuner=None, max_refine=3, refine_kappa=1e5, strategy="df", big_qr_n=384,
                  big_lsqr_numel=1 << 23, engine="python"):
-        if precision not in ("mixed", "f64"):
+        if precision not in ("mixed", "f64", "f64_batched"):
             raise ValueError(f"unknown precision {precision!r}")
         if engine not in ("python", "capi"):
             raise ValueError(f"unknown engine {engine!r}")
@@ -55,7 +58,10 @@ class BatchedSPO:
         self.ptol = ptol
         self.iter_lim = iter_lim
         self.precision = precision
-        self.nstreams = streams if precision == "mixed" else 1
+        self.nstreams = streams if precision != "f64" else 1
+        # arithmetic of the batched LSQR: double-float on hi/lo planes, or
+        # binary64 on A
+        self.lsqr_mode = "f64" if precision == "f64_batched" else "df"
         self.tuner = tuner if tuner is not None else Tuner()
         self.max_refine = max_refine
         self.refine_kappa = refine_kappa
@@ -97,7 +103,7 @@ class BatchedSPO:
         seeds = [int(s) for s in rng.integers(0, 2 ** 62, size=len(problems))]
         if self.precision == "f64":
             return self._plain(problems, seeds)
-        if self.strategy == "refine":
+        if self.strategy == "refine" and self.precision == "mixed":
             return self._batched(problems, seeds)
         if self.engine == "capi":
             plan = self._capi_plan(problems, seeds)
@@ -142,8 +148,11 @@ class BatchedSPO:
             d = min(int(self.sf * n), m)
             nmax = max(nmax, n)
             it = dict(m=m, n=n, d=d, nnz=min(self.nnz, d), seed=seeds[i])
-            it["hi"] = torch.empty((m, n), dtype=torch.float32, device=dev)
-            it["lo"] = torch.empty((m, n), dtype=torch.float32, device=dev)
+            if self.lsqr_mode == "df":
+                it["hi"] = torch.empty((m, n), dtype=torch.float32, device=dev)
+                it["lo"] = torch.empty((m, n), dtype=torch.float32, device=dev)
+            else:
+                it["hi"] = it["lo"] = None
             it["T"] = torch.empty((n + 1, d), dtype=torch.float64, device=dev)
             it["Thi"] = torch.empty((n + 1, d), dtype=torch.float32, device=dev)
             it["Tlo"] = torch.empty((n + 1, d), dtype=torch.float32, device=dev)
@@ -188,8 +197,9 @@ class BatchedSPO:
         for j, i in enumerate(plan["order"]):
             it, (A, b) = items[i], problems[i]
             with torch.cuda.stream(streams[j % self.nstreams]):
-                _lib.call("rla_split_f64", it["m"], it["n"], K.ptr(A), A.stride(0), K.ptr(it["hi"]),
-                          K.ptr(it["lo"]), it["n"], K.stream())
+                if self.lsqr_mode == "df":
+                    _lib.call("rla_split_f64", it["m"], it["n"], K.ptr(A), A.stride(0), K.ptr(it["hi"]),
+                              K.ptr(it["lo"]), it["n"], K.stream())
                 rows, signs = K.sjlt_pattern(it["d"], it["m"], it["nnz"], it["seed"])
                 scale = 1.0 / math.sqrt(it["nnz"])
                 # exact (fixed-point) sketch of the binary64 A: with condition
@@ -228,7 +238,8 @@ class BatchedSPO:
         for i in plan["ls_big"]:
             it, (A, b) = items[i], problems[i]
             n = it["n"]
-            _lib.call("rla_lsqr_launch", K.MODES["df"], it["m"], n, n, None, K.ptr(it["hi"]), K.ptr(it["lo"]), n,
+            A_, hi, lo, lda = self._lsqr_operand(it, A)
+            _lib.call("rla_lsqr_launch", K.MODES[self.lsqr_mode], it["m"], n, n, A_, hi, lo, lda,
                       K.ptr(it["Rinv"]), n, 0.0, K.ptr(b), K.ptr(it["z"]), 1, 0.0, 0.0, 0.0, float(self.ptol),
                       int(self.iter_lim), 0, K.ptr(it["out"]), K.ptr(it["arn"]), None, K.ptr(it["coop_ws"]),
                       C.byref(C.c_size_t(it["coop_ws"].numel())), K.stream())
@@ -238,7 +249,7 @@ class BatchedSPO:
         for s, (ordt, cnt, nmx, g, ctas, nxt) in zip(cls_streams, plan["ls_classes"]):
             s.wait_stream(main)
             with torch.cuda.stream(s):
-                _lib.call("rla_lsqr_batched", K.MODES["df"], K.ptr(plan["ls_dev"]), K.ptr(ordt), cnt, nmx, g, ctas,
+                _lib.call("rla_lsqr_batched", K.MODES[self.lsqr_mode], K.ptr(plan["ls_dev"]), K.ptr(ordt), cnt, nmx, g, ctas,
                           K.ptr(nxt), K.stream())
         for s in cls_streams:
             main.wait_stream(s)
@@ -275,8 +286,8 @@ class BatchedSPO:
             if "Rinv" not in it:
                 it["Rinv"] = torch.empty((it["n"], it["n"]), dtype=torch.float64, device=K.device())
             rec = C.addressof(buf) + i * plan["ls_rec"]
-            _lib.call("rla_lsqr_record", C.c_void_p(rec), it["m"], it["n"], it["n"], None, K.ptr(it["hi"]),
-                      K.ptr(it["lo"]), it["n"], K.ptr(it["Rinv"]), it["n"], 0.0, K.ptr(b), K.ptr(it["z"]), 1,
+            A_, hi, lo, lda = self._lsqr_operand(it, A)
+            _lib.call("rla_lsqr_record", C.c_void_p(rec), it["m"], it["n"], it["n"], A_, hi, lo, lda, K.ptr(it["Rinv"]), it["n"], 0.0, K.ptr(b), K.ptr(it["z"]), 1,
                       0.0, 0.0, 0.0, float(self.ptol), int(self.iter_lim), K.ptr(it["out"]), K.ptr(it["arn"]),
                       None, K.ptr(it["x"]), K.ptr(it["ws"]))
         dev = K.device()
@@ -300,8 +311,9 @@ class BatchedSPO:
         for i in ls_big:
             it = items[i]
             n = it["n"]
-            need = _lib.size_query("rla_lsqr_launch", K.MODES["df"], it["m"], n, n, None, K.ptr(it["hi"]),
-                                   K.ptr(it["lo"]), n, K.ptr(it["Rinv"]), n, 0.0, K.ptr(plan["problems"][i][1]),
+            A_, hi, lo, lda = self._lsqr_operand(it, plan["problems"][i][0])
+            need = _lib.size_query("rla_lsqr_launch", K.MODES[self.lsqr_mode], it["m"], n, n, A_, hi, lo, lda,
+                                   K.ptr(it["Rinv"]), n, 0.0, K.ptr(plan["problems"][i][1]),
                                    K.ptr(it["z"]), 1, 0.0, 0.0, 0.0, float(self.ptol), int(self.iter_lim), 0,
                                    K.ptr(it["out"]), K.ptr(it["arn"]), None)
             it["coop_ws"] = torch.empty(max(need, 256), dtype=torch.uint8, device=dev)
@@ -393,15 +405,23 @@ class BatchedSPO:
                   C.byref(C.c_size_t(plan["hws"].numel())), K.stream())
         K.STATS.launches += 6 * plan["nprob"] + 4
 
-    @staticmethod
-    def layout_key(problems):
-        """Batch signature for the tuned layout: count and the log2 histogram of
-        element counts (the quantity the cluster rule reads)."""
+    def _lsqr_operand(self, it, A):
+        """(A, A_hi, A_lo, lda) pointers of the LSQR record: the hi/lo planes
+        (double-float) or A itself (binary64)."""
+        if self.lsqr_mode == "df":
+            return None, K.ptr(it["hi"]), K.ptr(it["lo"]), it["n"]
+        return K.ptr(A), None, None, A.stride(0)
+
+    def layout_key(self, problems):
+        """Batch signature for the tuned layout: the LSQR arithmetic, the count
+        and the log2 histogram of element counts (the quantity the cluster
+        rule reads)."""
         hist = {}
         for A, _ in problems:
             e = int(round(math.log2(max(A.numel(), 1))))
             hist[e] = hist.get(e, 0) + 1
-        return "layout:%d:%s" % (len(problems), ",".join(f"{k}x{v}" for k, v in sorted(hist.items())))
+        return "layout:%s:%d:%s" % (self.lsqr_mode, len(problems),
+                                    ",".join(f"{k}x{v}" for k, v in sorted(hist.items())))
 
     def tune_layout(self, problems, rng=0, reps=1):
         """Time every candidate LSQR layout (``LAYOUTS``) on this batch (each a
@@ -467,7 +487,7 @@ class BatchedSPO:
 
     def info_from_plan(self, plan):
         o = plan["outs"].cpu().numpy()
-        return [{"strategy": "df", "itn": int(r[0]), "istop": int(r[1]), "err": int(r[2])} for r in o]
+        return [{"strategy": self.lsqr_mode, "itn": int(r[0]), "istop": int(r[1]), "err": int(r[2])} for r in o]
 
     def _plain(self, problems, seeds):
         xs, info = [], []

@@ -65,6 +65,11 @@ class SVD1(SVDecomposer):
         caller has already made an eager call with these shapes)."""
         return SVDReplay(self, A, k, tol, over, rng, warm)
 
+    def stream(self, shape, k, tol, over, rng=0, depth=2):
+        """Pipelined calls on a sequence of pinned binary32 host matrices of
+        one shape (``SVDStream``); tensor-core chain only."""
+        return SVDStream(self, shape, k, tol, over, rng, depth)
+
 
 class SVDReplay:
     """An SVD1 call on the bf16 tensor-core chain captured as one CUDA graph.
@@ -116,15 +121,99 @@ class SVDReplay:
                 else:
                     self.out = (U, s, Vh)
         self.bad_host = torch.zeros(1, dtype=torch.int32).pin_memory()
+        self.done = torch.cuda.Event()
+        self.last_rng = rng
 
-    def replay(self, rng=None):
-        self.slots.set_from(self.rng if rng is None else rng)
+    def launch(self, rng=None):
+        """Enqueue one replay on the current stream (no synchronisation); the
+        outputs and the deferred checks' flag are ready when ``done`` is."""
+        self.last_rng = self.rng if rng is None else rng
+        self.slots.set_from(self.last_rng)
         self.graph.replay()
         self.bad_host.copy_(self.bad, non_blocking=True)
-        torch.cuda.current_stream().synchronize()
-        if int(self.bad_host[0]):
+        self.done.record()
+
+    def failed(self):
+        """After ``done``: True when the replay's deferred checks failed."""
+        return bool(int(self.bad_host[0]))
+
+    def replay(self, rng=None):
+        self.launch(rng)
+        self.done.synchronize()
+        if self.failed():
             k, tol, over = self.args
-            return self.svd(self.A, k, tol, over, self.rng if rng is None else rng)
+            return self.svd(self.A, k, tol, over, self.last_rng)
         return self.out
 
     __call__ = replay
+
+
+class SVDStream:
+    """SVD1 over a sequence of pinned binary32 host matrices of one shape,
+    with the host->device copy of the next matrix overlapping the
+    computation of the current one.
+
+    ``depth`` device input buffers each have their own captured call
+    (``SVDReplay`` on that buffer).  Per item: the copy engine brings the
+    matrix into the next free buffer on a copy stream; the compute stream
+    waits for that copy only, replays the buffer's graph; a third stream
+    copies U, s, Vh into the buffer's pinned host outputs.  A buffer is
+    reused only after its previous item's results were handed out, so with
+    ``depth`` = 2 the copy of item i + 1 runs during the computation of item i.
+    ``map(items)`` takes (A_host, rng) pairs and yields (U, s, Vh) host
+    tensors in order, each the result an ``svd(A_host, k, tol, over, rng)``
+    call gives (a replay whose deferred checks fail is redone eagerly).  The
+    yielded tensors belong to the buffer and are overwritten by the item
+    ``depth`` places later: copy them before resuming the generator.
+    """
+
+    def __init__(self, svd, shape, k, tol, over, rng=0, depth=2):
+        m, n = shape
+        self.svd, self.args, self.depth = svd, (k, tol, over), max(1, int(depth))
+        dev = K.device()
+        gen = torch.Generator(device=dev).manual_seed(12345)
+        self.dev = [torch.randn((m, n), generator=gen, device=dev) for _ in range(self.depth)]
+        self.reps = [SVDReplay(svd, d, k, tol, over, rng, warm=(b == 0)) for b, d in enumerate(self.dev)]
+        self.hout = [tuple(torch.empty(t.shape, dtype=t.dtype).pin_memory() for t in rep.out) for rep in self.reps]
+        self.copy_in = torch.cuda.Stream()
+        self.copy_out = torch.cuda.Stream()
+        self.loaded = [torch.cuda.Event() for _ in range(self.depth)]
+        self.fin = [torch.cuda.Event() for _ in range(self.depth)]
+        self.count = 0
+
+    def _submit(self, A_h, rng):
+        if not (isinstance(A_h, torch.Tensor) and A_h.is_pinned() and A_h.dtype == torch.float32
+                and tuple(A_h.shape) == tuple(self.dev[0].shape)):
+            raise ValueError("SVDStream takes pinned binary32 host tensors of the stream's shape")
+        b = self.count % self.depth
+        self.count += 1
+        main = torch.cuda.current_stream()
+        with torch.cuda.stream(self.copy_in):
+            self.dev[b].copy_(A_h, non_blocking=True)
+            self.loaded[b].record(self.copy_in)
+        main.wait_event(self.loaded[b])
+        rep = self.reps[b]
+        rep.launch(rng)
+        self.copy_out.wait_event(rep.done)
+        with torch.cuda.stream(self.copy_out):
+            for h, t in zip(self.hout[b], rep.out):
+                h.copy_(t, non_blocking=True)
+            self.fin[b].record(self.copy_out)
+        return b, A_h, rng
+
+    def _finish(self, b, A_h, rng):
+        self.fin[b].synchronize()
+        if self.reps[b].failed():
+            k, tol, over = self.args
+            return self.svd(A_h, k, tol, over, rng)
+        return self.hout[b]
+
+    def map(self, items):
+        from collections import deque
+        pending = deque()
+        for A_h, rng in items:
+            if len(pending) == self.depth:
+                yield self._finish(*pending.popleft())
+            pending.append(self._submit(A_h, rng))
+        while pending:
+            yield self._finish(*pending.popleft())

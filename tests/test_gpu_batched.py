@@ -29,7 +29,7 @@ def batch(pg):
     return probs, refs, shapes
 
 
-@pytest.mark.parametrize("precision", ["f64", "mixed"])
+@pytest.mark.parametrize("precision", ["f64", "mixed", "f64_batched"])
 def test_batched_spo_matches_lapack(pg, batch, tmp_path, precision):
     probs, refs, shapes = batch
     tuner = pg.Tuner(path=str(tmp_path / "tune.json"))
@@ -42,6 +42,9 @@ def test_batched_spo_matches_lapack(pg, batch, tmp_path, precision):
         assert info["err"] == 0
     if precision == "mixed":
         assert {i["strategy"] for i in solver.last_info} <= {"df", "refine"}
+    if precision == "f64_batched":
+        assert {i["strategy"] for i in solver.last_info} == {"f64"}
+        assert all(it["hi"] is None for it in solver.plan(probs, rng=3)["items"])
 
 
 def test_tuner_measures_and_caches(pg, tmp_path):
@@ -109,14 +112,14 @@ def hard_batch(pg):
     return items
 
 
-@pytest.mark.parametrize("route", ["call_mixed", "call_f64", "graph_replay"])
+@pytest.mark.parametrize("route", ["call_mixed", "call_f64", "graph_replay", "graph_replay_f64_batched"])
 def test_batched_hard_problems(pg, hard_batch, route):
     """BatchedSPO on inconsistent and large-residual problems, through the
     plain call and through a captured CUDA graph replayed twice (outputs
     poisoned with NaN before each replay), at the 1e-10 prediction gate."""
     probs = [(torch.from_numpy(A).cuda(), torch.from_numpy(b).cuda()) for _, A, b in hard_batch]
-    if route == "graph_replay":
-        solver = pg.BatchedSPO(precision="mixed", streams=4)
+    if route.startswith("graph_replay"):
+        solver = pg.BatchedSPO(precision="f64_batched" if route.endswith("f64_batched") else "mixed", streams=4)
         replay = solver.capture(probs, rng=9)
         for _ in range(2):
             for it in replay.plan["items"]:

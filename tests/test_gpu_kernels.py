@@ -51,10 +51,12 @@ def test_gemm(K, mode, tol, ta, tb, shape):
 
 @pytest.mark.parametrize("mode,tol", [("f64", 1e-13), ("df", 1e-12), ("f32", 2e-5)])
 @pytest.mark.parametrize("trans", [False, True])
-@pytest.mark.parametrize("n,k", [(5, 40), (64, 300), (130, 2000), (210, 8192)])
+@pytest.mark.parametrize("n,k", [(5, 40), (64, 300), (130, 2000), (210, 8192), (1, 1024), (9, 1100), (248, 3001)])
 def test_syrk_symmetric_gram(K, mode, tol, trans, n, k):
     """Upper tiles computed, lower tiles mirrored: equal to the full product
-    and symmetric (bitwise for binary32/64), with and without split-K."""
+    and symmetric (bitwise for binary32/64), with and without split-K (and,
+    binary32 A A^T with n <= 248 and k >= 1024, through the slice-per-CTA
+    kernel)."""
     rng = np.random.default_rng(n + k)
     A = rng.standard_normal((k, n) if trans else (n, k))
     dt = torch.float32 if mode == "f32" else torch.float64

@@ -87,3 +87,26 @@ def test_replay_falls_back_when_checks_fail(pg):
     Ue, se, Vhe = svd(A, 20, np.nan, 5, 1)
     assert s.shape == se.shape and U.shape == Ue.shape and Vh.shape == Vhe.shape
     assert torch.equal(s, se)
+
+
+def test_stream_matches_eager_per_item(pg):
+    """SVD1.stream over host matrices (two different ones alternating, a
+    zero matrix whose checks fail in between): every item equals the eager
+    call on that host matrix with that seed."""
+    A1 = _problem(2000, 1000, 3).cpu().pin_memory()
+    A2 = (_problem(2000, 1000, 4) * 3.0).cpu().pin_memory()
+    Z = torch.zeros((2000, 1000)).pin_memory()
+    svd = _chain(pg)
+    k, over = 40, 10
+    sv = svd.stream((2000, 1000), k, np.nan, over, 0)
+    items = [(A1, 5), (A2, 6), (Z, 7), (A1, 8), (A2, 9)]
+    got = [tuple(t.clone() for t in out) for out in sv.map(items)]
+    assert len(got) == len(items)
+    for (Ah, r), (U, s, Vh) in zip(items, got):
+        assert not U.is_cuda and not s.is_cuda and not Vh.is_cuda
+        Ue, se, Vhe = svd(Ah, k, np.nan, over, r)
+        assert s.shape == se.shape and U.shape == Ue.shape
+        if se.numel() == 0 or float(se.abs().max()) == 0.0:
+            assert torch.equal(s, se)
+        else:
+            assert _close(s, se) and _close(U, Ue) and _close(Vh, Vhe), r
