@@ -905,13 +905,19 @@ def run_case(args):
         for _ in range(3):
             K.sjlt_apply(rows, signs, 8, d, A, 8 ** -0.5)
     elif args.case == "small":
-        # the small dense kernels of one RSVD step at l = 210
+        # the small dense kernels of one RSVD step at l = 210: the binary32
+        # Grams of the final basis (210 x 16384) and of B (210 x 8192), the
+        # stabilizer's Cholesky + inverse, the Cholesky alone, the Jacobi SVD
         C = torch.randn((210, 210), generator=g, device="cuda")
         G = (C.double() @ C.double().t()).contiguous()
         G32 = G.float().contiguous()
+        Qt = torch.randn((K_RANK + OVER, M_ROWS), generator=g, device="cuda")
+        B = torch.randn((K_RANK + OVER, N_COLS), generator=g, device="cuda")
         for _ in range(3):
+            K.syrk(Qt, mode="f32")
+            K.syrk(B, mode="f32")
             K.chol_inv_f32(G32)
-            R = K.potrf_df_small(G)
+            R = K.chol_f32(G32)
             K.svd_jacobi(R)
     elif args.case == "spo":
         # three double-float sketch-and-precondition solves, A 20000 x 200 (kappa 1e8),
