@@ -467,14 +467,16 @@ namespace {
 // Binary32 Gram of a few long rows, G = A A^T for A (N x K), N <= 248, K
 // large (the l x n matrix B and the l x m final basis of the randomized SVD).
 // The 128 x 128 output tiles of the general kernel leave most SMs idle at
-// N ~ 200; here each CTA takes a slice of K (about K / #SMs columns), stages
-// it transposed in shared memory 32 columns at a time (cp.async, double
-// buffered), and computes the whole upper triangle of 8 x 8 tiles over it,
-// one or two tiles per thread (tiles enumerated row by row, so neighbouring
-// threads share the row operand).  The slices' partials (binary32) are
-// summed in slice order in binary64 by the reduce kernel, which mirrors the
-// tiles below the diagonal.
-constexpr int kGwKS = 32, kGwTh = 256, kGwMaxN = 248;
+// N ~ 200; here each CTA (one per SM) takes a slice of K (K / #SMs columns),
+// stages it transposed in shared memory 32 columns at a time (cp.async,
+// double buffered), and computes the whole upper triangle of 8 x 8 tiles over
+// it, one tile per thread (tiles enumerated row by row, so neighbouring
+// threads share the row operand; 512 threads for up to 496 tiles).  The
+// slices' partials (binary32) are summed in slice order by the reduce
+// kernel in double-float on the FP32 pipe (two-sum per partial; binary64
+// adds would run at 1/64 of the FP32 rate), which also mirrors the tiles
+// below the diagonal.
+constexpr int kGwKS = 32, kGwTh = 512, kGwMaxN = 248;
 
 __host__ __device__ inline int gw_tiles(int64_t N) { return static_cast<int>((N + 7) / 8); }
 __host__ __device__ inline int gw_ld(int64_t N) { return gw_tiles(N) * 8 + 4; }
@@ -485,23 +487,15 @@ __global__ void __launch_bounds__(kGwTh, 1) gram_rows_f32_kernel(int N, int64_t 
   extern __shared__ __align__(16) float As[];  // [2][kGwKS][NP]: column c of buffer b at As + (b kGwKS + c) NP
   const int nt = gw_tiles(N), NP = gw_ld(N), P = nt * (nt + 1) / 2;
   const int tid = threadIdx.x;
-  int ti[2], tj[2];
-  bool on[2];
+  const bool on = tid < P;
+  int p = tid, ti = 0;
+  while (on && p >= nt - ti) { p -= nt - ti; ++ti; }
+  const int tj = ti + p;
+  float acc[8][8];
 #pragma unroll
-  for (int s = 0; s < 2; ++s) {
-    int p = tid + s * kGwTh, r = 0;
-    on[s] = p < P;
-    while (on[s] && p >= nt - r) { p -= nt - r; ++r; }
-    ti[s] = r;
-    tj[s] = r + p;
-  }
-  float acc[2][8][8];
+  for (int a = 0; a < 8; ++a)
 #pragma unroll
-  for (int s = 0; s < 2; ++s)
-#pragma unroll
-    for (int a = 0; a < 8; ++a)
-#pragma unroll
-      for (int b = 0; b < 8; ++b) acc[s][a][b] = 0.f;
+    for (int b = 0; b < 8; ++b) acc[a][b] = 0.f;
   const int64_t k0 = static_cast<int64_t>(blockIdx.x) * kchunk, k1 = min(K, k0 + kchunk);
   const int rows = nt * 8;
   // chunk q of the slice -> buffer q & 1; lanes copy 32 consecutive columns of
@@ -526,71 +520,78 @@ __global__ void __launch_bounds__(kGwTh, 1) gram_rows_f32_kernel(int N, int64_t 
       cp_async_wait<0>();
     }
     __syncthreads();
-#pragma unroll 2
-    for (int c = 0; c < kGwKS; ++c) {
-      const float* col = As + (buf * kGwKS + c) * NP;
-#pragma unroll
-      for (int s = 0; s < 2; ++s) {
-        if (!on[s]) continue;
-        const float4 a0 = *reinterpret_cast<const float4*>(col + ti[s] * 8);
-        const float4 a1 = *reinterpret_cast<const float4*>(col + ti[s] * 8 + 4);
-        const float4 b0 = *reinterpret_cast<const float4*>(col + tj[s] * 8);
-        const float4 b1 = *reinterpret_cast<const float4*>(col + tj[s] * 8 + 4);
+    if (on) {
+#pragma unroll 4
+      for (int c = 0; c < kGwKS; ++c) {
+        const float* col = As + (buf * kGwKS + c) * NP;
+        const float4 a0 = *reinterpret_cast<const float4*>(col + ti * 8);
+        const float4 a1 = *reinterpret_cast<const float4*>(col + ti * 8 + 4);
+        const float4 b0 = *reinterpret_cast<const float4*>(col + tj * 8);
+        const float4 b1 = *reinterpret_cast<const float4*>(col + tj * 8 + 4);
         const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
         const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
 #pragma unroll
         for (int a = 0; a < 8; ++a)
 #pragma unroll
-          for (int b = 0; b < 8; ++b) acc[s][a][b] = fmaf(av[a], bv[b], acc[s][a][b]);
+          for (int b = 0; b < 8; ++b) acc[a][b] = fmaf(av[a], bv[b], acc[a][b]);
       }
     }
     __syncthreads();
   }
+  if (!on) return;
   float* out = part + static_cast<int64_t>(blockIdx.x) * N * N;
 #pragma unroll
-  for (int s = 0; s < 2; ++s) {
-    if (!on[s]) continue;
+  for (int a = 0; a < 8; ++a) {
+    const int i = ti * 8 + a;
+    if (i >= N) continue;
 #pragma unroll
-    for (int a = 0; a < 8; ++a) {
-      const int i = ti[s] * 8 + a;
-      if (i >= N) continue;
-#pragma unroll
-      for (int b = 0; b < 8; ++b) {
-        const int j = tj[s] * 8 + b;
-        if (j < N) out[static_cast<int64_t>(i) * N + j] = acc[s][a][b];
-      }
+    for (int b = 0; b < 8; ++b) {
+      const int j = tj * 8 + b;
+      if (j < N) out[static_cast<int64_t>(i) * N + j] = acc[a][b];
     }
   }
 }
 
-// C = alpha * sum_z part[z] + beta * C in slice order (binary64), entries of
-// tiles below the diagonal read from the mirror entry.  The loads of a group
-// of 32 slices are issued before their adds.
+// C = alpha * sum_z part[z] + beta * C in slice order for the entries of the
+// tiles on and above the diagonal (coalesced reads of the partials), written
+// to C[i][j] and to the mirror entry C[j][i] below the diagonal tiles.  The
+// sum is a double-float pair (hi, lo) on the FP32 pipe: each partial enters
+// hi by a two-sum, the rounding errors collect in lo.  The loads of a group
+// of 16 slices are issued before their adds.
 __global__ void gram_rows_reduce_kernel(int N, int splits, double alpha, const float* __restrict__ part, double beta,
                                         float* __restrict__ C, int64_t ldc) {
-  const int64_t idx = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (idx >= static_cast<int64_t>(N) * N) return;
-  const int i = static_cast<int>(idx / N), j = static_cast<int>(idx % N);
-  const bool mir = (i >> 3) > (j >> 3);
-  const int64_t off = mir ? static_cast<int64_t>(j) * N + i : static_cast<int64_t>(i) * N + j;
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= N * N) return;
+  const int i = idx / N, j = idx - i * N;
+  if ((i >> 3) > (j >> 3)) return;  // below the diagonal tiles: written by the mirror thread
+  const float* src = part + i * N + j;
   const int64_t stride = static_cast<int64_t>(N) * N;
-  constexpr int kU = 32;
-  double s = 0.0;
+  constexpr int kU = 16;
+  float hi = 0.f, lo = 0.f;
   for (int z0 = 0; z0 < splits; z0 += kU) {
     float v[kU];
 #pragma unroll
-    for (int u = 0; u < kU; ++u) v[u] = z0 + u < splits ? __ldcg(part + (z0 + u) * stride + off) : 0.f;
+    for (int u = 0; u < kU; ++u) v[u] = z0 + u < splits ? __ldcg(src + (z0 + u) * stride) : 0.f;
 #pragma unroll
-    for (int u = 0; u < kU; ++u) s += static_cast<double>(v[u]);
+    for (int u = 0; u < kU; ++u) {
+      const float t = hi + v[u], bb = t - hi;
+      lo += (hi - (t - bb)) + (v[u] - bb);
+      hi = t;
+    }
   }
-  double r = alpha * s;
+  const double sum = static_cast<double>(hi) + static_cast<double>(lo);
+  double r = alpha * sum;
   if (beta != 0.0) r += beta * static_cast<double>(C[static_cast<int64_t>(i) * ldc + j]);
   C[static_cast<int64_t>(i) * ldc + j] = static_cast<float>(r);
+  if ((i >> 3) < (j >> 3)) {
+    double rm = alpha * sum;
+    if (beta != 0.0) rm += beta * static_cast<double>(C[static_cast<int64_t>(j) * ldc + i]);
+    C[static_cast<int64_t>(j) * ldc + i] = static_cast<float>(rm);
+  }
 }
 
-inline int64_t gram_rows_kchunk(int64_t K) {
-  return imax(2 * kGwKS, ceil_div(ceil_div(imax(K, 1), sm_count()), kGwKS) * kGwKS);
-}
+// one slice of K per SM
+inline int64_t gram_rows_kchunk(int64_t K) { return imax(kGwKS, ceil_div(imax(K, 1), sm_count())); }
 
 int gram_rows_launch(int64_t N, int64_t K, double alpha, const float* A, int64_t lda, double beta, float* C,
                      int64_t ldc, void* ws, size_t* ws_bytes, cudaStream_t st) {

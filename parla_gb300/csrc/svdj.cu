@@ -422,47 +422,66 @@ __global__ void __launch_bounds__(512, 1) svd_jacobi_block_kernel(JacBArgs a) {
   unsigned seen = 0, rotated = 0;
   int cur = 0, sweeps = 0;
   bool converged = false;
+  // squared norm of a half-warp's column (E elements per lane, xor tree)
+  auto hw_norm2 = [&](const float (&v)[E]) {
+    float n0 = 0.f, n1 = 0.f;
+#pragma unroll
+    for (int e = 0; e < E; e += 2) {
+      n0 = fmaf(v[e], v[e], n0);
+      if (e + 1 < E) n1 = fmaf(v[e + 1], v[e + 1], n1);
+    }
+    float nn = n0 + n1;
+#pragma unroll
+    for (int o = 8; o > 0; o >>= 1) nn += __shfl_xor_sync(0xffffffffu, nn, o);
+    return __shfl_sync(0xffffffffu, nn, half * 16);
+  };
   while (!converged && sweeps < a.max_sweeps) {
+    // Each slot carries its column's squared norm in its padding (word 16 E),
+    // so it travels with the column between CTAs.  Exact at the start of a
+    // sweep; a rotation updates the pair's norms by app - t apq, aqq + t apq
+    // (recomputed from the rotated columns when either drops below a quarter).
+    for (int sb = 2 * warp; sb < b2; sb += 2 * (blockDim.x >> 5)) {  // warp-uniform trip count
+      const int sl = sb + half;
+      float v[E];
+      jac_load<E>(v, slot(cur, sl < b2 ? sl : 0) + hl * E, sl < b2);
+      const float nn = hw_norm2(v);
+      if (sl < b2 && hl == 0) slot(cur, sl)[16 * E] = nn;
+    }
+    __syncthreads();
     for (int orr = 0; orr < 2 * P - 1; ++orr) {
       const int lrounds = orr == 0 ? b2 - 1 : b;
+      // pair indices of round r, advanced by one per round (no division):
+      // first outer round ps = 1 + (hw - 1 + r) mod (2b - 1) (0 for hw = 0),
+      // qs = 1 + (2b - 2 - hw + r) mod (2b - 1); later ones ps = hw,
+      // qs = b + (hw + r) mod b
+      const int wrap = orr == 0 ? b2 - 1 : b;
+      int mp = hw == 0 ? 0 : hw - 1, mq = orr == 0 ? b2 - 2 - hw : hw;
       for (int r = 0; r < lrounds; ++r) {
         const bool act = hw < b;
-        int ps, qs;
-        if (orr == 0) {
-          ps = hw == 0 ? 0 : 1 + (hw - 1 + r) % (b2 - 1);
-          qs = 1 + (b2 - 2 - hw + r) % (b2 - 1);
-        } else {
-          ps = hw;
-          qs = b + (hw + r) % b;
-        }
+        const int ps = orr == 0 ? (hw == 0 ? 0 : 1 + mp) : hw;
+        const int qs = orr == 0 ? 1 + mq : b + mq;
+        if (++mp == wrap) mp = 0;
+        if (++mq == wrap) mq = 0;
         float* sx = slot(cur, act ? ps : 0);
         float* sy = slot(cur, act ? qs : 0);
         float x[E], y[E];
         jac_load<E>(x, sx + hl * E, act);
         jac_load<E>(y, sy + hl * E, act);
-        float app0 = 0.f, aqq0 = 0.f, apq0 = 0.f, app1 = 0.f, aqq1 = 0.f, apq1 = 0.f;
+        const float app = act ? sx[16 * E] : 1.f, aqq = act ? sy[16 * E] : 1.f;
+        float apq0 = 0.f, apq1 = 0.f;
 #pragma unroll
         for (int e = 0; e < E; e += 2) {
-          app0 = fmaf(x[e], x[e], app0);
-          aqq0 = fmaf(y[e], y[e], aqq0);
           apq0 = fmaf(x[e], y[e], apq0);
-          if (e + 1 < E) {
-            app1 = fmaf(x[e + 1], x[e + 1], app1);
-            aqq1 = fmaf(y[e + 1], y[e + 1], aqq1);
-            apq1 = fmaf(x[e + 1], y[e + 1], apq1);
-          }
+          if (e + 1 < E) apq1 = fmaf(x[e + 1], y[e + 1], apq1);
         }
-        float app = app0 + app1, aqq = aqq0 + aqq1, apq = apq0 + apq1;
+        float apq = apq0 + apq1;
 #pragma unroll
-        for (int o = 8; o > 0; o >>= 1) {
-          app += __shfl_xor_sync(0xffffffffu, app, o);
-          aqq += __shfl_xor_sync(0xffffffffu, aqq, o);
-          apq += __shfl_xor_sync(0xffffffffu, apq, o);
-        }
-        app = __shfl_sync(0xffffffffu, app, half * 16);
-        aqq = __shfl_sync(0xffffffffu, aqq, half * 16);
+        for (int o = 8; o > 0; o >>= 1) apq += __shfl_xor_sync(0xffffffffu, apq, o);
         apq = __shfl_sync(0xffffffffu, apq, half * 16);
-        if (act && apq * apq > tol2 * app * aqq) {
+        const bool rot = act && apq * apq > tol2 * app * aqq;
+        float np = app, nq = aqq;
+        bool renorm = false;
+        if (rot) {
           // t = tan(theta): approximate square root and quotients are enough
           // for the angle; c = 1/sqrt(1 + t^2) gets one Newton step, so the
           // rotation applied (c, s = t c) is orthogonal to working precision
@@ -484,7 +503,22 @@ __global__ void __launch_bounds__(512, 1) svd_jacobi_block_kernel(JacBArgs a) {
           }
           jac_store<E>(sx + hl * E, x);
           jac_store<E>(sy + hl * E, y);
+          np = fmaf(-t, apq, app);
+          nq = fmaf(t, apq, aqq);
+          renorm = np < 0.25f * app || nq < 0.25f * aqq;  // same in every lane of the half-warp
           if (hl == 0) ++rotated;
+        }
+        // (shuffles outside the divergent branch: the two half-warps differ)
+        if (__any_sync(0xffffffffu, renorm)) {
+          const float rp = hw_norm2(x), rq = hw_norm2(y);
+          if (renorm) {
+            np = rp;
+            nq = rq;
+          }
+        }
+        if (rot && hl == 0) {
+          sx[16 * E] = np;
+          sy[16 * E] = nq;
         }
         __syncthreads();
       }

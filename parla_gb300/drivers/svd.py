@@ -111,8 +111,9 @@ class SVDReplay:
                 Am = opd.wrap(A, svd.precision)         # inside: the bf16 images are part of the graph
                 U, s, Vh = svd._run(A, Am, k, tol, over, gen, graph=True)
                 bad = (s < eps10).any()
-                for f in chk.flags:
-                    bad = bad | (f != 0).any()
+                flags = chk.all_flags()
+                if flags is not None:
+                    bad = bad | (flags != 0).any()
                 self.bad = bad.to(torch.int32).reshape(1)
                 if self.host:
                     self.out = hout

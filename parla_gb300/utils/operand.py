@@ -27,10 +27,21 @@ class DeferredChecks:
     guarded (synchronising, shift-on-failure) path.
     """
 
+    POOL = 32
+
     def __init__(self):
-        self.flags = []
+        self.flags = []        # registered flags other than the pool's
+        self._pool = None      # int32[POOL], zeroed once per call (one fill)
+        self._used = 0
 
     def new_flag(self):
+        """A zeroed int32 device word for a kernel's status (non-zero = failed)."""
+        if self._pool is None:
+            self._pool = torch.zeros(self.POOL, dtype=torch.int32, device=K.device())
+        if self._used < self.POOL:
+            f = self._pool[self._used:self._used + 1]
+            self._used += 1
+            return f
         f = torch.zeros(1, dtype=torch.int32, device=K.device())
         self.flags.append(f)
         return f
@@ -39,10 +50,16 @@ class DeferredChecks:
         """Register an existing int32 device flag (non-zero = failed)."""
         self.flags.append(f.reshape(-1))
 
+    def all_flags(self):
+        """Every flag of the call as one int32 device vector (None: no flags)."""
+        parts = ([self._pool[:self._used]] if self._used else []) + self.flags
+        if not parts:
+            return None
+        return parts[0] if len(parts) == 1 else torch.cat(parts)
+
     def failed(self):
-        if not self.flags:
-            return False
-        return bool(torch.cat(self.flags).any().item())
+        flags = self.all_flags()
+        return False if flags is None else bool(flags.any().item())
 
 
 _tls = threading.local()
