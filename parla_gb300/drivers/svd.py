@@ -157,10 +157,13 @@ class SVDStream:
     ``depth`` device input buffers each have their own captured call
     (``SVDReplay`` on that buffer).  Per item: the copy engine brings the
     matrix into the next free buffer on a copy stream; the compute stream
-    waits for that copy only, replays the buffer's graph; a third stream
-    copies U, s, Vh into the buffer's pinned host outputs.  A buffer is
-    reused only after its previous item's results were handed out, so with
-    ``depth`` = 2 the copy of item i + 1 runs during the computation of item i.
+    waits for that copy only and replays the buffer's graph; an output
+    stream copies U, s, Vh into the buffer's pinned host outputs.  A buffer
+    is reused only after its previous item's results were handed out, so
+    with ``depth`` = 2 the copy of item i + 1 runs during the computation of
+    item i.  (The items' graphs run one after another: run side by side, the
+    passes' one-CTA-per-SM grids wait for the SMs that the other item's
+    small factorizations hold, and the pair measured slower.)
     ``map(items)`` takes (A_host, rng) pairs and yields (U, s, Vh) host
     tensors in order, each the result an ``svd(A_host, k, tol, over, rng)``
     call gives (a replay whose deferred checks fail is redone eagerly).  The
