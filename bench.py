@@ -992,9 +992,9 @@ def run_case(args):
         # every LSQR in the persistent cluster launches (as nearly all of the
         # 1024-problem batch's are)
         import parla_gb300 as pg
-        from parla_gb300.drivers.batched import batch_shapes, make_problem
+        from parla_gb300.drivers.batched import batch_shapes, make_problem as make_ls_problem
         shapes = batch_shapes(48, 7)
-        probs = [make_problem(m, n, kap, 1e-8, 1000 + i)[:2] for i, (m, n, kap) in enumerate(shapes)]
+        probs = [make_ls_problem(m, n, kap, 1e-8, 1000 + i)[:2] for i, (m, n, kap) in enumerate(shapes)]
         solver = pg.BatchedSPO(precision="mixed", streams=16, big_lsqr_numel=1 << 40)
         plan = solver.plan(probs, rng=5)
         solver._launch(plan)

@@ -626,10 +626,14 @@ def trtri_upper(R, mode=None):
 
 
 def split_f64(A):
+    """A = hi + lo (binary32 planes, to ~2^-48).  The planes' rows are padded
+    to 16 bytes (leading dimension n rounded up to 4; views of n columns), so
+    the double-float LSQR can stream them with 16-byte copies."""
     m, n = A.shape
-    hi = torch.empty((m, n), dtype=torch.float32, device=A.device)
-    lo = torch.empty((m, n), dtype=torch.float32, device=A.device)
-    _timed("split_f64", 1, call, "rla_split_f64", m, n, ptr(A), A.stride(0), ptr(hi), ptr(lo), n, stream())
+    ldp = (n + 3) // 4 * 4
+    hi = torch.empty((m, ldp), dtype=torch.float32, device=A.device)[:, :n]
+    lo = torch.empty((m, ldp), dtype=torch.float32, device=A.device)[:, :n]
+    _timed("split_f64", 1, call, "rla_split_f64", m, n, ptr(A), A.stride(0), ptr(hi), ptr(lo), ldp, stream())
     return hi, lo
 
 
@@ -690,7 +694,9 @@ def lsqr_run(A, M, b, z0, sqrt_delta, atol, btol, conlim, iter_lim, mode="f64", 
     hi, lo = split if split is not None else (None, None)
     if code == RLA_DF and split is None:
         hi, lo = split_f64(A)
-    head = (code, m, n, p, ptr(A), ptr(hi), ptr(lo), A.stride(0), ptr(M), M.stride(0), float(sqrt_delta),
+    # (double-float reads only the planes: their leading dimension)
+    lda = hi.stride(0) if code == RLA_DF else A.stride(0)
+    head = (code, m, n, p, ptr(A), ptr(hi), ptr(lo), lda, ptr(M), M.stride(0), float(sqrt_delta),
             ptr(b), ptr(z), int(z0 is not None), float(atol), float(btol), float(conlim), int(iter_lim),
             arn.ctypes.data_as(C.c_void_p), C.byref(itn), C.byref(istop),
             norms.ctypes.data_as(C.c_void_p) if norms is not None else None)

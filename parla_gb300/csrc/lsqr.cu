@@ -20,6 +20,7 @@
 //         double-float products and sums on the FP32 pipes: same 8 bytes per
 //         element of traffic, HBM-bound instead of FP64-bound.
 #include <cooperative_groups.h>
+#include <type_traits>
 
 #include "arith.cuh"
 
@@ -128,6 +129,12 @@ struct Scal {  // LSQR recurrence state (binary64, shared memory, advanced by th
   double rnorm, pred2, aphi1, aphi2;  // prediction-error rule: sum of phi^2, the last two |phi|
 };
 
+// 16-byte asynchronous global -> shared copy (cp.async.cg, L2 only).
+__device__ __forceinline__ void lsqr_cp16(float* dst, const float* src) {
+  const uint32_t d = static_cast<uint32_t>(__cvta_generic_to_shared(dst));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+}
+
 // Lane `lane`'s share of a strided sum: entries lane, lane+32, ... (< G) of
 // p[g * stride], added in that order.  The loads of a group of 16 are all
 // issued before the first add, so the sum costs one L2 round trip per 512
@@ -172,6 +179,9 @@ __device__ __forceinline__ void lsqr_body(const LsqrArgs& a, const int G, const 
   using R = P;
   using V = typename P::V;
   V* xs = reinterpret_cast<V*>(smem_raw);             // n entries: y or u chunk staging
+  // per-warp rings of staged rows of A (fused pass, double-float planes);
+  // the same bytes hold the cross-warp A^T u partials after the pass
+  float* stage_base = reinterpret_cast<float*>(smem_raw + ((a.n * static_cast<int64_t>(sizeof(V)) + 15) & ~int64_t(15)));
   __shared__ V red[32];
   __shared__ double redd[32];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
@@ -264,7 +274,10 @@ __device__ __forceinline__ void lsqr_body(const LsqrArgs& a, const int G, const 
     // a time, one group ahead, and passed along by shuffles, so no load
     // latency sits on a row's dependency chain.
     constexpr int NP = NPL > 0 ? NPL : 1;
-    constexpr int kDepth = NPL <= 2 ? 4 : NPL <= 4 ? 2 : NPL <= 8 ? 1 : 0;
+    // (the double-float variants with 8 or more columns per lane stream
+    // their rows through shared memory below instead)
+    constexpr bool kCanStage = std::is_same<V, df>::value && NPL >= 8;
+    constexpr int kDepth = kCanStage ? 0 : NPL <= 2 ? 4 : NPL <= 4 ? 2 : NPL <= 8 ? 1 : 0;
     auto load_row = [&](int64_t i, V (&dst)[NP]) {
 #pragma unroll
       for (int q = 0; q < NP; ++q) {
@@ -278,15 +291,59 @@ __device__ __forceinline__ void lsqr_body(const LsqrArgs& a, const int G, const 
       const int64_t row = r0 + warp + (k + lane) * nw;
       return row < r1 ? __ldcg(usrc + row) : 0.0;
     };
+    // Wide double-float rows (8 or 16 columns per lane, where registers for
+    // a row in flight are short) stream through a per-warp ring of two row
+    // slots in shared memory instead: the hi and lo rows of the next row are
+    // copied with 16-byte cp.async while this row is reduced (planes with a
+    // leading dimension that is a multiple of 4 and 16-byte aligned bases).
+    const bool staged = kCanStage && (a.lda & 3) == 0 &&
+                        ((reinterpret_cast<uintptr_t>(a.Ahi) | reinterpret_cast<uintptr_t>(a.Alo)) & 15) == 0;
+    const int n4 = static_cast<int>((a.n + 3) / 4);
+    float* const ring = stage_base + static_cast<int64_t>(warp) * 16 * n4;  // [2 slots][hi, lo][4 n4]
+    auto issue = [&](int64_t row, int slot) {
+      float* h = ring + slot * 8 * n4;
+      float* l = h + 4 * n4;
+      const float* gh = a.Ahi + row * a.lda;
+      const float* gl = a.Alo + row * a.lda;
+      for (int c = lane; c < n4; c += 32) {  // columns < 4 n4 <= lda: inside the row
+        lsqr_cp16(h + 4 * c, gh + 4 * c);
+        lsqr_cp16(l + 4 * c, gl + 4 * c);
+      }
+      asm volatile("cp.async.commit_group;" ::: "memory");
+    };
     V buf[kDepth + 1][NP];
     int64_t i = r0 + warp;
+    if (staged) {
+      if (i < r1) issue(i, 0);
+    } else {
 #pragma unroll
-    for (int d = 0; d < kDepth; ++d)
-      if (i + d * nw < r1) load_row(i + d * nw, buf[d]);
+      for (int d = 0; d < kDepth; ++d)
+        if (i + d * nw < r1) load_row(i + d * nw, buf[d]);
+    }
     double ucur = load_u(0), unext = load_u(32);
     for (int64_t k = 0; i < r1; i += nw, ++k) {
-      if (kDepth > 0 && i + kDepth * nw < r1) load_row(i + kDepth * nw, buf[kDepth]);
-      if (kDepth == 0) load_row(i, buf[0]);
+      if (staged) {
+        if constexpr (kCanStage) {
+          __syncwarp();  // every lane is done with the slot refilled next
+          if (i + nw < r1) {
+            issue(i + nw, static_cast<int>((k + 1) & 1));
+            asm volatile("cp.async.wait_group 1;" ::: "memory");
+          } else {
+            asm volatile("cp.async.wait_group 0;" ::: "memory");
+          }
+          __syncwarp();  // the other lanes' copies of this row have landed
+          const float* h = ring + static_cast<int>(k & 1) * 8 * n4;
+          const float* l = h + 4 * n4;
+#pragma unroll
+          for (int q = 0; q < NP; ++q) {
+            const int64_t j = lane + 32 * q;
+            buf[0][q] = j < a.n ? df{h[j], l[j]} : R::zero();
+          }
+        }
+      } else {
+        if (kDepth > 0 && i + kDepth * nw < r1) load_row(i + kDepth * nw, buf[kDepth]);
+        if (kDepth == 0) load_row(i, buf[0]);
+      }
       if ((k & 31) == 0 && k > 0) {
         ucur = unext;
         unext = load_u(k + 32);
@@ -326,7 +383,9 @@ __device__ __forceinline__ void lsqr_body(const LsqrArgs& a, const int G, const 
         part = R::fma(part, ue, ue);
       }
     }
-    // cross-warp sum of the A^T u partials (region after the y stage)
+    // cross-warp sum of the A^T u partials (region after the y stage; it
+    // overlaps the row rings, so every warp has left its ring first)
+    if (staged) __syncthreads();
     V* W = xs + a.n;
 #pragma unroll
     for (int q = 0; q < (NPL > 0 ? NPL : 1); ++q) {
@@ -730,8 +789,15 @@ inline LsqrWs lsqr_ws_layout(int64_t m, int64_t n, int64_t p, int G, int iter_li
 }
 inline size_t lsqr_smem_bytes(int64_t n, size_t vsize) {
   // y stage (n) + per-warp A^T u partials (8 warps x n), at least the
-  // 8 x 32 staging of the M^T t product
-  return static_cast<size_t>(imax(n + 8 * n, 256)) * vsize;
+  // 8 x 32 staging of the M^T t product; the partials' region also holds
+  // the per-warp row rings of the fused pass (8 warps x 2 slots x hi, lo
+  // rows of 4 ceil(n / 4) floats), after the y stage rounded to 16 bytes
+  const size_t base = static_cast<size_t>(imax(n + 8 * n, 256)) * vsize;
+  const size_t ys = (static_cast<size_t>(n) * vsize + 15) / 16 * 16;
+  const size_t rings = static_cast<size_t>(kLsqrThreads / 32) * 16 * static_cast<size_t>((n + 3) / 4) * sizeof(float);
+  const size_t parts = static_cast<size_t>(8 * n) * vsize;
+  const size_t staged = ys + (rings > parts ? rings : parts);
+  return base > staged ? base : staged;
 }
 
 template <class P>

@@ -79,7 +79,7 @@ __global__ void presolve_z_kernel(const ZRec* __restrict__ recs, int nprob) {
 }
 
 struct Item {
-  int64_t m, n, d;
+  int64_t m, n, d, ldp;  // ldp: row stride of the hi/lo planes (n rounded up to 4: 16-byte rows)
   int nnz;
   size_t hi, lo, rows, signs, Ask, bsk, T, Thi, Tlo, tau, Rinv, arn, lws, cws;  // device offsets
   size_t cws_bytes;
@@ -127,8 +127,9 @@ int build_plan(int nprob, const rla_ls_problem* probs, int sf, int vec_nnz, int 
     it.nnz = static_cast<int>(std::min<int64_t>(vec_nnz, it.d));
     P.dmax = std::max(P.dmax, it.d);
     P.nmax = std::max(P.nmax, it.n);
-    it.hi = take(off, sizeof(float) * it.m * it.n);
-    it.lo = take(off, sizeof(float) * it.m * it.n);
+    it.ldp = (it.n + 3) / 4 * 4;
+    it.hi = take(off, sizeof(float) * it.m * it.ldp);
+    it.lo = take(off, sizeof(float) * it.m * it.ldp);
     it.rows = take(off, sizeof(int32_t) * it.m * it.nnz);
     it.signs = take(off, sizeof(int8_t) * it.m * it.nnz);
     it.Ask = take(off, sizeof(double) * it.d * it.n);
@@ -281,7 +282,7 @@ extern "C" int rla_spo_batched(int nprob, const rla_ls_problem* probs, int sampl
             static_cast<double*>(dptr(it.tau))};
     std::memcpy(hb + P.z_rec + sizeof(ZRec) * i, &zr, sizeof(ZRec));
     rc = rla_lsqr_record(hb + P.ls_rec + ls_sz * i, it.m, it.n, it.n, nullptr,
-                         static_cast<const float*>(dptr(it.hi)), static_cast<const float*>(dptr(it.lo)), it.n,
+                         static_cast<const float*>(dptr(it.hi)), static_cast<const float*>(dptr(it.lo)), it.ldp,
                          static_cast<const double*>(dptr(it.Rinv)), it.n, 0.0, q.b,
                          static_cast<double*>(dptr(it.tau)), 1, 0.0, 0.0, 0.0, ptol, iter_lim, status + 3 * i,
                          static_cast<double*>(dptr(it.arn)), nullptr, q.x, dptr(it.lws));
@@ -336,7 +337,7 @@ extern "C" int rla_spo_batched(int nprob, const rla_ls_problem* probs, int sampl
     void* sjw = dptr(P.sj_off + P.sj_ws * (j % nss));
     size_t sjb = P.sj_ws;
     const double scale = 1.0 / std::sqrt(static_cast<double>(it.nnz));
-    if ((r = rla_split_f64(it.m, it.n, q.A, q.lda, hi, lo, it.n, rs))) break;
+    if ((r = rla_split_f64(it.m, it.n, q.A, q.lda, hi, lo, it.ldp, rs))) break;
     if ((r = rla_sjlt_pattern(it.d, it.m, it.nnz, q.seed, rows, signs, rs))) break;
     if ((r = rla_sjlt_apply(RLA_F64, it.d, it.m, it.n, it.nnz, rows, signs, scale, q.A, q.lda, dptr(it.Ask), it.n,
                             sjw, &sjb, rs)))
@@ -372,7 +373,7 @@ extern "C" int rla_spo_batched(int nprob, const rla_ls_problem* probs, int sampl
     const rla_ls_problem& q = probs[i];
     size_t cb = it.cws_bytes;
     r = rla_lsqr_launch(RLA_DF, it.m, it.n, it.n, nullptr, static_cast<const float*>(dptr(it.hi)),
-                        static_cast<const float*>(dptr(it.lo)), it.n, static_cast<const double*>(dptr(it.Rinv)), it.n,
+                        static_cast<const float*>(dptr(it.lo)), it.ldp, static_cast<const double*>(dptr(it.Rinv)), it.n,
                         0.0, q.b, static_cast<double*>(dptr(it.tau)), 1, 0.0, 0.0, 0.0, ptol, iter_lim, 0,
                         status + 3 * i, static_cast<double*>(dptr(it.arn)), nullptr, dptr(it.cws), &cb, stream);
     if (r) { cleanup(); return r; }

@@ -149,8 +149,10 @@ class BatchedSPO:
             nmax = max(nmax, n)
             it = dict(m=m, n=n, d=d, nnz=min(self.nnz, d), seed=seeds[i])
             if self.lsqr_mode == "df":
-                it["hi"] = torch.empty((m, n), dtype=torch.float32, device=dev)
-                it["lo"] = torch.empty((m, n), dtype=torch.float32, device=dev)
+                # rows padded to 16 bytes: the LSQR streams them with 16-byte copies
+                ldp = (n + 3) // 4 * 4
+                it["hi"] = torch.empty((m, ldp), dtype=torch.float32, device=dev)
+                it["lo"] = torch.empty((m, ldp), dtype=torch.float32, device=dev)
             else:
                 it["hi"] = it["lo"] = None
             it["T"] = torch.empty((n + 1, d), dtype=torch.float64, device=dev)
@@ -199,7 +201,7 @@ class BatchedSPO:
             with torch.cuda.stream(streams[j % self.nstreams]):
                 if self.lsqr_mode == "df":
                     _lib.call("rla_split_f64", it["m"], it["n"], K.ptr(A), A.stride(0), K.ptr(it["hi"]),
-                              K.ptr(it["lo"]), it["n"], K.stream())
+                              K.ptr(it["lo"]), it["hi"].stride(0), K.stream())
                 rows, signs = K.sjlt_pattern(it["d"], it["m"], it["nnz"], it["seed"])
                 scale = 1.0 / math.sqrt(it["nnz"])
                 # exact (fixed-point) sketch of the binary64 A: with condition
@@ -409,7 +411,7 @@ class BatchedSPO:
         """(A, A_hi, A_lo, lda) pointers of the LSQR record: the hi/lo planes
         (double-float) or A itself (binary64)."""
         if self.lsqr_mode == "df":
-            return None, K.ptr(it["hi"]), K.ptr(it["lo"]), it["n"]
+            return None, K.ptr(it["hi"]), K.ptr(it["lo"]), it["hi"].stride(0)
         return K.ptr(A), None, None, A.stride(0)
 
     def layout_key(self, problems):
