@@ -292,16 +292,17 @@ __device__ __forceinline__ void lsqr_body(const LsqrArgs& a, const int G, const 
       return row < r1 ? __ldcg(usrc + row) : 0.0;
     };
     // Wide double-float rows (8 or 16 columns per lane, where registers for
-    // a row in flight are short) stream through a per-warp ring of two row
-    // slots in shared memory instead: the hi and lo rows of the next row are
-    // copied with 16-byte cp.async while this row is reduced (planes with a
-    // leading dimension that is a multiple of 4 and 16-byte aligned bases).
+    // a row in flight are short) stream through a per-warp row slot in shared
+    // memory instead: once a row has been read out of the slot into
+    // registers, the hi and lo rows of the warp's next row are copied into it
+    // with 16-byte cp.async while this row is reduced (planes with a leading
+    // dimension that is a multiple of 4 and 16-byte aligned bases).
     const bool staged = kCanStage && (a.lda & 3) == 0 &&
                         ((reinterpret_cast<uintptr_t>(a.Ahi) | reinterpret_cast<uintptr_t>(a.Alo)) & 15) == 0;
     const int n4 = static_cast<int>((a.n + 3) / 4);
-    float* const ring = stage_base + static_cast<int64_t>(warp) * 16 * n4;  // [2 slots][hi, lo][4 n4]
-    auto issue = [&](int64_t row, int slot) {
-      float* h = ring + slot * 8 * n4;
+    float* const ring = stage_base + static_cast<int64_t>(warp) * 8 * n4;  // [hi, lo][4 n4]
+    auto issue = [&](int64_t row) {
+      float* h = ring;
       float* l = h + 4 * n4;
       const float* gh = a.Ahi + row * a.lda;
       const float* gl = a.Alo + row * a.lda;
@@ -314,7 +315,7 @@ __device__ __forceinline__ void lsqr_body(const LsqrArgs& a, const int G, const 
     V buf[kDepth + 1][NP];
     int64_t i = r0 + warp;
     if (staged) {
-      if (i < r1) issue(i, 0);
+      if (i < r1) issue(i);
     } else {
 #pragma unroll
       for (int d = 0; d < kDepth; ++d)
@@ -324,21 +325,17 @@ __device__ __forceinline__ void lsqr_body(const LsqrArgs& a, const int G, const 
     for (int64_t k = 0; i < r1; i += nw, ++k) {
       if (staged) {
         if constexpr (kCanStage) {
-          __syncwarp();  // every lane is done with the slot refilled next
-          if (i + nw < r1) {
-            issue(i + nw, static_cast<int>((k + 1) & 1));
-            asm volatile("cp.async.wait_group 1;" ::: "memory");
-          } else {
-            asm volatile("cp.async.wait_group 0;" ::: "memory");
-          }
+          asm volatile("cp.async.wait_group 0;" ::: "memory");
           __syncwarp();  // the other lanes' copies of this row have landed
-          const float* h = ring + static_cast<int>(k & 1) * 8 * n4;
+          const float* h = ring;
           const float* l = h + 4 * n4;
 #pragma unroll
           for (int q = 0; q < NP; ++q) {
             const int64_t j = lane + 32 * q;
             buf[0][q] = j < a.n ? df{h[j], l[j]} : R::zero();
           }
+          __syncwarp();  // every lane has read the slot: refill it with the next row
+          if (i + nw < r1) issue(i + nw);
         }
       } else {
         if (kDepth > 0 && i + kDepth * nw < r1) load_row(i + kDepth * nw, buf[kDepth]);
@@ -790,11 +787,11 @@ inline LsqrWs lsqr_ws_layout(int64_t m, int64_t n, int64_t p, int G, int iter_li
 inline size_t lsqr_smem_bytes(int64_t n, size_t vsize) {
   // y stage (n) + per-warp A^T u partials (8 warps x n), at least the
   // 8 x 32 staging of the M^T t product; the partials' region also holds
-  // the per-warp row rings of the fused pass (8 warps x 2 slots x hi, lo
-  // rows of 4 ceil(n / 4) floats), after the y stage rounded to 16 bytes
+  // the per-warp row slots of the fused pass (8 warps x hi, lo rows of
+  // 4 ceil(n / 4) floats), after the y stage rounded to 16 bytes
   const size_t base = static_cast<size_t>(imax(n + 8 * n, 256)) * vsize;
   const size_t ys = (static_cast<size_t>(n) * vsize + 15) / 16 * 16;
-  const size_t rings = static_cast<size_t>(kLsqrThreads / 32) * 16 * static_cast<size_t>((n + 3) / 4) * sizeof(float);
+  const size_t rings = static_cast<size_t>(kLsqrThreads / 32) * 8 * static_cast<size_t>((n + 3) / 4) * sizeof(float);
   const size_t parts = static_cast<size_t>(8 * n) * vsize;
   const size_t staged = ys + (rings > parts ? rings : parts);
   return base > staged ? base : staged;
