@@ -155,8 +155,9 @@ class SVDStream:
     computation of the current one.
 
     ``depth`` device input buffers each have their own captured call
-    (``SVDReplay`` on that buffer).  Per item: the copy engine brings the
-    matrix into the next free buffer on a copy stream; the compute stream
+    (``SVDReplay`` on that buffer).  Per item: the copy engines bring the
+    matrix into the next free buffer (four row blocks on four copy streams,
+    so that more than one engine serves the host link); the compute stream
     waits for that copy only and replays the buffer's graph; an output
     stream copies U, s, Vh into the buffer's pinned host outputs.  A buffer
     is reused only after its previous item's results were handed out, so
@@ -179,9 +180,9 @@ class SVDStream:
         self.dev = [torch.randn((m, n), generator=gen, device=dev) for _ in range(self.depth)]
         self.reps = [SVDReplay(svd, d, k, tol, over, rng, warm=(b == 0)) for b, d in enumerate(self.dev)]
         self.hout = [tuple(torch.empty(t.shape, dtype=t.dtype).pin_memory() for t in rep.out) for rep in self.reps]
-        self.copy_in = torch.cuda.Stream()
+        self.copy_in = [torch.cuda.Stream() for _ in range(4)]
         self.copy_out = torch.cuda.Stream()
-        self.loaded = [torch.cuda.Event() for _ in range(self.depth)]
+        self.loaded = [[torch.cuda.Event() for _ in self.copy_in] for _ in range(self.depth)]
         self.fin = [torch.cuda.Event() for _ in range(self.depth)]
         self.count = 0
 
@@ -192,10 +193,14 @@ class SVDStream:
         b = self.count % self.depth
         self.count += 1
         main = torch.cuda.current_stream()
-        with torch.cuda.stream(self.copy_in):
-            self.dev[b].copy_(A_h, non_blocking=True)
-            self.loaded[b].record(self.copy_in)
-        main.wait_event(self.loaded[b])
+        m = A_h.shape[0]
+        nc = len(self.copy_in)
+        for c, (cs, ev) in enumerate(zip(self.copy_in, self.loaded[b])):
+            r0, r1 = m * c // nc, m * (c + 1) // nc
+            with torch.cuda.stream(cs):
+                self.dev[b][r0:r1].copy_(A_h[r0:r1], non_blocking=True)
+                ev.record(cs)
+            main.wait_event(ev)
         rep = self.reps[b]
         rep.launch(rng)
         self.copy_out.wait_event(rep.done)
