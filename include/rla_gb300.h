@@ -224,11 +224,21 @@ int rla_gram_f32_df(int trans, int64_t N, int64_t K, const float* A,
  * is the sketch size: the R^-1 application of CholeskyQR on transposed
  * panels, Q^T = R^-T Y^T (`Q = Y R^-1`, parla/utils/linalg_wrappers.py:6-7,
  * as the stabilizer of parla/comps/sketchers/aware.py:124-184 uses it),
- * Vh = U^T B and U = Q Ub (parla/drivers/svd.py:164-172). */
+ * Vh = U^T B and U = Q Ub (parla/drivers/svd.py:164-172).  sdiv, when not
+ * NULL (device, c entries), divides row i of Y by sdiv[i] (rows with
+ * sdiv[i] <= 0 become zero): Vh = diag(1/s) U^T B in one pass. */
 int rla_gemm_tn_panel_f32(int tri, int64_t c, int64_t l, int64_t M,
                           const float* W, int64_t ldw, const float* X,
                           int64_t ldx, float* Y, int64_t ldy, void* Yb,
-                          int64_t ldyb, rla_stream_t stream);
+                          int64_t ldyb, const float* sdiv, rla_stream_t stream);
+
+/* *out (device int) = 1 if any of the nflags device status words is non-zero
+ * or any of the ns device values s is below smin (or NaN), else 0, in one
+ * launch: the deferred checks of a captured randomized SVD (the pivot and
+ * convergence flags of its small factorizations and the s < 10 eps
+ * truncation test of parla/drivers/svd.py:170-174). */
+int rla_flags_any(const int* flags, int64_t nflags, const float* s, int64_t ns,
+                  float smin, int* out, rla_stream_t stream);
 
 /* Tensor-core GEMM (tcgen05.mma kind::f16, TMA-fed, FP32 accumulation in
  * TMEM): D (M x N, fp32) = alpha X W^T + beta D with X (M x K) and W (N x K)
@@ -361,6 +371,16 @@ int rla_svd_jacobi(int dtype, int64_t n, const void* Ct, int64_t ldc, void* U, i
 int rla_chol_inv_f32(int64_t n, const float* G, int64_t ldg, float* Rinv,
                      int64_t ldr, float* R, int64_t ldro, int* info,
                      rla_stream_t stream);
+
+/* R (n x n, upper) of G = R^T R as rla_chol_inv_f32 without the inverse,
+ * with the scaled-pivot test of the binary32 small-SVD route: *info = j+1 if
+ * pivot j was not positive, n+1+j for the first j with
+ * R_jj^2 < min_ratio G_jj (the diagonally scaled Gram too ill-conditioned for
+ * binary32), else 0.  Replaces the Gram side of la.svd(B)
+ * (parla/drivers/svd.py:164) on that route. */
+int rla_chol_f32_checked(int64_t n, const float* G, int64_t ldg, float* R,
+                         int64_t ldr, float min_ratio, int* info,
+                         rla_stream_t stream);
 
 /* ------------------------------------------------------------- LSQR */
 

@@ -420,25 +420,42 @@ def chol_inv_f32(G, want_r=False, info=None):
     return (Rinv, R) if want_r else Rinv
 
 
-def gemm_tn_panel(W, X, tri=False, want_bf16=False):
+def gemm_tn_panel(W, X, tri=False, want_bf16=False, sdiv=None):
     """Y = W^T X for a small binary32 W (l x c) and a binary32 panel X (l x M)
     (``rla_gemm_tn_panel_f32``); ``tri``: W is upper triangular.  With
-    ``want_bf16`` also a bf16 copy of Y.  Returns Y, or (Y, Yb).  Rows of X
-    that are not 16-byte aligned (M or its stride not a multiple of 4) take
-    the general GEMM."""
+    ``want_bf16`` also a bf16 copy of Y; with ``sdiv`` (c values) row i of Y
+    is divided by sdiv[i] (zero where sdiv[i] <= 0).  Returns Y, or (Y, Yb).
+    Rows of X that are not 16-byte aligned (M or its stride not a multiple
+    of 4) take the general GEMM."""
     l, M = X.shape
     c = W.shape[1]
     assert W.shape[0] == l and W.dtype == torch.float32 and X.dtype == torch.float32
     W = W if W.stride(1) == 1 else W.contiguous()
     X = X if X.stride(1) == 1 else X.contiguous()
+    if sdiv is not None:
+        sdiv = sdiv if (sdiv.dtype == torch.float32 and sdiv.is_contiguous()) else sdiv.float().contiguous()
     if M % 4 or X.stride(0) % 4 or X.data_ptr() % 16:
         Y = gemm((torch.triu(W) if tri else W).contiguous(), X.contiguous(), transa=True, mode="f32")
+        if sdiv is not None:
+            Y = Y * torch.where(sdiv > 0, 1.0 / sdiv, torch.zeros_like(sdiv))[:, None]
         return (Y, convert(Y, torch.bfloat16)) if want_bf16 else Y
     Y = torch.empty((c, M), dtype=torch.float32, device=X.device)
     Yb = empty_bf16(c, M, X.device) if want_bf16 else None
     _timed("gemm_panel", 1, call, "rla_gemm_tn_panel_f32", int(tri), c, l, M, ptr(W), W.stride(0), ptr(X), X.stride(0),
-           ptr(Y), Y.stride(0), ptr(Yb), Yb.stride(0) if Yb is not None else 0, stream())
+           ptr(Y), Y.stride(0), ptr(Yb), Yb.stride(0) if Yb is not None else 0, ptr(sdiv), stream())
     return (Y, Yb) if want_bf16 else Y
+
+
+def flags_any(flags, s=None, smin=0.0):
+    """Device int32 [1]: 1 if any flag is non-zero or any s is below smin
+    (``rla_flags_any``, one launch)."""
+    out = torch.empty(1, dtype=torch.int32, device=device())
+    nf = 0 if flags is None else flags.numel()
+    if s is not None:
+        s = s if (s.dtype == torch.float32 and s.is_contiguous()) else s.float().contiguous()
+    _timed("flags_any", 1, call, "rla_flags_any", ptr(flags) if nf else None, nf, ptr(s) if s is not None else None,
+           0 if s is None else s.numel(), C.c_float(smin), ptr(out), stream())
+    return out
 
 
 def gram_f32_df(A, trans=False):
@@ -456,18 +473,27 @@ def gram_f32_df(A, trans=False):
     return G
 
 
-def chol_f32(G, info=None):
+def chol_f32(G, info=None, min_ratio=0.0):
     """Upper Cholesky factor R of an FP32 SPD G (n <= 216), one CTA, without
-    the inverse (``rla_chol_inv_f32`` with Rinv = NULL).  Returns None when n
-    is too large.  ``info`` as in chol_inv_f32."""
+    the inverse.  Returns None when n is too large.  ``info`` as in
+    chol_inv_f32.  With ``min_ratio`` > 0 the scaled pivots are checked too
+    (``rla_chol_f32_checked``): the flag is n + 1 + j for the first j with
+    R_jj^2 < min_ratio G_jj; without ``info`` that case returns None."""
     n = G.shape[0]
     if n > 216:
         return None
     R = torch.empty((n, n), dtype=torch.float32, device=G.device)
     inf = info if info is not None else torch.zeros(1, dtype=torch.int32, device=G.device)
-    _timed("chol_f32", 1, call, "rla_chol_inv_f32", n, ptr(G), G.stride(0), None, n, ptr(R), n, ptr(inf), stream())
+    if min_ratio > 0.0:
+        _timed("chol_f32", 1, call, "rla_chol_f32_checked", n, ptr(G), G.stride(0), ptr(R), n,
+               C.c_float(min_ratio), ptr(inf), stream())
+    else:
+        _timed("chol_f32", 1, call, "rla_chol_inv_f32", n, ptr(G), G.stride(0), None, n, ptr(R), n, ptr(inf),
+               stream())
     if info is None:
         bad = int(inf.item())
+        if bad > n:
+            return None
         if bad:
             raise _lib.RlaError("rla_chol_inv_f32", 3, f"pivot {bad - 1} not positive")
     return R

@@ -57,7 +57,8 @@ SIGNATURES = {
     "rla_gemm": [_i32, _i32, _i32, _i64, _i64, _i64, _f64, _p, _i64, _p, _i64, _f64, _p, _i64, _p, _psz, _p],
     "rla_syrk": [_i32, _i32, _i64, _i64, _f64, _p, _i64, _f64, _p, _i64, _p, _psz, _p],
     "rla_gram_f32_df": [_i32, _i64, _i64, _p, _i64, _p, _i64, _p, _psz, _p],
-    "rla_gemm_tn_panel_f32": [_i32, _i64, _i64, _i64, _p, _i64, _p, _i64, _p, _i64, _p, _i64, _p],
+    "rla_gemm_tn_panel_f32": [_i32, _i64, _i64, _i64, _p, _i64, _p, _i64, _p, _i64, _p, _i64, _p, _p],
+    "rla_flags_any": [_p, _i64, _p, _i64, C.c_float, _p, _p],
     "rla_gemm_bf16_tc": [_i64, _i64, _i64, _p, _i64, _p, _i64, _p, _i64, _i32, C.c_float, C.c_float, _i32,
                          _p, _psz, _p],
     "rla_gemm_bf16_tc_status": [_p, C.POINTER(C.c_int), _p],
@@ -81,6 +82,7 @@ SIGNATURES = {
     "rla_orgqr": [_i32, _i64, _i64, _p, _i64, _p, _p, _i64, _p, _psz, _p],
     "rla_potrf_upper": [_i32, _i64, _p, _i64, _p, _p, _psz, _p],
     "rla_chol_inv_f32": [_i64, _p, _i64, _p, _i64, _p, _i64, _p, _p],
+    "rla_chol_f32_checked": [_i64, _p, _i64, _p, _i64, C.c_float, _p, _p],
     "rla_potrf_df_small": [_i64, _p, _i64, _p, _i64, _p, _i64, _p, _p],
     "rla_col_sumsq": [_i64, _i64, _p, _i64, _p, _p],
     "rla_rbf_kernel_matrix": [_i64, _i32, _p, _i64, C.c_float, _i32, _p, _i64, _p, _p, _i64, _p],

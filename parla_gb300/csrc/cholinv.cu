@@ -180,7 +180,7 @@ __device__ void ci_trailing(float* a, const float* P, int LD, int n, int t0, int
 template <bool INV>
 __global__ void __launch_bounds__(kCiThreads, 1)
 chol_inv_kernel(int n, const float* __restrict__ G, int64_t ldg, float* __restrict__ Rinv, int64_t ldr,
-                float* __restrict__ Rout, int64_t ldro, int* __restrict__ info) {
+                float* __restrict__ Rout, int64_t ldro, int* __restrict__ info, float min_ratio) {
   extern __shared__ __align__(16) float smem[];
   const int LD = ci_ld(n), PC = ci_pcols(n);
   float* a = smem;                    // upper: G -> R;  strictly lower: L = R^-T (INV)
@@ -188,7 +188,7 @@ chol_inv_kernel(int n, const float* __restrict__ G, int64_t ldg, float* __restri
   float* const P1 = P0 + kNB * PC;
   float* Dv = a + n * LD + 2 * kNB * PC;  // R_d^-T of the block being factored, kNB x kNB
   float* dl = Dv + kNB * kNB;         // diagonal of L
-  __shared__ int s_bad;
+  __shared__ int s_bad, s_scaled;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = kCiThreads >> 5;
   const bool group_a = tid < kCiGroup;
 
@@ -217,6 +217,16 @@ chol_inv_kernel(int n, const float* __restrict__ G, int64_t ldg, float* __restri
     if (tid == 0) *info = s_bad;
     return;
   }
+  if (min_ratio > 0.f) {  // scaled pivots: R_jj^2 >= min_ratio G_jj, first failure reported
+    if (tid == 0) s_scaled = n;
+    __syncthreads();
+    for (int r = tid; r < n; r += kCiThreads) {
+      const float d = a[r * LD + r];
+      if (!(d * d >= min_ratio * G[static_cast<int64_t>(r) * ldg + r])) atomicMin(&s_scaled, r);
+    }
+    __syncthreads();
+    if (tid == 0 && s_scaled < n) *info = n + 1 + s_scaled;
+  }
   if (Rout) {
     for (int r = warp; r < n; r += nw)
       for (int c = lane; c < n; c += 32) Rout[static_cast<int64_t>(r) * ldro + c] = c >= r ? a[r * LD + c] : 0.f;
@@ -231,6 +241,25 @@ chol_inv_kernel(int n, const float* __restrict__ G, int64_t ldg, float* __restri
 }  // namespace
 }  // namespace rla
 
+namespace rla {
+namespace {
+// Raise the dynamic shared-memory limit of both instantiations, once per
+// device and thread.
+int ci_attributes() {
+  static thread_local int attr_dev = -1;
+  int dev = 0;
+  RLA_CUDA_TRY(cudaGetDevice(&dev));
+  if (attr_dev != dev) {
+    const int cap = static_cast<int>(ci_smem_bytes(kCholInvMax));
+    RLA_CUDA_TRY(cudaFuncSetAttribute(chol_inv_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
+    RLA_CUDA_TRY(cudaFuncSetAttribute(chol_inv_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
+    attr_dev = dev;
+  }
+  return RLA_OK;
+}
+}  // namespace
+}  // namespace rla
+
 extern "C" int rla_chol_inv_f32(int64_t n, const float* G, int64_t ldg, float* Rinv, int64_t ldr, float* R,
                                 int64_t ldro, int* info, rla_stream_t stream) {
   using namespace rla;
@@ -241,19 +270,31 @@ extern "C" int rla_chol_inv_f32(int64_t n, const float* G, int64_t ldg, float* R
   if (n == 0) return RLA_OK;
   if (!G) return RLA_ERR_ARG;
   const size_t smem = ci_smem_bytes(static_cast<int>(n));
-  static thread_local int attr_dev = -1;
-  int dev = 0;
-  RLA_CUDA_TRY(cudaGetDevice(&dev));
-  if (attr_dev != dev) {  // raise the dynamic smem limit once per device and thread
-    const int cap = static_cast<int>(ci_smem_bytes(kCholInvMax));
-    RLA_CUDA_TRY(cudaFuncSetAttribute(chol_inv_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
-    RLA_CUDA_TRY(cudaFuncSetAttribute(chol_inv_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
-    attr_dev = dev;
-  }
+  const int rc = ci_attributes();
+  if (rc != RLA_OK) return rc;
   if (Rinv)
-    chol_inv_kernel<true><<<1, kCiThreads, smem, st>>>(static_cast<int>(n), G, ldg, Rinv, ldr, R, ldro, info);
+    chol_inv_kernel<true><<<1, kCiThreads, smem, st>>>(static_cast<int>(n), G, ldg, Rinv, ldr, R, ldro, info, 0.f);
   else
-    chol_inv_kernel<false><<<1, kCiThreads, smem, st>>>(static_cast<int>(n), G, ldg, nullptr, 0, R, ldro, info);
+    chol_inv_kernel<false><<<1, kCiThreads, smem, st>>>(static_cast<int>(n), G, ldg, nullptr, 0, R, ldro, info, 0.f);
+  RLA_LAUNCH_CHECK();
+  return RLA_OK;
+}
+
+// R only, with the scaled-pivot check: *info = j + 1 if pivot j was not
+// positive, n + 1 + j for the first j with R_jj^2 < min_ratio G_jj, else 0.
+extern "C" int rla_chol_f32_checked(int64_t n, const float* G, int64_t ldg, float* R, int64_t ldr, float min_ratio,
+                                    int* info, rla_stream_t stream) {
+  using namespace rla;
+  if (n < 0 || ldg < n || ldr < n || !info || !R) return RLA_ERR_ARG;
+  if (n > kCholInvMax) return RLA_ERR_UNSUPPORTED;
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  RLA_CUDA_TRY(cudaMemsetAsync(info, 0, sizeof(int), st));
+  if (n == 0) return RLA_OK;
+  if (!G) return RLA_ERR_ARG;
+  const int rc = ci_attributes();
+  if (rc != RLA_OK) return rc;
+  chol_inv_kernel<false><<<1, kCiThreads, ci_smem_bytes(static_cast<int>(n)), st>>>(
+      static_cast<int>(n), G, ldg, nullptr, 0, R, ldr, info, min_ratio);
   RLA_LAUNCH_CHECK();
   return RLA_OK;
 }

@@ -795,7 +795,7 @@ constexpr int kTpBM = 64, kTpBN = 256, kTpBK = 16, kTpThreads = 256;
 __global__ void __launch_bounds__(kTpThreads, 2)
 gemm_tn_panel_kernel(int tri, int cdim, int l, int64_t M, const float* __restrict__ R, int64_t ldr,
                      const float* __restrict__ X, int64_t ldx, float* __restrict__ Y, int64_t ldy,
-                     __nv_bfloat16* __restrict__ Yb, int64_t ldyb) {
+                     __nv_bfloat16* __restrict__ Yb, int64_t ldyb, const float* __restrict__ sdiv) {
   __shared__ __align__(16) float Ls[2][kTpBK][kTpBM];  // Ls[b][kk][i] = W[k0 + kk][i0 + i]
   __shared__ __align__(16) float Xs[2][kTpBK][kTpBN];
   const int tid = threadIdx.x, ty = tid >> 5, tx = tid & 31;
@@ -861,6 +861,12 @@ gemm_tn_panel_kernel(int tri, int cdim, int l, int64_t M, const float* __restric
   for (int a = 0; a < 8; ++a) {
     const int i = i0 + 8 * ty + a;
     if (i >= cdim) continue;
+    if (sdiv) {  // row i of Y divided by sdiv[i] (0 where sdiv[i] <= 0)
+      const float d = sdiv[i];
+      const float f = d > 0.f ? 1.f / d : 0.f;
+#pragma unroll
+      for (int c = 0; c < 8; ++c) acc[a][c] *= f;
+    }
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
       const int64_t j = j0 + 128 * h + 4 * tx;
@@ -885,7 +891,7 @@ gemm_tn_panel_kernel(int tri, int cdim, int l, int64_t M, const float* __restric
 
 extern "C" int rla_gemm_tn_panel_f32(int tri, int64_t c, int64_t l, int64_t M, const float* W, int64_t ldw,
                                      const float* X, int64_t ldx, float* Y, int64_t ldy, void* Yb, int64_t ldyb,
-                                     rla_stream_t stream) {
+                                     const float* sdiv, rla_stream_t stream) {
   using namespace rla;
   if (c < 0 || l < 0 || M < 0 || ldw < c || ldx < M || ldy < M || (Yb && ldyb < M) || (tri && c > l))
     return RLA_ERR_ARG;
@@ -898,7 +904,33 @@ extern "C" int rla_gemm_tn_panel_f32(int tri, int64_t c, int64_t l, int64_t M, c
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   dim3 grid(static_cast<unsigned>(ceil_div(M, kTpBN)), static_cast<unsigned>(ceil_div(c, kTpBM)));
   gemm_tn_panel_kernel<<<grid, kTpThreads, 0, st>>>(tri ? 1 : 0, static_cast<int>(c), static_cast<int>(l), M, W, ldw,
-                                                    X, ldx, Y, ldy, static_cast<__nv_bfloat16*>(Yb), ldyb);
+                                                    X, ldx, Y, ldy, static_cast<__nv_bfloat16*>(Yb), ldyb, sdiv);
+  RLA_LAUNCH_CHECK();
+  return RLA_OK;
+}
+
+// ---------------------------------------------------------------------------
+// *out = 1 if any of the nflags status words is non-zero or any of the ns
+// values s is below smin (NaN counts as below), else 0: the deferred checks
+// of a captured call reduced in one launch.
+namespace rla {
+namespace {
+__global__ void __launch_bounds__(256) flags_any_kernel(const int* __restrict__ flags, int64_t nflags,
+                                                        const float* __restrict__ s, int64_t ns, float smin,
+                                                        int* __restrict__ out) {
+  int bad = 0;
+  for (int64_t i = threadIdx.x; i < nflags; i += blockDim.x) bad |= flags[i] != 0;
+  for (int64_t i = threadIdx.x; i < ns; i += blockDim.x) bad |= !(s[i] >= smin);
+  bad = __syncthreads_or(bad);
+  if (threadIdx.x == 0) *out = bad ? 1 : 0;
+}
+}  // namespace
+}  // namespace rla
+
+extern "C" int rla_flags_any(const int* flags, int64_t nflags, const float* s, int64_t ns, float smin, int* out,
+                             rla_stream_t stream) {
+  if (nflags < 0 || ns < 0 || !out || (nflags > 0 && !flags) || (ns > 0 && !s)) return RLA_ERR_ARG;
+  rla::flags_any_kernel<<<1, 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(flags, nflags, s, ns, smin, out);
   RLA_LAUNCH_CHECK();
   return RLA_OK;
 }

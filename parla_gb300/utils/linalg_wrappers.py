@@ -115,20 +115,17 @@ def _svd_gram_f32(B, trans):
     G = K.syrk(B, trans=trans, mode="f32")   # (trans: B^T B for a tall B)
     chk = current_checks()
     if chk is not None:
-        flag = chk.new_flag()
-        R = K.chol_f32(G, info=flag)
-        # (the check reads R only where the Cholesky succeeded; a failed one raised flag)
-        ratio = torch.diagonal(R) ** 2 / torch.diagonal(G).clamp_min(1e-300)
-        chk.add_flag((ratio.min() < SCALED_PIVOT_MIN).to(torch.int32).reshape(1))
+        # one flag for both tests: a non-positive pivot, or a scaled pivot
+        # R_jj^2 / G_jj below SCALED_PIVOT_MIN (checked inside the kernel)
+        R = K.chol_f32(G, info=chk.new_flag(), min_ratio=SCALED_PIVOT_MIN)
         U, s, inf = K.svd_jacobi(R)
         chk.add_flag(inf[:1])
         return U, s
     try:
-        R = K.chol_f32(G)
+        R = K.chol_f32(G, min_ratio=SCALED_PIVOT_MIN)
     except RlaError:
         return None
-    ratio = float((torch.diagonal(R) ** 2 / torch.diagonal(G).clamp_min(1e-300)).min())
-    if not ratio >= SCALED_PIVOT_MIN:
+    if R is None:
         return None
     U, s, inf = K.svd_jacobi(R)
     if int(inf[0].item()):
@@ -150,8 +147,7 @@ def small_svd_wide(B):
         res = _svd_gram_f32(B, trans=False)
         if res is not None:
             U, s = res
-            inv = torch.where(s > 0, 1.0 / s, torch.zeros_like(s))
-            Vh = K.gemm_tn_panel(U, B) * inv[:, None]
+            Vh = K.gemm_tn_panel(U, B, sdiv=s)   # diag(1/s) U^T B (rows with s = 0 zero)
             return U, s, Vh
     G = K.gram_f32_df(B) if B.dtype == torch.float32 else K.syrk(B, mode="df")
     if B.dtype == torch.float32 and B.shape[0] <= JACOBI_MAX:

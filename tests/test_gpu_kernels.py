@@ -121,6 +121,57 @@ def test_gemm_tn_panel(K, tri, l, c, M):
     assert torch.equal(Yb, Y.to(torch.bfloat16))
 
 
+@pytest.mark.parametrize("M", [8192, 1001])
+def test_gemm_tn_panel_row_divide(K, M):
+    """sdiv: row i of Y = W^T X divided by sdiv[i], zero rows where sdiv <= 0
+    (the Vh = diag(1/s) U^T B of the small SVD in one pass)."""
+    rng = np.random.default_rng(M)
+    l = c = 60
+    W = rng.standard_normal((l, c)).astype(np.float32)
+    X = rng.standard_normal((l, M)).astype(np.float32)
+    sd = np.abs(rng.standard_normal(c)).astype(np.float32) + 0.1
+    sd[[3, 17]] = 0.0
+    sd[40] = -1.0
+    Y = K.gemm_tn_panel(dev(W), dev(X), sdiv=dev(sd)).cpu().numpy()
+    inv = np.where(sd > 0, 1.0 / np.maximum(sd, 1e-30), 0.0)
+    ref = (W.astype(np.float64).T @ X.astype(np.float64)) * inv[:, None]
+    assert rel(Y, ref) <= 2e-6 * np.sqrt(l)
+    assert np.all(Y[[3, 17, 40]] == 0.0)
+
+
+def test_chol_f32_checked_scaled_pivots(K):
+    """rla_chol_f32_checked: R equal to the unchecked Cholesky's; the flag is
+    n + 1 + j for the first scaled pivot R_jj^2 / G_jj below min_ratio."""
+    rng = np.random.default_rng(5)
+    n = 100
+    X = rng.standard_normal((3 * n, n))
+    G = (X.T @ X).astype(np.float32)
+    R0 = K.chol_f32(dev(G))
+    flag = torch.zeros(1, dtype=torch.int32, device="cuda")
+    R1 = K.chol_f32(dev(G), info=flag, min_ratio=1e-2)
+    assert int(flag.item()) == 0 and torch.equal(R0, R1)
+    # make column 37 nearly a combination of the first ones: its scaled pivot collapses
+    X2 = X.copy()
+    X2[:, 37] = X2[:, :5].sum(axis=1) + 1e-3 * X2[:, 37]
+    G2 = (X2.T @ X2).astype(np.float32)
+    R2 = K.chol_f32(dev(G2), info=flag, min_ratio=1e-2)
+    d = torch.diagonal(R2).double().cpu().numpy() ** 2 / np.diag(G2).astype(np.float64)
+    first = int(np.argmax(d < 1e-2))
+    assert d[first] < 1e-2 and int(flag.item()) == n + 1 + first
+    assert K.chol_f32(dev(G2), min_ratio=1e-2) is None   # synchronising form
+
+
+def test_flags_any(K):
+    f = torch.zeros(5, dtype=torch.int32, device="cuda")
+    s = torch.tensor([3.0, 2.0, 1e-3], device="cuda")
+    assert int(K.flags_any(f, s, 1e-6).item()) == 0
+    assert int(K.flags_any(f, s, 1e-2).item()) == 1
+    f[3] = 7
+    assert int(K.flags_any(f, s, 1e-6).item()) == 1
+    assert int(K.flags_any(None, torch.tensor([1.0, float("nan")], device="cuda"), 0.0).item()) == 1
+    assert int(K.flags_any(None, None, 0.0).item()) == 0
+
+
 def test_gemm_alpha_beta(K):
     rng = np.random.default_rng(3)
     A, B, Cm = rng.standard_normal((50, 40)), rng.standard_normal((40, 30)), rng.standard_normal((50, 30))
