@@ -123,6 +123,13 @@ def chain(pg, precision="bf16"):
     return pg.SVD1(pg.QB1(pg.RF1(pg.RS1(pg.SkOpGA(), NUM_PASS))), precision=precision)
 
 
+def _config(world):
+    """The workload configuration, identical in both arms."""
+    return {"workload": "SVD1(QB1(RF1(RS1(SkOpGA, num_pass=4)))) on A 16384x8192 fp32, k=200, over=10",
+            "global_batch": world, "seq_len": 0,
+            "parallelism": "single GPU" if world == 1 else f"{world} independent replicas (one RSVD per GPU)"}
+
+
 def _dist():
     """(rank, world, dist module or None) of a torchrun launch."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -360,12 +367,10 @@ def run_ours(args):
         "vs_baseline": None,
         "dtype": "bf16 tensor-core products, fp32 accumulation and factorizations",
         "data": "synthetic (seeded Haar U, V; s_i = i^-1.5 + 1e-4)",
-        "config": {"workload": "SVD1(QB1(RF1(RS1(SkOpGA, num_pass=4)))) on A 16384x8192 fp32, k=200, over=10",
-                   "global_batch": world, "seq_len": 0,
-                   "parallelism": "single GPU" if world == 1 else f"{world} independent replicas (one RSVD per GPU)",
-                   "l2": "inputs larger than L2 (A = 537 MB)",
-                   "path": "tcgen05 bf16 passes (fp32 accumulate), tensor-core CholeskyQR stabilizer",
-                   "step": "one CUDA-graph replay of the SVD1 call (SVD1.capture), new sketch seed per step"},
+        "config": _config(world),
+        "config_notes": {"l2": "inputs larger than L2 (A = 537 MB)",
+                         "path": "tcgen05 bf16 passes (fp32 accumulate), tensor-core CholeskyQR stabilizer",
+                         "step": "one CUDA-graph replay of the SVD1 call (SVD1.capture), new sketch seed per step"},
         "error": {"frob_err": err, "optimal_tail": tail, "ratio": err / tail,
                   "plain_fp32_ratio": err_plain / tail},
         "plain_fp32_gpu": {"ms_per_step": plain_ms, "speedup": plain_ms / (total_ms / args.steps),
@@ -898,8 +903,8 @@ def run_reference(args):
         "warmup": args.warmup, "ms_per_step": 1e3 / cb["value"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64 (reference promotes f32 input)",
         "data": "synthetic (seeded Haar U, V; s_i = i^-1.5 + 1e-4)", "impl": "reference",
-        "config": {"workload": "SVD1(QB1(RF1(RS1(SkOpGA, num_pass=4)))) on A 16384x8192 fp32, k=200, over=10",
-                   "global_batch": 1, "seq_len": 0, "parallelism": "host cores"},
+        "config": _config(max(1, args.gpus)),
+        "runs_on": "host cores of rank 0 (the GPU only draws the same seeded matrix)",
         "cpu_baseline": cb,
         "e2e": {"value": cb["value"], "unit": "rsvd/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "wall_s": elapsed,
