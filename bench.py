@@ -736,6 +736,23 @@ def bench_ls_batched(torch, pg, count, cpu_budget=0.0):
     out["plain_fp64"] = {"solves_per_s": count / dtp, "ms": dtp * 1e3}
     out["speedup"] = out["batched"]["solves_per_s"] / out["plain_fp64"]["solves_per_s"]
     out["speedup_vs_batched_fp64"] = out["batched"]["solves_per_s"] / out["batched_fp64"]["solves_per_s"]
+    # the iterative-refinement strategy (binary32 LSQR corrections, double-
+    # float residuals, chosen per problem when kappa(R) <= 1e5) against
+    # double-float LSQR for every problem, on the same per-problem eager path
+    # (refine_kappa = 0 turns the refinement off), first 128 problems
+    sub = probs[:128]
+    res = {}
+    for label, rk in (("df_only", 0.0), ("refine_where_kappa_le_1e5", 1e5)):
+        sv = pg.BatchedSPO(precision="mixed", streams=16, strategy="refine", refine_kappa=rk)
+        sv(sub, rng=3)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sv(sub, rng=4)
+        torch.cuda.synchronize()
+        res[label] = {"ms": (time.perf_counter() - t0) * 1e3,
+                      "problems_refined": int(sum(i["strategy"] == "refine" for i in sv.last_info)),
+                      "lsqr_itn_mean": float(np.mean([i["itn"] for i in sv.last_info]))}
+    out["strategy_compare_128"] = dict(res, what="per-problem eager path on the first 128 problems (wall clock)")
     idx = _stratified_sample(shapes, 48)
     worst, worst_p, worst_b, errs = 0.0, 0.0, 0.0, []
     for i in idx:
