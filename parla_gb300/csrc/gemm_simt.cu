@@ -602,11 +602,15 @@ int gram_rows_launch(int64_t N, int64_t K, double alpha, const float* A, int64_t
   if (!ws || !ws_bytes || *ws_bytes < need) return RLA_ERR_WORKSPACE;
   if (N == 0) return RLA_OK;
   const size_t smem = 2 * static_cast<size_t>(kGwKS) * gw_ld(N) * sizeof(float);
-  // one attribute for the largest N, set by the first call (thread-safe static)
-  static const cudaError_t attr = cudaFuncSetAttribute(
-      gram_rows_f32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-      static_cast<int>(2 * kGwKS * gw_ld(kGwMaxN) * sizeof(float)));
-  RLA_CUDA_TRY(attr);
+  // one attribute for the largest N, raised once per device and thread
+  static thread_local int attr_dev = -1;
+  int dev = 0;
+  RLA_CUDA_TRY(cudaGetDevice(&dev));
+  if (attr_dev != dev) {
+    RLA_CUDA_TRY(cudaFuncSetAttribute(gram_rows_f32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      static_cast<int>(2 * kGwKS * gw_ld(kGwMaxN) * sizeof(float))));
+    attr_dev = dev;
+  }
   auto* part = static_cast<float*>(ws);
   gram_rows_f32_kernel<<<static_cast<unsigned>(splits), kGwTh, smem, st>>>(static_cast<int>(N), K, kchunk, A, lda,
                                                                            part);
