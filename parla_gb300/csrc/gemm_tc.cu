@@ -278,19 +278,8 @@ __global__ void tc_splitk_reduce(int64_t M, int64_t N, int splits, const float* 
   int64_t e = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (e >= M * N) return;
   int64_t col = e / M, row = e % M;  // part layout [z][col][row]
-  // slices added in order; the loads of a group of 16 are issued first
-  const float* src = part + col * M + row;
-  const int64_t stride = N * M;
-  constexpr int kU = 16;
   float s = 0.f;
-  for (int z0 = 0; z0 < splits; z0 += kU) {
-    float v[kU];
-#pragma unroll
-    for (int u = 0; u < kU; ++u) v[u] = z0 + u < splits ? __ldcg(src + (z0 + u) * stride) : 0.f;
-#pragma unroll
-    for (int u = 0; u < kU; ++u)
-      if (z0 + u < splits) s += v[u];
-  }
+  for (int z = 0; z < splits; ++z) s += part[(static_cast<int64_t>(z) * N + col) * M + row];
   float* dst = out_trans ? (D + col * ldd + row) : (D + row * ldd + col);
   float r = alpha * s;
   if (beta != 0.f) r = fmaf(beta, *dst, r);
