@@ -230,15 +230,53 @@ potrf_kernel(int64_t n, typename Ar<V>::S* __restrict__ G, int64_t ldg, int* __r
 }
 
 // ------------------------------------------------- triangular inverse
-// X = R^-1, R and X row-major upper triangular; one warp per column of X.
+// X = R^-1, R and X row-major upper triangular; one warp per column of X,
+// back substitution x_i = -(sum_{k > i} R_ik x_k) / R_ii.  With `staged`,
+// the CTA first copies the rows 0..c_last of R it needs (the upper triangle
+// up to its last column, packed by rows) into shared memory in the working
+// precision, with 1/R_ii in place of each diagonal entry, so every step of
+// the chain reads shared memory and multiplies instead of dividing (the
+// binary64 -> double-float conversions leave the chain as well).
+__host__ __device__ inline int64_t trtri_tri_off(int64_t i, int64_t w) { return i * w - i * (i - 1) / 2; }
+
 template <typename V>
 __global__ void trtri_kernel(int64_t n, const typename Ar<V>::S* __restrict__ Rm, int64_t ldr,
-                             typename Ar<V>::S* __restrict__ X, int64_t ldx) {
+                             typename Ar<V>::S* __restrict__ X, int64_t ldx, int staged) {
   using R = Ar<V>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
   V* x = reinterpret_cast<V*>(smem_raw) + static_cast<int64_t>(w) * n;
-  const int64_t c = static_cast<int64_t>(blockIdx.x) * (blockDim.x >> 5) + w;
+  const int64_t c = static_cast<int64_t>(blockIdx.x) * nw + w;
+  if (staged) {
+    // rows 0..cl of R, columns i..cl (row i has cl + 1 - i entries)
+    const int64_t cl = min(n, static_cast<int64_t>(blockIdx.x + 1) * nw) - 1, wd = cl + 1;
+    V* Rs = reinterpret_cast<V*>(smem_raw) + static_cast<int64_t>(nw) * n;
+    // one flat loop over the wd x wd square (rows coalesced, independent
+    // iterations, so loads of several entries are in flight per thread)
+#pragma unroll 4
+    for (int64_t e = threadIdx.x; e < wd * wd; e += blockDim.x) {
+      const int64_t i = e / wd, k = e - i * wd;
+      if (k < i) continue;
+      const V v = R::ld(Rm + i * ldr + k);
+      Rs[trtri_tri_off(i, wd) + (k - i)] = k == i ? R::div(R::one(), v) : v;
+    }
+    __syncthreads();
+    if (c >= n) return;
+    for (int64_t i = lane; i <= c; i += 32) x[i] = R::zero();
+    __syncwarp();
+    if (lane == 0) x[c] = Rs[trtri_tri_off(c, wd)];
+    __syncwarp();
+    for (int64_t i = c - 1; i >= 0; --i) {
+      const V* ri = Rs + trtri_tri_off(i, wd) - i;  // ri[k] = R_ik for i <= k <= cl
+      V acc = R::zero();
+      for (int64_t k = i + 1 + lane; k <= c; k += 32) acc = R::fma(acc, ri[k], x[k]);
+      acc = R::wsum(acc);
+      if (lane == 0) x[i] = R::neg(R::mul(acc, ri[i]));
+      __syncwarp();
+    }
+    for (int64_t i = lane; i < n; i += 32) R::st(X + i * ldx + c, i <= c ? x[i] : R::zero());
+    return;
+  }
   if (c >= n) return;
   for (int64_t i = lane; i <= c; i += 32) x[i] = R::zero();
   __syncwarp();
@@ -631,6 +669,10 @@ int rla_trtri_upper(int dtype, int64_t n, const void* R, int64_t ldr, void* X, i
   size_t vsz = dtype == RLA_F32 ? 4 : 8;
   size_t smem = static_cast<size_t>(warps) * n * vsz;
   if (smem > 200 * 1024) return RLA_ERR_UNSUPPORTED;
+  // stage the packed triangle when it fits beside the per-warp vectors
+  const size_t tri = static_cast<size_t>(n) * (n + 1) / 2 * vsz;
+  const int staged = smem + tri <= 200 * 1024 ? 1 : 0;
+  if (staged) smem += tri;
   static thread_local int attr_dev = -1;
   int dev = 0;
   RLA_CUDA_TRY(cudaGetDevice(&dev));
@@ -642,13 +684,16 @@ int rla_trtri_upper(int dtype, int64_t n, const void* R, int64_t ldr, void* X, i
   }
   switch (dtype) {
     case RLA_F64:
-      trtri_kernel<double><<<grid, warps * 32, smem, st>>>(n, static_cast<const double*>(R), ldr, static_cast<double*>(X), ldx);
+      trtri_kernel<double><<<grid, warps * 32, smem, st>>>(n, static_cast<const double*>(R), ldr, static_cast<double*>(X), ldx,
+                                                          staged);
       break;
     case RLA_DF:
-      trtri_kernel<df><<<grid, warps * 32, smem, st>>>(n, static_cast<const double*>(R), ldr, static_cast<double*>(X), ldx);
+      trtri_kernel<df><<<grid, warps * 32, smem, st>>>(n, static_cast<const double*>(R), ldr, static_cast<double*>(X), ldx,
+                                                          staged);
       break;
     case RLA_F32:
-      trtri_kernel<float><<<grid, warps * 32, smem, st>>>(n, static_cast<const float*>(R), ldr, static_cast<float*>(X), ldx);
+      trtri_kernel<float><<<grid, warps * 32, smem, st>>>(n, static_cast<const float*>(R), ldr, static_cast<float*>(X), ldx,
+                                                          staged);
       break;
     default: return RLA_ERR_ARG;
   }
