@@ -446,10 +446,22 @@ def gemm_tn_panel(W, X, tri=False, want_bf16=False, sdiv=None):
     return (Y, Yb) if want_bf16 else Y
 
 
-def flags_any(flags, s=None, smin=0.0):
-    """Device int32 [1]: 1 if any flag is non-zero or any s is below smin
-    (``rla_flags_any``, one launch)."""
-    out = torch.empty(1, dtype=torch.int32, device=device())
+def copy_u64(src, dst):
+    """dst <- src (64-bit words) by a kernel (``rla_copy_u64``); either may be
+    a pinned host tensor."""
+    assert src.numel() * src.element_size() == dst.numel() * dst.element_size()
+    assert src.element_size() * src.numel() % 8 == 0 and src.is_contiguous() and dst.is_contiguous()
+    _timed("copy_u64", 1, call, "rla_copy_u64", ptr(src), ptr(dst), src.numel() * src.element_size() // 8,
+           stream())
+    return dst
+
+
+def flags_any(flags, s=None, smin=0.0, out=None):
+    """int32 [1]: 1 if any flag is non-zero or any s is below smin
+    (``rla_flags_any``, one launch).  ``out`` may be a pinned host tensor
+    (written over the host link)."""
+    if out is None:
+        out = torch.empty(1, dtype=torch.int32, device=device())
     nf = 0 if flags is None else flags.numel()
     if s is not None:
         s = s if (s.dtype == torch.float32 and s.is_contiguous()) else s.float().contiguous()

@@ -59,6 +59,7 @@ SIGNATURES = {
     "rla_gram_f32_df": [_i32, _i64, _i64, _p, _i64, _p, _i64, _p, _psz, _p],
     "rla_gemm_tn_panel_f32": [_i32, _i64, _i64, _i64, _p, _i64, _p, _i64, _p, _i64, _p, _i64, _p, _p],
     "rla_flags_any": [_p, _i64, _p, _i64, C.c_float, _p, _p],
+    "rla_copy_u64": [_p, _p, _i64, _p],
     "rla_gemm_bf16_tc": [_i64, _i64, _i64, _p, _i64, _p, _i64, _p, _i64, _i32, C.c_float, C.c_float, _i32,
                          _p, _psz, _p],
     "rla_gemm_bf16_tc_status": [_p, C.POINTER(C.c_int), _p],

@@ -197,6 +197,27 @@ __global__ void split_f64_kernel(int64_t rows, int64_t cols, const double* __res
 }  // namespace
 }  // namespace rla
 
+// dst[i] = src[i] for n 64-bit words by a kernel (one CTA): either side may be
+// page-locked host memory, read or written over the host link, so a captured
+// graph moves its few control words without a copy-engine node (which would
+// queue behind a large host copy on another stream).
+namespace rla {
+namespace {
+__global__ void copy_u64_kernel(const uint64_t* __restrict__ src, uint64_t* __restrict__ dst, int64_t n) {
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i];
+}
+}  // namespace
+}  // namespace rla
+
+extern "C" int rla_copy_u64(const void* src, void* dst, int64_t n, rla_stream_t stream) {
+  if (n < 0 || (n > 0 && (!src || !dst))) return RLA_ERR_ARG;
+  if (n == 0) return RLA_OK;
+  rla::copy_u64_kernel<<<1, 128, 0, reinterpret_cast<cudaStream_t>(stream)>>>(static_cast<const uint64_t*>(src),
+                                                                              static_cast<uint64_t*>(dst), n);
+  RLA_LAUNCH_CHECK();
+  return RLA_OK;
+}
+
 // x = hi + lo to about 2^-48 relative: the double-float image of an FP64 matrix.
 extern "C" int rla_split_f64(int64_t rows, int64_t cols, const double* x, int64_t ldx, float* hi, float* lo,
                              int64_t ldh, rla_stream_t stream) {

@@ -194,7 +194,10 @@ chol_inv_kernel(int n, const float* __restrict__ G, int64_t ldg, float* __restri
 
   for (int r = warp; r < n; r += nw)
     for (int c = lane; c < LD; c += 32) a[r * LD + c] = (c >= r && c < n) ? G[static_cast<int64_t>(r) * ldg + c] : 0.f;
-  if (tid == 0) s_bad = 0;
+  if (tid == 0) {
+    s_bad = 0;
+    *info = 0;  // (written here, not by a memset before the launch; failures overwrite it below)
+  }
   __syncthreads();
   if (group_a) ci_factor_block<INV>(a, P0, Dv, dl, &s_bad, LD, n, 0, tid);
   __syncthreads();
@@ -266,8 +269,10 @@ extern "C" int rla_chol_inv_f32(int64_t n, const float* G, int64_t ldg, float* R
   if (n < 0 || ldg < n || (Rinv && ldr < n) || (R && ldro < n) || !info || (!Rinv && !R)) return RLA_ERR_ARG;
   if (n > kCholInvMax) return RLA_ERR_UNSUPPORTED;
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-  RLA_CUDA_TRY(cudaMemsetAsync(info, 0, sizeof(int), st));
-  if (n == 0) return RLA_OK;
+  if (n == 0) {
+    RLA_CUDA_TRY(cudaMemsetAsync(info, 0, sizeof(int), st));
+    return RLA_OK;
+  }
   if (!G) return RLA_ERR_ARG;
   const size_t smem = ci_smem_bytes(static_cast<int>(n));
   const int rc = ci_attributes();
@@ -288,8 +293,10 @@ extern "C" int rla_chol_f32_checked(int64_t n, const float* G, int64_t ldg, floa
   if (n < 0 || ldg < n || ldr < n || !info || !R) return RLA_ERR_ARG;
   if (n > kCholInvMax) return RLA_ERR_UNSUPPORTED;
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-  RLA_CUDA_TRY(cudaMemsetAsync(info, 0, sizeof(int), st));
-  if (n == 0) return RLA_OK;
+  if (n == 0) {
+    RLA_CUDA_TRY(cudaMemsetAsync(info, 0, sizeof(int), st));
+    return RLA_OK;
+  }
   if (!G) return RLA_ERR_ARG;
   const int rc = ci_attributes();
   if (rc != RLA_OK) return rc;

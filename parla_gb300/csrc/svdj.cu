@@ -699,8 +699,10 @@ extern "C" int rla_svd_jacobi(int dtype, int64_t n, const void* Ct, int64_t ldc,
   if (dtype != RLA_F32) return RLA_ERR_UNSUPPORTED;
   if (n > kJacMaxN) return RLA_ERR_UNSUPPORTED;
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-  RLA_CUDA_TRY(cudaMemsetAsync(info, 0, 2 * sizeof(int), st));
-  if (n == 0) return RLA_OK;
+  if (n == 0) {  // (the kernels write both status words themselves)
+    RLA_CUDA_TRY(cudaMemsetAsync(info, 0, 2 * sizeof(int), st));
+    return RLA_OK;
+  }
   if (!Ct || !U || !s) return RLA_ERR_ARG;
   if (cluster == 0) {
     // block Jacobi: up to 8 CTAs, two blocks of b columns each

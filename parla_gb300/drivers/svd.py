@@ -103,6 +103,9 @@ class SVDReplay:
         hout = tuple(torch.empty(sh, dtype=torch.float32).pin_memory() for sh in ((m, k), (k,), (k, n))) \
             if self.host else None
         self.slots = usk.SeedSlots()
+        # the deferred checks' verdict, written by the graph's last kernel
+        # straight into pinned host memory (no copy-engine node)
+        self.bad_host = torch.zeros(1, dtype=torch.int32).pin_memory()
         self.graph = torch.cuda.CUDAGraph()
         eps10 = 10 * np.finfo(float).eps
         with opd.deferred_checks() as chk, usk.recording(self.slots):
@@ -111,14 +114,13 @@ class SVDReplay:
                 Am = opd.wrap(A, svd.precision)         # inside: the bf16 images are part of the graph
                 U, s, Vh = svd._run(A, Am, k, tol, over, gen, graph=True)
                 # every deferred check and the s < 10 eps test, one launch
-                self.bad = K.flags_any(chk.all_flags(), s, eps10)
+                K.flags_any(chk.all_flags(), s, eps10, out=self.bad_host)
                 if self.host:
                     self.out = hout
                     for h, t in zip(self.out, (U, s, Vh)):
                         h.copy_(t, non_blocking=True)
                 else:
                     self.out = (U, s, Vh)
-        self.bad_host = torch.zeros(1, dtype=torch.int32).pin_memory()
         self.done = torch.cuda.Event()
         self.last_rng = rng
 
@@ -128,7 +130,6 @@ class SVDReplay:
         self.last_rng = self.rng if rng is None else rng
         self.slots.set_from(self.last_rng)
         self.graph.replay()
-        self.bad_host.copy_(self.bad, non_blocking=True)
         self.done.record()
 
     def failed(self):

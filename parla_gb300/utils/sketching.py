@@ -32,9 +32,12 @@ class SeedSlots:
     While ``recording(slots)`` is active, every device draw of a seed still
     consumes the caller's Generator exactly as an eager call does, but hands
     the operator a one-word device tensor instead of the integer; the graph
-    captures a copy into that word from a pinned host word, so a replay draws
-    the sketch of whatever seed the host wrote there (``set_from``).  Slots
-    are allocated up front: nothing is allocated on the host while capturing.
+    captures a copy into that word from a pinned host word (by a one-CTA
+    kernel reading host memory, not a copy-engine node, so the replay does
+    not queue behind a large host copy on another stream), and a replay
+    draws the sketch of whatever seed the host wrote there (``set_from``).
+    Slots are allocated up front: nothing is allocated on the host while
+    capturing.
     """
 
     def __init__(self, count=4):
@@ -48,7 +51,7 @@ class SeedSlots:
         h, d = self.host[self.used], self.dev[self.used]
         self.used += 1
         h[0] = seed - (1 << 64) if seed >= (1 << 63) else seed
-        d.copy_(h, non_blocking=True)
+        K.copy_u64(h, d)
         return d
 
     def set_from(self, rng):
