@@ -336,8 +336,15 @@ __global__ void __launch_bounds__(512, 1) svd_jacobi_f32_kernel(JacArgs a) {
 // kernel (top[0] stays, top[k] -> top[k+1], top[P-1] -> bottom[P-1],
 // bottom[k] -> bottom[k-1], bottom[0] -> top[1]) through distributed shared
 // memory, one cluster barrier.  Every pair of columns meets once per sweep,
-// with 2 cs - 1 cluster barriers instead of ~n.  Lane l of a half-warp holds
-// rows l E .. l E + E - 1 of a column (64-bit shared-memory accesses).
+// with 2 cs - 1 cluster barriers instead of ~n.
+//
+// A group of L lanes (a half-warp; the kernel also takes L = 32) owns a
+// pair; lane l holds E elements of each column, interleaved so that the
+// group's accesses are consecutive: element e of lane l is row
+// (e / 2) 2 L + 2 l + e % 2 for even E (64-bit accesses), row e L + l for
+// odd E.  In the cross rounds, pair i keeps its top
+// column A_i for all b local rounds, so the group holds it (and its squared
+// norm) in registers and writes it back once at the end of the outer round.
 struct JacBArgs {
   int n, b, cs;
   const float* Ct;
@@ -350,40 +357,51 @@ struct JacBArgs {
   float tol;
 };
 
-// A lane's E consecutive elements of a column slot: 64-bit shared-memory
-// accesses when E is even (slots start on 32-byte boundaries).
-template <int E>
-__device__ __forceinline__ void jac_load(float (&v)[E], const float* p, bool act) {
+// word of a column slot that holds element e of lane l
+template <int E, int L>
+__device__ __forceinline__ int jac_word(int l, int e) {
+  if constexpr (E % 2 == 0) return (e >> 1) * (2 * L) + 2 * l + (e & 1);
+  else return e * L + l;
+}
+
+// a lane's E elements of a column slot (64-bit accesses when E is even; the
+// slots start on 8-byte boundaries)
+template <int E, int L>
+__device__ __forceinline__ void jac_load(float (&v)[E], const float* p, int l, bool act) {
   if constexpr (E % 2 == 0) {
 #pragma unroll
     for (int e = 0; e < E; e += 2) {
-      const float2 w = act ? reinterpret_cast<const float2*>(p)[e / 2] : make_float2(0.f, 0.f);
+      const float2 w = act ? reinterpret_cast<const float2*>(p)[(e >> 1) * L + l] : make_float2(0.f, 0.f);
       v[e] = w.x;
       v[e + 1] = w.y;
     }
   } else {
 #pragma unroll
-    for (int e = 0; e < E; ++e) v[e] = act ? p[e] : 0.f;
+    for (int e = 0; e < E; ++e) v[e] = act ? p[e * L + l] : 0.f;
   }
 }
-template <int E>
-__device__ __forceinline__ void jac_store(float* p, const float (&v)[E]) {
+template <int E, int L>
+__device__ __forceinline__ void jac_store(float* p, int l, const float (&v)[E]) {
   if constexpr (E % 2 == 0) {
 #pragma unroll
-    for (int e = 0; e < E; e += 2) reinterpret_cast<float2*>(p)[e / 2] = make_float2(v[e], v[e + 1]);
+    for (int e = 0; e < E; e += 2) reinterpret_cast<float2*>(p)[(e >> 1) * L + l] = make_float2(v[e], v[e + 1]);
   } else {
 #pragma unroll
-    for (int e = 0; e < E; ++e) p[e] = v[e];
+    for (int e = 0; e < E; ++e) p[e * L + l] = v[e];
   }
 }
 
-template <int E>
+template <int E, int L>
 __global__ void __launch_bounds__(512, 1) svd_jacobi_block_kernel(JacBArgs a) {
+  static_assert(L == 16 || L == 32, "a pair's lane group is a half-warp or a warp");
+  constexpr int G = 32 / L;          // lane groups per warp
+  constexpr int LD = L * E + 8;      // slot: L E elements, squared norm at word L E
+  constexpr unsigned kFull = 0xffffffffu;
   cg::cluster_group cluster = cg::this_cluster();
   const int rank = static_cast<int>(cluster.block_rank());
-  const int tid = threadIdx.x, lane = tid & 31, hl = lane & 15, half = lane >> 4, warp = tid >> 5;
-  const int hw = 2 * warp + half;
-  constexpr int LD = 16 * E + 8;
+  const int tid = threadIdx.x, lane = tid & 31, hl = lane & (L - 1), half = lane / L, warp = tid >> 5;
+  const int nwarps = static_cast<int>(blockDim.x >> 5);
+  const int hw = G * warp + half;    // lane group index
   const int b = a.b, b2 = 2 * b, N = 2 * a.cs * b;
   extern __shared__ __align__(16) float sm[];
   float* cols = sm;                                                   // [2 buf][2b slots][LD]
@@ -392,12 +410,12 @@ __global__ void __launch_bounds__(512, 1) svd_jacobi_block_kernel(JacBArgs a) {
   float* sig = reinterpret_cast<float*>(total + 4);                   // [N] (rank 0)
   auto slot = [&](int buf, int sl) { return cols + (buf * b2 + sl) * LD; };
 
-  for (int sl = hw; sl < b2; sl += 2 * (blockDim.x >> 5)) {
+  for (int sl = hw; sl < b2; sl += G * nwarps) {
     const int c = (2 * rank + (sl >= b ? 1 : 0)) * b + (sl >= b ? sl - b : sl);
     float* dst = slot(0, sl);
 #pragma unroll
     for (int e = 0; e < E; ++e) {
-      const int i = hl * E + e;
+      const int i = jac_word<E, L>(hl, e);
       dst[i] = (c < a.n && i < a.n) ? a.Ct[static_cast<int64_t>(c) * a.ldc + i] : 0.f;
     }
     if (hl == 0) ids[sl] = c;
@@ -422,8 +440,8 @@ __global__ void __launch_bounds__(512, 1) svd_jacobi_block_kernel(JacBArgs a) {
   unsigned seen = 0, rotated = 0;
   int cur = 0, sweeps = 0;
   bool converged = false;
-  // squared norm of a half-warp's column (E elements per lane, xor tree)
-  auto hw_norm2 = [&](const float (&v)[E]) {
+  // squared norm of a lane group's column (E elements per lane, xor tree)
+  auto grp_norm2 = [&](const float (&v)[E]) {
     float n0 = 0.f, n1 = 0.f;
 #pragma unroll
     for (int e = 0; e < E; e += 2) {
@@ -432,42 +450,49 @@ __global__ void __launch_bounds__(512, 1) svd_jacobi_block_kernel(JacBArgs a) {
     }
     float nn = n0 + n1;
 #pragma unroll
-    for (int o = 8; o > 0; o >>= 1) nn += __shfl_xor_sync(0xffffffffu, nn, o);
-    return __shfl_sync(0xffffffffu, nn, half * 16);
+    for (int o = L / 2; o > 0; o >>= 1) nn += __shfl_xor_sync(kFull, nn, o);
+    return __shfl_sync(kFull, nn, half * L);
   };
+  const bool act = hw < b;  // a pair in every local round
   while (!converged && sweeps < a.max_sweeps) {
-    // Each slot carries its column's squared norm in its padding (word 16 E),
+    // Each slot carries its column's squared norm in its padding (word L E),
     // so it travels with the column between CTAs.  Exact at the start of a
     // sweep; a rotation updates the pair's norms by app - t apq, aqq + t apq
     // (recomputed from the rotated columns when either drops below a quarter).
-    for (int sb = 2 * warp; sb < b2; sb += 2 * (blockDim.x >> 5)) {  // warp-uniform trip count
+    for (int sb = G * warp; sb < b2; sb += G * nwarps) {  // warp-uniform trip count
       const int sl = sb + half;
       float v[E];
-      jac_load<E>(v, slot(cur, sl < b2 ? sl : 0) + hl * E, sl < b2);
-      const float nn = hw_norm2(v);
-      if (sl < b2 && hl == 0) slot(cur, sl)[16 * E] = nn;
+      jac_load<E, L>(v, slot(cur, sl < b2 ? sl : 0), hl, sl < b2);
+      const float nn = grp_norm2(v);
+      if (sl < b2 && hl == 0) slot(cur, sl)[L * E] = nn;
     }
     __syncthreads();
     for (int orr = 0; orr < 2 * P - 1; ++orr) {
-      const int lrounds = orr == 0 ? b2 - 1 : b;
+      const bool cross = orr > 0;  // the top column stays with its group
+      const int lrounds = cross ? b : b2 - 1;
       // pair indices of round r, advanced by one per round (no division):
       // first outer round ps = 1 + (hw - 1 + r) mod (2b - 1) (0 for hw = 0),
       // qs = 1 + (2b - 2 - hw + r) mod (2b - 1); later ones ps = hw,
       // qs = b + (hw + r) mod b
-      const int wrap = orr == 0 ? b2 - 1 : b;
-      int mp = hw == 0 ? 0 : hw - 1, mq = orr == 0 ? b2 - 2 - hw : hw;
+      const int wrap = cross ? b : b2 - 1;
+      int mp = hw == 0 ? 0 : hw - 1, mq = cross ? hw : b2 - 2 - hw;
+      float x[E];
+      float xn = 1.f;  // squared norm of x in the cross rounds
+      if (cross) {
+        jac_load<E, L>(x, slot(cur, act ? hw : 0), hl, act);
+        xn = act ? slot(cur, hw)[L * E] : 1.f;
+      }
       for (int r = 0; r < lrounds; ++r) {
-        const bool act = hw < b;
-        const int ps = orr == 0 ? (hw == 0 ? 0 : 1 + mp) : hw;
-        const int qs = orr == 0 ? 1 + mq : b + mq;
+        const int ps = cross ? hw : (hw == 0 ? 0 : 1 + mp);
+        const int qs = cross ? b + mq : 1 + mq;
         if (++mp == wrap) mp = 0;
         if (++mq == wrap) mq = 0;
         float* sx = slot(cur, act ? ps : 0);
         float* sy = slot(cur, act ? qs : 0);
-        float x[E], y[E];
-        jac_load<E>(x, sx + hl * E, act);
-        jac_load<E>(y, sy + hl * E, act);
-        const float app = act ? sx[16 * E] : 1.f, aqq = act ? sy[16 * E] : 1.f;
+        float y[E];
+        if (!cross) jac_load<E, L>(x, sx, hl, act);
+        jac_load<E, L>(y, sy, hl, act);
+        const float app = cross ? xn : (act ? sx[L * E] : 1.f), aqq = act ? sy[L * E] : 1.f;
         float apq0 = 0.f, apq1 = 0.f;
 #pragma unroll
         for (int e = 0; e < E; e += 2) {
@@ -476,8 +501,8 @@ __global__ void __launch_bounds__(512, 1) svd_jacobi_block_kernel(JacBArgs a) {
         }
         float apq = apq0 + apq1;
 #pragma unroll
-        for (int o = 8; o > 0; o >>= 1) apq += __shfl_xor_sync(0xffffffffu, apq, o);
-        apq = __shfl_sync(0xffffffffu, apq, half * 16);
+        for (int o = L / 2; o > 0; o >>= 1) apq += __shfl_xor_sync(kFull, apq, o);
+        apq = __shfl_sync(kFull, apq, half * L);
         const bool rot = act && apq * apq > tol2 * app * aqq;
         float np = app, nq = aqq;
         bool renorm = false;
@@ -501,24 +526,32 @@ __global__ void __launch_bounds__(512, 1) svd_jacobi_block_kernel(JacBArgs a) {
             x[e] = fmaf(-sn, fmaf(tau, xe, ye), xe);
             y[e] = fmaf(sn, fmaf(-tau, ye, xe), ye);
           }
-          jac_store<E>(sx + hl * E, x);
-          jac_store<E>(sy + hl * E, y);
+          if (!cross) jac_store<E, L>(sx, hl, x);
+          jac_store<E, L>(sy, hl, y);
           np = fmaf(-t, apq, app);
           nq = fmaf(t, apq, aqq);
-          renorm = np < 0.25f * app || nq < 0.25f * aqq;  // same in every lane of the half-warp
+          renorm = np < 0.25f * app || nq < 0.25f * aqq;  // same in every lane of the group
           if (hl == 0) ++rotated;
         }
-        // (shuffles outside the divergent branch: the two half-warps differ)
-        if (__any_sync(0xffffffffu, renorm)) {
-          const float rp = hw_norm2(x), rq = hw_norm2(y);
+        // (shuffles outside the divergent branch: the groups of a warp differ)
+        if (__any_sync(kFull, renorm)) {
+          const float rp = grp_norm2(x), rq = grp_norm2(y);
           if (renorm) {
             np = rp;
             nq = rq;
           }
         }
         if (rot && hl == 0) {
-          sx[16 * E] = np;
-          sy[16 * E] = nq;
+          if (!cross) sx[L * E] = np;
+          sy[L * E] = nq;
+        }
+        if (cross) xn = np;  // (np = app without a rotation)
+        __syncthreads();
+      }
+      if (cross) {
+        if (act) {
+          jac_store<E, L>(slot(cur, hw), hl, x);
+          if (hl == 0) slot(cur, hw)[L * E] = xn;
         }
         __syncthreads();
       }
@@ -552,44 +585,44 @@ __global__ void __launch_bounds__(512, 1) svd_jacobi_block_kernel(JacBArgs a) {
   }
 
   // singular values: norms of the final columns; rank them (descending)
-  for (int sb = 2 * warp; sb < b2; sb += 2 * (blockDim.x >> 5)) {
+  for (int sb = G * warp; sb < b2; sb += G * nwarps) {
     const int sl = sb + half;
-    const bool act = sl < b2;
+    const bool on = sl < b2;
     float nn = 0.f;
 #pragma unroll
     for (int e = 0; e < E; ++e) {
-      const float v = act ? slot(cur, sl)[hl * E + e] : 0.f;
+      const float v = on ? slot(cur, sl)[jac_word<E, L>(hl, e)] : 0.f;
       nn = fmaf(v, v, nn);
     }
 #pragma unroll
-    for (int o = 8; o > 0; o >>= 1) nn += __shfl_xor_sync(0xffffffffu, nn, o);
-    nn = __shfl_sync(0xffffffffu, nn, half * 16);
-    if (act && hl == 0) {
+    for (int o = L / 2; o > 0; o >>= 1) nn += __shfl_xor_sync(kFull, nn, o);
+    nn = __shfl_sync(kFull, nn, half * L);
+    if (on && hl == 0) {
       const int id = ids[cur * b2 + sl];
       cluster.map_shared_rank(sig, 0)[id] = id < a.n ? sqrtf(nn) : -1.f;
     }
   }
   cluster.sync();
   const float* sig0 = cluster.map_shared_rank(sig, 0);
-  for (int sb = 2 * warp; sb < b2; sb += 2 * (blockDim.x >> 5)) {
+  for (int sb = G * warp; sb < b2; sb += G * nwarps) {
     const int sl = sb + half;
     const int id = sl < b2 ? ids[cur * b2 + sl] : a.n;
-    const bool act = id < a.n;
-    const float sv = act ? sig0[id] : 0.f;
+    const bool on = id < a.n;
+    const float sv = on ? sig0[id] : 0.f;
     int cnt = 0;
-    if (act)
-      for (int i = hl; i < N; i += 16) {
+    if (on)
+      for (int i = hl; i < N; i += L) {
         const float o = sig0[i];
         cnt += (o > sv || (o == sv && i < id)) ? 1 : 0;
       }
 #pragma unroll
-    for (int o = 8; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
-    if (act) {
+    for (int o = L / 2; o > 0; o >>= 1) cnt += __shfl_xor_sync(kFull, cnt, o);
+    if (on) {
       const float* col = slot(cur, sl);
       const float inv = sv > 0.f ? 1.f / sv : 0.f;
 #pragma unroll
       for (int e = 0; e < E; ++e) {
-        const int i = hl * E + e;
+        const int i = jac_word<E, L>(hl, e);
         if (i < a.n) a.U[static_cast<int64_t>(i) * a.ldu + cnt] = col[i] * inv;
       }
       if (hl == 0) a.s[cnt] = sv;
@@ -602,20 +635,22 @@ __global__ void __launch_bounds__(512, 1) svd_jacobi_block_kernel(JacBArgs a) {
   cluster.sync();  // peers read rank 0's shared memory above
 }
 
-template <int E>
+template <int E, int L>
 int launch_jacobi_block(JacBArgs a, cudaStream_t st) {
-  constexpr int LD = 16 * E + 8;
+  constexpr int LD = L * E + 8;
   const int N = 2 * a.cs * a.b;
   const size_t smem = static_cast<size_t>(2 * 2 * a.b) * LD * sizeof(float) + 2 * 2 * a.b * sizeof(int) +
                       4 * sizeof(unsigned) + static_cast<size_t>(N) * sizeof(float);
   if (smem > 225 * 1024) return RLA_ERR_UNSUPPORTED;
-  const int threads = 32 * (a.b < 4 ? 2 : (a.b + 1) / 2);
+  // one lane group per pair, at least two warps
+  const int groups = a.b < 2 * (32 / L) ? 2 * (32 / L) : a.b;
+  const int threads = 32 * ((groups + 32 / L - 1) / (32 / L));
   if (threads > 512) return RLA_ERR_UNSUPPORTED;
   static thread_local int attr_dev = -1;
   int dev = 0;
   RLA_CUDA_TRY(cudaGetDevice(&dev));
   if (attr_dev != dev) {
-    RLA_CUDA_TRY(cudaFuncSetAttribute(svd_jacobi_block_kernel<E>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    RLA_CUDA_TRY(cudaFuncSetAttribute(svd_jacobi_block_kernel<E, L>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       225 * 1024));
     attr_dev = dev;
   }
@@ -631,7 +666,7 @@ int launch_jacobi_block(JacBArgs a, cudaStream_t st) {
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  RLA_CUDA_TRY(cudaLaunchKernelEx(&cfg, svd_jacobi_block_kernel<E>, a));
+  RLA_CUDA_TRY(cudaLaunchKernelEx(&cfg, svd_jacobi_block_kernel<E, L>, a));
   return RLA_OK;
 }
 
@@ -719,19 +754,22 @@ extern "C" int rla_svd_jacobi(int dtype, int64_t n, const void* Ct, int64_t ldc,
     ab.info = info;
     ab.max_sweeps = max_sweeps;
     ab.tol = 2.0f * 5.96e-8f * sqrtf(static_cast<float>(n));
+    // a half-warp per pair: a warp per pair (L = 32) measured slower at
+    // n = 210 (0.97 against 0.89 ms): twice the warps repeat the per-pair
+    // angle, reductions and barrier arrivals
     const int ept = static_cast<int>((n + 15) / 16);
-    if (ept <= 1) return launch_jacobi_block<1>(ab, st);
-    if (ept <= 2) return launch_jacobi_block<2>(ab, st);
-    if (ept <= 4) return launch_jacobi_block<4>(ab, st);
-    if (ept <= 6) return launch_jacobi_block<6>(ab, st);
-    if (ept <= 8) return launch_jacobi_block<8>(ab, st);
-    if (ept <= 10) return launch_jacobi_block<10>(ab, st);
-    if (ept <= 12) return launch_jacobi_block<12>(ab, st);
-    if (ept <= 14) return launch_jacobi_block<14>(ab, st);
-    if (ept <= 16) return launch_jacobi_block<16>(ab, st);
-    if (ept <= 20) return launch_jacobi_block<20>(ab, st);
-    if (ept <= 24) return launch_jacobi_block<24>(ab, st);
-    return launch_jacobi_block<28>(ab, st);
+    if (ept <= 1) return launch_jacobi_block<1, 16>(ab, st);
+    if (ept <= 2) return launch_jacobi_block<2, 16>(ab, st);
+    if (ept <= 4) return launch_jacobi_block<4, 16>(ab, st);
+    if (ept <= 6) return launch_jacobi_block<6, 16>(ab, st);
+    if (ept <= 8) return launch_jacobi_block<8, 16>(ab, st);
+    if (ept <= 10) return launch_jacobi_block<10, 16>(ab, st);
+    if (ept <= 12) return launch_jacobi_block<12, 16>(ab, st);
+    if (ept <= 14) return launch_jacobi_block<14, 16>(ab, st);
+    if (ept <= 16) return launch_jacobi_block<16, 16>(ab, st);
+    if (ept <= 20) return launch_jacobi_block<20, 16>(ab, st);
+    if (ept <= 24) return launch_jacobi_block<24, 16>(ab, st);
+    return launch_jacobi_block<28, 16>(ab, st);
   }
   JacArgs a;
   a.n = static_cast<int>(n);
