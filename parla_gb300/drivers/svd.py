@@ -123,14 +123,22 @@ class SVDReplay:
                     self.out = (U, s, Vh)
         self.done = torch.cuda.Event()
         self.last_rng = rng
+        self.inflight = False
 
     def launch(self, rng=None):
-        """Enqueue one replay on the current stream (no synchronisation); the
-        outputs and the deferred checks' flag are ready when ``done`` is."""
+        """Enqueue one replay on the current stream; the outputs and the
+        deferred checks' flag are ready when ``done`` is.  The graph reads its
+        seed words from pinned host memory while it runs, so a launch first
+        waits for the previous replay of this graph (if still in flight)
+        before it writes them: back-to-back launches each draw their own
+        sketch."""
+        if self.inflight:
+            self.done.synchronize()
         self.last_rng = self.rng if rng is None else rng
         self.slots.set_from(self.last_rng)
         self.graph.replay()
         self.done.record()
+        self.inflight = True
 
     def failed(self):
         """After ``done``: True when the replay's deferred checks failed."""

@@ -143,3 +143,32 @@ def test_make_problem_conditioning_on_cpu():
     assert math.isclose(float(np.linalg.cond(A.numpy())), 1e6, rel_tol=1e-6)
     r = b.numpy() - A.numpy() @ x.numpy()
     assert np.linalg.norm(r) == pytest.approx(1e-3 * np.linalg.norm(A.numpy() @ x.numpy()), rel=1e-12)
+
+
+def test_replay_launch_waits_before_rewriting_seed_words():
+    """A captured RSVD reads its seed words from pinned host memory while it
+    runs: a second launch must wait for the first replay before writing them."""
+    from parla_gb300.drivers.svd import SVDReplay
+    log = []
+
+    class Event:
+        def synchronize(self):
+            log.append("wait")
+
+        def record(self):
+            log.append("record")
+
+    class Slots:
+        def set_from(self, rng):
+            log.append(("seed", rng))
+
+    class Graph:
+        def replay(self):
+            log.append("replay")
+
+    rep = object.__new__(SVDReplay)
+    rep.rng, rep.slots, rep.graph, rep.done, rep.inflight = 7, Slots(), Graph(), Event(), False
+    rep.launch(1)
+    rep.launch(None)
+    assert log == [("seed", 1), "replay", "record", "wait", ("seed", 7), "replay", "record"]
+    assert rep.last_rng == 7
