@@ -545,14 +545,15 @@ int rla_convert_bf16_pair(int src_dtype, int64_t rows, int64_t cols,
 /* hi (float) + lo (float) = x (double) to about 2^-48 relative; the planes
  * share the row stride ldh.  Prepares A for the double-float LSQR and GEMM
  * paths (no reference counterpart: GB300-specific data layout). */
+int rla_split_f64(int64_t rows, int64_t cols, const double* x, int64_t ldx,
+                  float* hi, float* lo, int64_t ldh, rla_stream_t stream);
+
 /* dst[i] = src[i] for n 64-bit words by a kernel; either pointer may be
  * page-locked host memory (read or written over the host link), so a
  * captured CUDA graph moves its control words (sketch seeds, status flags)
- * without a copy-engine node. */
+ * without a copy-engine node (no reference counterpart: the reference draws
+ * its seeds on the host, parla/utils/sketching.py:20-31). */
 int rla_copy_u64(const void* src, void* dst, int64_t n, rla_stream_t stream);
-
-int rla_split_f64(int64_t rows, int64_t cols, const double* x, int64_t ldx,
-                  float* hi, float* lo, int64_t ldh, rla_stream_t stream);
 
 
 /* ------------------------------------------------------------------------
