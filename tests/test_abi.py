@@ -54,6 +54,16 @@ def test_argument_errors_need_no_gpu(lib):
                             None, None, None) == 1
     assert _lib.call_status("rla_sjlt_pattern", 4, 10, 8, 1, None, None, None) == 1  # nnz > d
     assert _lib.call_status("rla_trtri_upper", 0, 3, None, 3, None, 3, None) == 1
+    # the control-word kernels of a captured call: sizes and pointers checked
+    # before the launch; an empty copy launches nothing
+    assert _lib.call_status("rla_copy_u64", None, None, -1, None) == 1
+    assert _lib.call_status("rla_copy_u64", None, None, 2, None) == 1
+    assert _lib.call_status("rla_copy_u64", None, None, 0, None) == 0
+    assert _lib.call_status("rla_flags_any", None, 1, None, 0, 0.0, None, None) == 1   # no output word
+    assert _lib.call_status("rla_flags_any", None, -1, None, 0, 0.0, None, None) == 1
+    assert _lib.call_status("rla_chol_f32_checked", -1, None, 1, None, 1, 0.5, None, None) == 1
+    assert _lib.call_status("rla_chol_f32_checked", 300, None, 300, None, 300, 0.5, None, None) == 1  # no info
+    assert _lib.call_status("rla_svd_jacobi", 1, 3, None, 3, None, 3, None, None, 40, 9, None) == 1  # cluster > 8
 
 
 def test_sliced_digit_plan_needs_no_gpu(lib):
